@@ -1,0 +1,285 @@
+/*
+ * tensorf_gb300.h -- C ABI of the GB300 (sm_103a) TensoRF-VM render-and-train path.
+ *
+ * Every entry point:
+ *   - takes caller-owned DEVICE pointers (plain pointers, element counts), a POD
+ *     descriptor where the shape is more than a couple of integers, and a
+ *     cudaStream_t passed as `void*` (NULL = legacy default stream);
+ *   - validates shapes, dtypes, alignment and null pointers on the host and returns
+ *     a negative TVM_ERR_* code before launching anything when they are wrong, with
+ *     a message readable through tvm_last_error_message() (per calling thread);
+ *   - allocates nothing: scratch comes from a caller buffer sized by the matching
+ *     *_workspace_size() call;
+ *   - keeps no global mutable state besides the per-thread error message, so calls
+ *     on distinct streams from distinct threads are independent.
+ *
+ * Layouts (device memory). Field tensors are CHANNEL-LAST:
+ *   lines  [3][G][C]     element (m, x, c)        at (m*G + x)*C + c
+ *   planes [3][G][G][C]  element (m, row, col, c) at ((m*G + row)*G + col)*C + c
+ * The reference stores TensorVMSingle.vector as (3, C, G) and .matrix as (3, C, G, G)
+ * (tensorf/tensor_vm.py:129-138); tvm_vm_to_channel_last() converts. Pair m reads its
+ * line at coordinate P_m[0] and its plane at (row, col) = (P_m[1], P_m[2]) with
+ * P_0 = (0,1,2), P_1 = (2,0,1), P_2 = (1,2,0) (tensor_vm.py:50-52).
+ *
+ * Randomness is an INPUT: sample jitter and the Gumbel noise of the weighted
+ * appearance-sample choice are arrays the caller passes (or fills with
+ * tvm_noise_fill), so results are bit-reproducible and the reference's own draws can
+ * be replayed.
+ */
+#ifndef TENSORF_GB300_H_
+#define TENSORF_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TVM_ABI_VERSION 1
+
+/* Symbols of this library are exported with default visibility. */
+#ifndef TVM_API
+#define TVM_API __attribute__((visibility("default")))
+#endif
+
+/* Status codes. */
+#define TVM_OK 0
+#define TVM_ERR_INVALID (-1)     /* null pointer or bad scalar argument */
+#define TVM_ERR_SHAPE (-2)       /* sizes out of the supported range */
+#define TVM_ERR_DTYPE (-3)       /* unsupported dtype / dtype combination */
+#define TVM_ERR_ALIGN (-4)       /* pointer not aligned as the layout requires */
+#define TVM_ERR_UNSUPPORTED (-5) /* valid request this build does not implement */
+#define TVM_ERR_LAUNCH (-6)      /* CUDA launch or runtime error */
+#define TVM_ERR_NONFINITE (-7)   /* non-finite value detected */
+#define TVM_ERR_TIMEOUT (-8)     /* a bounded device wait gave up */
+#define TVM_ERR_WORKSPACE (-9)   /* workspace too small */
+
+/* Storage dtypes. */
+#define TVM_F32 0
+#define TVM_BF16 1
+#define TVM_F64 2
+
+/* Render modes (tensorf/render.py:18-23). */
+#define TVM_MODE_RGB 0
+#define TVM_MODE_DIST_MEDIAN 1
+#define TVM_MODE_DIST_MEAN 2
+
+/* Samplers. */
+#define TVM_SAMPLER_BBOX 0     /* render.py:175-186, 350-434 */
+#define TVM_SAMPLER_CONTRACT 1 /* render.py:122-173 (schedule supplied by caller) */
+
+/* One VM-decomposed tensor (TensorVM, tensor_vm.py:14-40). */
+typedef struct {
+  int32_t grid_dim; /* G */
+  int32_t channels; /* C per vector-matrix pair; multiple of 4 */
+  int32_t dtype;    /* TVM_F32 / TVM_BF16 / TVM_F64 */
+  int32_t _pad;
+  const void* lines;  /* [3][G][C] */
+  const void* planes; /* [3][G][G][C] */
+} tvm_vm_field;
+
+/* Model description: the two VM tensors and the FeatureMlp (networks.py:38-121). */
+typedef struct {
+  int32_t grid_dim;            /* G */
+  int32_t density_channels;    /* C_d (density_feat_dim) */
+  int32_t appearance_channels; /* C_a (appearance_feat_dim) */
+  int32_t feature_n_freqs;     /* fourier frequencies of the squashed features */
+  int32_t viewdir_n_freqs;     /* fourier frequencies of the view direction */
+  int32_t squash_dim;          /* FeatureMlp.feature_squash_dim, 27 */
+  int32_t units;               /* FeatureMlp.units, 128 */
+  int32_t dtype;               /* arithmetic/storage mode: TVM_F32, TVM_BF16, TVM_F64 */
+} tvm_model_desc;
+
+/* Offsets (in elements of the master dtype: float, or double for TVM_F64) of every
+ * parameter segment inside one flat parameter buffer. Grad, Adam mu and nu buffers
+ * use the same layout. Segments are 64-element aligned. MLP kernels are (in, out)
+ * row-major like flax's Dense kernels. */
+typedef struct {
+  int64_t density_lines, density_planes;
+  int64_t appearance_lines, appearance_planes;
+  int64_t mlp_w0, mlp_w1, mlp_b1, mlp_w2, mlp_b2, mlp_w3, mlp_b3;
+  int64_t mlp_begin; /* first MLP element: [0, mlp_begin) is the tensor lr group */
+  int64_t total;
+  /* BF16 mode: element offsets of the bf16 shadow copies of the field tensors inside
+   * the shadow buffer; 0 otherwise. */
+  int64_t shadow_density_lines, shadow_density_planes;
+  int64_t shadow_appearance_lines, shadow_appearance_planes;
+  int64_t shadow_total;
+  int32_t encoded_dim; /* MLP input width after the fourier encoding (150 for n=2) */
+  int32_t _pad;
+} tvm_param_layout;
+
+/* A batch of rays (cameras.Rays3D, cameras.py:10-20), device pointers. */
+typedef struct {
+  int64_t count;          /* R */
+  const float* origins;   /* (R, 3) */
+  const float* directions;/* (R, 3) */
+} tvm_rays;
+
+/* Per-call render configuration (render.RenderConfig, render.py:26-36, plus the
+ * inputs the reference derives from PRNG keys). */
+typedef struct {
+  int32_t density_samples;    /* N */
+  int32_t appearance_samples; /* k */
+  int32_t mode;               /* TVM_MODE_* */
+  int32_t sampler;            /* TVM_SAMPLER_* */
+  float density_shift;        /* added before softplus; the reference uses +10.0 (render.py:207) */
+  float _pad0;
+  float aabb[6];              /* min xyz, max xyz (TrainState.aabb, training.py:96) */
+  const float* schedule;      /* CONTRACT: (N,) fixed t schedule; BBOX: unused */
+  const float* jitter;        /* BBOX: (N,) shared by all rays (render.py:177-186) or
+                                 NULL for no jitter; CONTRACT: (R, N) per sample */
+  int32_t jitter_per_ray;     /* BBOX only: 1 if jitter is (R, N) instead of (N,) */
+  int32_t gumbel_per_ray;     /* 1 if gumbel is (R, N), 0 if (N,) shared (reference) */
+  const float* gumbel;        /* Gumbel noise of jax.random.choice (render.py:461-469) */
+} tvm_render_desc;
+
+/* Adam hyper-parameters (training.py:207-243; optax.scale_by_adam). */
+typedef struct {
+  float lr_tensor;  /* 0.02 */
+  float lr_mlp;     /* 1e-3 */
+  float b1, b2, eps;/* 0.9, 0.99, 1e-8 */
+  float lr_decay;   /* multiplier from the exponential decay (training.py:158-181) */
+  int32_t count;    /* step count after increment: 1 on the first update */
+  int32_t _pad;
+} tvm_adam_desc;
+
+/* ---- library ---------------------------------------------------------------------- */
+TVM_API int tvm_abi_version(void);
+TVM_API const char* tvm_last_error_message(void);
+/* Number of kernels this library has launched from the calling thread. */
+TVM_API uint64_t tvm_kernel_launches(void);
+/* Measurement hook: when `events` (n cudaEvent_t created by the caller) is set for the
+ * calling thread, tvm_train_step / tvm_loss_and_grad / tvm_render_fwd record
+ * events[i] on their stream at the boundary before phase i and events[n_phases] after
+ * the last one (phases: 0 density fwd, 1 composite+select, 2 appearance gather,
+ * 3 MLP fwd, 4 colour+loss, 5 MLP bwd, 6 appearance scatter, 7 composite bwd,
+ * 8 density scatter, 9 Adam). Unused trailing phases record nothing. NULL disables. */
+TVM_API int tvm_set_phase_events(void* const* events, int32_t n);
+
+/* ---- parameter layout ---------------------------------------------------------- */
+/* Fill *out for the model. Replaces the pytree structure of render.LearnableParams
+ * (render.py:39-46) with one flat buffer. */
+TVM_API int tvm_get_param_layout(const tvm_model_desc* model, tvm_param_layout* out);
+
+/* Reference channel-first (3, C, G) / (3, C, G, G) float32 -> channel-last lines /
+ * planes in `dtype` (tensor_vm.py:129-138). dst_* are device buffers. */
+TVM_API int tvm_vm_to_channel_last(int32_t grid_dim, int32_t channels, const float* vector_cf,
+                           const float* matrix_cf, int32_t dtype, void* lines, void* planes,
+                           void* stream);
+/* Inverse of the above for float32 channel-last buffers (gradients, parameters). */
+TVM_API int tvm_vm_to_channel_first(int32_t grid_dim, int32_t channels, const float* lines,
+                            const float* planes, float* vector_cf, float* matrix_cf, void* stream);
+
+/* ---- (a) VM feature evaluation: TensorVM.interpolate (tensor_vm.py:42-89) --------- */
+/* coords (3, n) float32 in [-1, 1]; out (3C, n) float32, mode-major like the
+ * reference. */
+TVM_API int tvm_vm_features_fwd(const tvm_vm_field* field, const float* coords, int64_t n, float* out,
+                        void* stream);
+/* grad_out (3C, n) -> ACCUMULATES into grad_lines [3][G][C] and grad_planes
+ * [3][G][G][C] (float32, channel-last). Backward of map_coordinates(order=1,
+ * mode="nearest") (tensor_vm.py:226-250): clamped corners receive the weights of the
+ * unclamped coordinate. */
+TVM_API int tvm_vm_features_bwd(const tvm_vm_field* field, const float* coords, int64_t n,
+                        const float* grad_out, float* grad_lines, float* grad_planes,
+                        void* stream);
+
+/* ---- (b) ray samplers --------------------------------------------------------------- */
+/* sample_points_along_ray_within_bbox vmapped over rays (render.py:350-434, 177-186)
+ * or the contracted sampler (render.py:122-173), followed by the [-1, 1]
+ * normalisation (render.py:192-196). points (3, R, N) normalised; ts (R, N);
+ * step_sizes (R, N). Any output may be NULL. */
+TVM_API int tvm_sample_points(const tvm_rays* rays, const tvm_render_desc* cfg, float* points,
+                      float* ts, float* step_sizes, void* stream);
+
+/* ---- (c) compositing and selection -------------------------------------------------- */
+/* compute_segment_probabilities (render.py:300-347): sigmas, step_sizes (R, N) ->
+ * p_exits, p_terminates (R, N). */
+TVM_API int tvm_composite_fwd(const float* sigmas, const float* step_sizes, int64_t rays,
+                      int32_t samples, float* p_exits, float* p_terminates, void* stream);
+/* Backward of the above: grad_p_exits, grad_p_terminates (R, N) (either may be NULL)
+ * -> grad_sigmas (R, N) (overwritten). */
+TVM_API int tvm_composite_bwd(const float* sigmas, const float* step_sizes, int64_t rays,
+                      int32_t samples, const float* grad_p_exits, const float* grad_p_terminates,
+                      float* grad_sigmas, void* stream);
+/* Weighted choice without replacement (render.py:459-470): per row, the k indices
+ * with the largest log(p) + gumbel, largest first, equal keys -> lower index first.
+ * p (R, N); gumbel (N,) shared or (R, N) if gumbel_per_ray; indices (R, k) int32. */
+TVM_API int tvm_topk_select(const float* p, const float* gumbel, int32_t gumbel_per_ray, int64_t rays,
+                    int32_t samples, int32_t k, int32_t* indices, void* stream);
+
+/* ---- (d) FeatureMlp (networks.py:45-121) --------------------------------------------- */
+/* features (n, 3*C_a), viewdirs (n, 3) -> rgb (n, 3). params: flat buffer in the
+ * tvm_param_layout layout (master dtype float32; TVM_BF16 models use bf16 tensor
+ * cores, TVM_F32 models float32 arithmetic). workspace: tvm_mlp_workspace_size(). */
+TVM_API size_t tvm_mlp_workspace_size(const tvm_model_desc* model, int64_t n);
+TVM_API int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* features,
+                const float* viewdirs, int64_t n, float* rgb, void* workspace,
+                size_t workspace_bytes, void* stream);
+/* grad_rgb (n, 3) -> grad_features (n, 3*C_a) (overwritten, may be NULL) and
+ * ACCUMULATES the MLP weight gradients into grads (flat layout). */
+TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
+                const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
+                void* grads, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- fused render_rays / training_step ---------------------------------------------- */
+/* render_rays (render.py:105-279) for one chunk of rays. out: (R, 3) for RGB, (R,) for
+ * distances. params: flat master buffer; shadow: bf16 copies (TVM_BF16 models) or
+ * NULL. */
+TVM_API size_t tvm_render_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg,
+                                 int64_t rays);
+TVM_API int tvm_render_fwd(const tvm_model_desc* model, const void* params, const void* shadow,
+                   const tvm_rays* rays, const tvm_render_desc* cfg, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* TrainState.training_step (training.py:101-205): render (RGB mode), MSE loss against
+ * colors (R, 3), backward, Adam update of params/mu/nu (flat layout), refresh of the
+ * bf16 shadow (TVM_BF16), grads zeroed for the next step. loss_out: device float,
+ * written with the MSE. grads must be zero on entry (they are left zero). */
+TVM_API size_t tvm_train_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg,
+                                int64_t rays);
+TVM_API int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void* grads,
+                   void* adam_mu, void* adam_nu, const tvm_adam_desc* adam, const tvm_rays* rays,
+                   const float* colors, const tvm_render_desc* cfg, float* loss_out,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* Loss and gradients only (no Adam): used by gradient checks. grads ACCUMULATE. */
+TVM_API int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, const void* shadow,
+                      void* grads, const tvm_rays* rays, const float* colors,
+                      const tvm_render_desc* cfg, float* loss_out, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Fused Adam over the flat buffers (training.py:184-203, 213-243). n = layout.total.
+ * Elements [0, mlp_begin) use lr_tensor, the rest lr_mlp. Zeroes grads. If shadow is
+ * non-NULL (TVM_BF16) the field segments are rounded into it. */
+TVM_API int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* mu, void* nu,
+                  const tvm_adam_desc* adam, void* shadow, void* stream);
+/* Round the field segments of params into the bf16 shadow (after init / load). */
+TVM_API int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow,
+                       void* stream);
+
+/* ---- data generation ---------------------------------------------------------------- */
+/* Counter-based noise: dst[i] = U[0,1) (kind 0) or standard Gumbel (kind 1) from
+ * (seed, stream_id, i). */
+TVM_API int tvm_noise_fill(float* dst, int64_t n, uint64_t seed, uint64_t stream_id, int32_t kind,
+                   void* stream);
+/* Pinhole rays of one camera (cameras.py:100-143): K (3x3 row-major), R_wc (3x3),
+ * t_wc (3): origins/directions (H*W, 3) float32, pixel (v, u) row-major. The
+ * pixel subset `pixels` (n indices into H*W) may be NULL for the full frame. */
+TVM_API int tvm_camera_rays(const double* K, const double* R_world_camera, const double* t_world_camera,
+                    int32_t width, int32_t height, const int64_t* pixels, int64_t n,
+                    float* origins, float* directions, void* stream);
+/* FP64 quadrature of a field of constant-density spheres (analytic training target):
+ * centers (S,3), radii (S,), colors (S,3) float64; colors_out (R, 3) float32. The
+ * quadrature spans each ray's aabb segment with n_samples midpoint samples and a
+ * white background. */
+TVM_API int tvm_sphere_scene_render(const double* centers, const double* radii, const double* colors,
+                            int32_t spheres, double density, const float* aabb,
+                            const tvm_rays* rays, int32_t n_samples, float* colors_out,
+                            void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TENSORF_GB300_H_ */

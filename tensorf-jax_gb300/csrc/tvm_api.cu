@@ -1,0 +1,529 @@
+// C ABI entry points: argument validation, parameter layout, the per-seam functions
+// and the fused render_rays / training_step orchestration.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <algorithm>
+
+#include "tvm_internal.h"
+
+namespace tvm {
+
+static thread_local char g_err[512] = "";
+static thread_local uint64_t g_launches = 0;
+static thread_local cudaEvent_t g_events[32];
+static thread_local int g_n_events = 0;
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+void phase_mark(int phase, cudaStream_t st) {
+  if (phase >= 0 && phase < g_n_events) cudaEventRecord(g_events[phase], st);
+}
+
+int check_launch(const char* what) {
+  ++g_launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return TVM_ERR_LAUNCH;
+  }
+  return TVM_OK;
+}
+
+static int64_t seg(int64_t& off, int64_t n) {
+  const int64_t at = off;
+  off = round_up(off + n, 64);
+  return at;
+}
+
+static int encoded_dim(const tvm_model_desc& m) {
+  return m.squash_dim + 3 + 2 * m.feature_n_freqs * m.squash_dim + 2 * m.viewdir_n_freqs * 3;
+}
+
+static bool channels_ok(int c) { return c == 8 || c == 16 || c == 24 || c == 48; }
+
+static int validate_model(const tvm_model_desc* m) {
+  TVM_REQUIRE(m != nullptr, TVM_ERR_INVALID, "model descriptor is NULL");
+  TVM_REQUIRE(m->grid_dim >= 2 && m->grid_dim <= 4096, TVM_ERR_SHAPE, "grid_dim=%d outside [2, 4096]",
+              m->grid_dim);
+  TVM_REQUIRE(channels_ok(m->density_channels), TVM_ERR_UNSUPPORTED,
+              "density_channels=%d not compiled (8, 16, 24, 48)", m->density_channels);
+  TVM_REQUIRE(channels_ok(m->appearance_channels), TVM_ERR_UNSUPPORTED,
+              "appearance_channels=%d not compiled (8, 16, 24, 48)", m->appearance_channels);
+  TVM_REQUIRE(m->feature_n_freqs >= 0 && m->feature_n_freqs <= 16 && m->viewdir_n_freqs >= 0 &&
+                  m->viewdir_n_freqs <= 16,
+              TVM_ERR_SHAPE, "fourier frequencies must be in [0, 16]");
+  TVM_REQUIRE(m->squash_dim >= 1 && m->squash_dim <= 256 && m->units >= 1 && m->units <= 1024,
+              TVM_ERR_SHAPE, "squash_dim / units out of range");
+  TVM_REQUIRE(m->dtype == TVM_F32 || m->dtype == TVM_BF16, TVM_ERR_DTYPE,
+              "model dtype %d not supported (TVM_F32, TVM_BF16)", m->dtype);
+  return TVM_OK;
+}
+
+static void make_layout(const tvm_model_desc& m, tvm_param_layout& L) {
+  memset(&L, 0, sizeof(L));
+  const int64_t G = m.grid_dim;
+  const int64_t Cd = m.density_channels, Ca = m.appearance_channels;
+  const int enc = encoded_dim(m);
+  int64_t off = 0;
+  L.density_lines = seg(off, 3 * G * Cd);
+  L.density_planes = seg(off, 3 * G * G * Cd);
+  L.appearance_lines = seg(off, 3 * G * Ca);
+  L.appearance_planes = seg(off, 3 * G * G * Ca);
+  L.mlp_begin = off;
+  L.mlp_w0 = seg(off, 3 * Ca * m.squash_dim);
+  L.mlp_w1 = seg(off, (int64_t)enc * m.units);
+  L.mlp_b1 = seg(off, m.units);
+  L.mlp_w2 = seg(off, (int64_t)m.units * m.units);
+  L.mlp_b2 = seg(off, m.units);
+  L.mlp_w3 = seg(off, (int64_t)m.units * 3);
+  L.mlp_b3 = seg(off, 3);
+  L.total = off;
+  if (m.dtype == TVM_BF16) {
+    L.shadow_density_lines = L.density_lines;
+    L.shadow_density_planes = L.density_planes;
+    L.shadow_appearance_lines = L.appearance_lines;
+    L.shadow_appearance_planes = L.appearance_planes;
+    L.shadow_total = L.mlp_begin;
+  }
+  L.encoded_dim = enc;
+}
+
+static int validate_rays(const tvm_rays* rays) {
+  TVM_REQUIRE(rays != nullptr, TVM_ERR_INVALID, "rays is NULL");
+  TVM_REQUIRE(rays->count >= 0 && rays->count <= (1LL << 31), TVM_ERR_SHAPE, "ray count %lld out of range",
+              (long long)rays->count);
+  TVM_REQUIRE(rays->count == 0 || (rays->origins && rays->directions), TVM_ERR_INVALID,
+              "ray origins/directions are NULL");
+  return TVM_OK;
+}
+
+static int validate_render(const tvm_render_desc* c, int64_t R, bool need_select) {
+  TVM_REQUIRE(c != nullptr, TVM_ERR_INVALID, "render descriptor is NULL");
+  TVM_REQUIRE(c->density_samples >= 1 && c->density_samples <= 8192, TVM_ERR_SHAPE,
+              "density_samples=%d outside [1, 8192]", c->density_samples);
+  TVM_REQUIRE(c->sampler == TVM_SAMPLER_BBOX || c->sampler == TVM_SAMPLER_CONTRACT, TVM_ERR_INVALID,
+              "unknown sampler %d", c->sampler);
+  TVM_REQUIRE(c->mode == TVM_MODE_RGB || c->mode == TVM_MODE_DIST_MEAN || c->mode == TVM_MODE_DIST_MEDIAN,
+              TVM_ERR_INVALID, "unknown mode %d", c->mode);
+  for (int a = 0; a < 3; ++a)
+    TVM_REQUIRE(c->aabb[a] < c->aabb[3 + a], TVM_ERR_INVALID, "aabb min must be < max on every axis");
+  if (c->sampler == TVM_SAMPLER_CONTRACT) {
+    TVM_REQUIRE(c->density_samples >= 2, TVM_ERR_SHAPE, "contracted sampler needs >= 2 samples");
+    TVM_REQUIRE(c->schedule != nullptr && c->jitter != nullptr, TVM_ERR_INVALID,
+                "contracted sampler needs schedule (N,) and jitter (R, N)");
+  }
+  if (need_select && c->mode == TVM_MODE_RGB) {
+    TVM_REQUIRE(c->appearance_samples >= 1 && c->appearance_samples <= c->density_samples &&
+                    c->appearance_samples <= 1024,
+                TVM_ERR_SHAPE, "appearance_samples=%d must be in [1, min(N, 1024)]", c->appearance_samples);
+    TVM_REQUIRE(c->gumbel != nullptr, TVM_ERR_INVALID, "RGB mode needs the Gumbel noise array");
+  }
+  TVM_REQUIRE(R * (int64_t)c->density_samples < (1LL << 40), TVM_ERR_SHAPE, "R*N too large");
+  return TVM_OK;
+}
+
+static SamplerArgs sampler_args(const tvm_render_desc& c) {
+  SamplerArgs s;
+  s.sampler = c.sampler;
+  s.N = c.density_samples;
+  for (int a = 0; a < 6; ++a) s.aabb[a] = c.aabb[a];
+  s.schedule = c.schedule;
+  s.jitter = c.jitter;
+  s.jitter_per_ray = c.jitter_per_ray;
+  return s;
+}
+
+static MlpDims mlp_dims(const tvm_model_desc& m) {
+  MlpDims d;
+  d.feat = 3 * m.appearance_channels;
+  d.squash = m.squash_dim;
+  d.enc = encoded_dim(m);
+  d.units = m.units;
+  d.nf = m.feature_n_freqs;
+  d.nv = m.viewdir_n_freqs;
+  return d;
+}
+
+static MlpWeights mlp_weights(const tvm_param_layout& L, const float* p) {
+  return MlpWeights{p + L.mlp_w0, p + L.mlp_w1, p + L.mlp_b1, p + L.mlp_w2,
+                    p + L.mlp_b2, p + L.mlp_w3, p + L.mlp_b3};
+}
+static MlpGrads mlp_grads(const tvm_param_layout& L, float* g) {
+  return MlpGrads{g + L.mlp_w0, g + L.mlp_w1, g + L.mlp_b1, g + L.mlp_w2,
+                  g + L.mlp_b2, g + L.mlp_w3, g + L.mlp_b3};
+}
+
+// Fields read by the gathers: bf16 shadow in BF16 mode, the FP32 master otherwise.
+static FieldView density_field(const tvm_model_desc& m, const tvm_param_layout& L, const float* p,
+                               const void* shadow) {
+  if (m.dtype == TVM_BF16 && shadow) {
+    const __nv_bfloat16* s = static_cast<const __nv_bfloat16*>(shadow);
+    return FieldView{m.grid_dim, m.density_channels, TVM_BF16, s + L.shadow_density_lines,
+                     s + L.shadow_density_planes};
+  }
+  return FieldView{m.grid_dim, m.density_channels, TVM_F32, p + L.density_lines, p + L.density_planes};
+}
+static FieldView appearance_field(const tvm_model_desc& m, const tvm_param_layout& L, const float* p,
+                                  const void* shadow) {
+  if (m.dtype == TVM_BF16 && shadow) {
+    const __nv_bfloat16* s = static_cast<const __nv_bfloat16*>(shadow);
+    return FieldView{m.grid_dim, m.appearance_channels, TVM_BF16, s + L.shadow_appearance_lines,
+                     s + L.shadow_appearance_planes};
+  }
+  return FieldView{m.grid_dim, m.appearance_channels, TVM_F32, p + L.appearance_lines,
+                   p + L.appearance_planes};
+}
+
+// Buffers of one render / train pass, carved from the workspace in a fixed order.
+struct PassBufs {
+  float* sigma;
+  int32_t* sel;
+  float *w_sel, *p_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
+};
+
+static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, int64_t R,
+                           bool backward, Workspace& ws) {
+  PassBufs b{};
+  const int64_t N = c.density_samples;
+  const int64_t k = (c.mode == TVM_MODE_RGB) ? c.appearance_samples : 0;
+  const int64_t M = R * k;
+  const int64_t F = 3LL * m.appearance_channels;
+  b.sigma = ws.take<float>(R * N);
+  b.sel = ws.take<int32_t>(M);
+  b.w_sel = ws.take<float>(M);
+  b.p_last = ws.take<float>(R);
+  b.wsum = ws.take<float>(R);
+  b.X0 = ws.take<float>(M * F);
+  b.rgb = ws.take<float>(M * 3);
+  if (backward) {
+    b.dZ3 = ws.take<float>(M * 3);
+    b.gw = ws.take<float>(M);
+    b.gP = ws.take<float>(R);
+    b.gsum = ws.take<float>(R * N);
+    b.dX0 = ws.take<float>(M * F);
+  }
+  return b;
+}
+
+static size_t pass_bytes(const tvm_model_desc& m, const tvm_render_desc& c, int64_t R, bool backward) {
+  Workspace ws{nullptr, 0, 0, true};
+  carve_pass(m, c, R, backward, ws);
+  const int64_t k = (c.mode == TVM_MODE_RGB) ? c.appearance_samples : 0;
+  return ws.used + 256 + mlp_workspace_bytes(mlp_dims(m), R * k) + 256;
+}
+
+// render_rays forward, and (if grads != null) the loss and backward of training_step.
+static int run_pass(const tvm_model_desc& m, const float* params, const void* shadow, float* grads,
+                    const tvm_rays& rays, const float* colors, const tvm_render_desc& c,
+                    float* loss, float* out, void* workspace, size_t ws_bytes, cudaStream_t st) {
+  tvm_param_layout L;
+  make_layout(m, L);
+  const bool backward = grads != nullptr;
+  const int64_t R = rays.count;
+  Workspace ws{static_cast<char*>(workspace), ws_bytes, 0, false};
+  PassBufs b = carve_pass(m, c, R, backward, ws);
+  TVM_REQUIRE(ws.ok(), TVM_ERR_WORKSPACE, "workspace too small (%zu bytes)", ws_bytes);
+  if (R == 0) return TVM_OK;
+  const SamplerArgs s = sampler_args(c);
+  const FieldView fd = density_field(m, L, params, shadow);
+  const FieldView fa = appearance_field(m, L, params, shadow);
+  const int k = c.appearance_samples;
+
+  phase_mark(0, st);
+  TVM_TRY(launch_density_fwd(fd, c.density_shift, rays.origins, rays.directions, R, s, b.sigma, st));
+  phase_mark(1, st);
+  if (c.mode != TVM_MODE_RGB) {
+    TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, 0, nullptr, 0,
+                                    nullptr, nullptr, nullptr, nullptr, out, st));
+    phase_mark(2, st);
+    return TVM_OK;
+  }
+  TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
+                                  c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.wsum, nullptr, st));
+  phase_mark(2, st);
+  TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
+  phase_mark(3, st);
+  const MlpDims d = mlp_dims(m);
+  const MlpWeights w = mlp_weights(L, params);
+  const size_t mlp_off = ws.used;
+  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, backward, st));
+  phase_mark(4, st);
+  if (!backward) {
+    TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
+                              nullptr, nullptr, st));
+    phase_mark(5, st);
+    return TVM_OK;
+  }
+  TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, colors, out, loss, b.dZ3, b.gw,
+                            b.gP, st));
+  phase_mark(5, st);
+  Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
+  TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, R * k, b.dZ3, b.dX0, ws2, st));
+  phase_mark(6, st);
+  TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
+                                rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
+  phase_mark(7, st);
+  TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
+                               b.gsum, st));
+  phase_mark(8, st);
+  TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
+                             rays.directions, R, s, b.gsum, st));
+  phase_mark(9, st);
+  return TVM_OK;
+}
+
+}  // namespace tvm
+
+using namespace tvm;
+
+extern "C" {
+
+int tvm_abi_version(void) { return TVM_ABI_VERSION; }
+
+uint64_t tvm_kernel_launches(void) { return g_launches; }
+
+int tvm_set_phase_events(void* const* events, int32_t n) {
+  TVM_REQUIRE(n >= 0 && n <= 32, TVM_ERR_SHAPE, "at most 32 phase events");
+  TVM_REQUIRE(n == 0 || events != nullptr, TVM_ERR_INVALID, "events is NULL");
+  for (int i = 0; i < n; ++i) g_events[i] = static_cast<cudaEvent_t>(events[i]);
+  g_n_events = n;
+  return TVM_OK;
+}
+
+const char* tvm_last_error_message(void) { return g_err; }
+
+int tvm_get_param_layout(const tvm_model_desc* model, tvm_param_layout* out) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(out != nullptr, TVM_ERR_INVALID, "out is NULL");
+  make_layout(*model, *out);
+  return TVM_OK;
+}
+
+int tvm_vm_to_channel_last(int32_t grid_dim, int32_t channels, const float* vector_cf,
+                           const float* matrix_cf, int32_t dtype, void* lines, void* planes,
+                           void* stream) {
+  TVM_REQUIRE(grid_dim >= 2 && channels >= 1, TVM_ERR_SHAPE, "bad grid_dim/channels");
+  TVM_REQUIRE(vector_cf && matrix_cf && lines && planes, TVM_ERR_INVALID, "NULL pointer");
+  return launch_to_channel_last(grid_dim, channels, vector_cf, matrix_cf, dtype, lines, planes,
+                                as_stream(stream));
+}
+
+int tvm_vm_to_channel_first(int32_t grid_dim, int32_t channels, const float* lines,
+                            const float* planes, float* vector_cf, float* matrix_cf, void* stream) {
+  TVM_REQUIRE(grid_dim >= 2 && channels >= 1, TVM_ERR_SHAPE, "bad grid_dim/channels");
+  TVM_REQUIRE(vector_cf && matrix_cf && lines && planes, TVM_ERR_INVALID, "NULL pointer");
+  return launch_to_channel_first(grid_dim, channels, lines, planes, vector_cf, matrix_cf,
+                                 as_stream(stream));
+}
+
+static int validate_field(const tvm_vm_field* f) {
+  TVM_REQUIRE(f != nullptr, TVM_ERR_INVALID, "field is NULL");
+  TVM_REQUIRE(f->grid_dim >= 2 && f->grid_dim <= 4096, TVM_ERR_SHAPE, "grid_dim=%d outside [2, 4096]",
+              f->grid_dim);
+  TVM_REQUIRE(channels_ok(f->channels), TVM_ERR_UNSUPPORTED, "channels=%d not compiled (8, 16, 24, 48)",
+              f->channels);
+  TVM_REQUIRE(f->dtype == TVM_F32 || f->dtype == TVM_BF16, TVM_ERR_DTYPE, "field dtype %d", f->dtype);
+  TVM_REQUIRE(f->lines && f->planes, TVM_ERR_INVALID, "field lines/planes NULL");
+  TVM_REQUIRE(aligned(f->lines, 16) && aligned(f->planes, 16), TVM_ERR_ALIGN,
+              "field buffers must be 16-byte aligned");
+  return TVM_OK;
+}
+
+static FieldView view_of(const tvm_vm_field* f) {
+  return FieldView{f->grid_dim, f->channels, f->dtype, f->lines, f->planes};
+}
+
+int tvm_vm_features_fwd(const tvm_vm_field* field, const float* coords, int64_t n, float* out,
+                        void* stream) {
+  TVM_TRY(validate_field(field));
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(n == 0 || (coords && out), TVM_ERR_INVALID, "coords/out NULL");
+  return launch_vm_features_fwd(view_of(field), coords, n, out, as_stream(stream));
+}
+
+int tvm_vm_features_bwd(const tvm_vm_field* field, const float* coords, int64_t n,
+                        const float* grad_out, float* grad_lines, float* grad_planes, void* stream) {
+  TVM_TRY(validate_field(field));
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(n == 0 || (coords && grad_out && grad_lines && grad_planes), TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(grad_lines, 16) && aligned(grad_planes, 16), TVM_ERR_ALIGN,
+              "gradient buffers must be 16-byte aligned");
+  return launch_vm_features_bwd(view_of(field), coords, n, grad_out, grad_lines, grad_planes,
+                                as_stream(stream));
+}
+
+int tvm_sample_points(const tvm_rays* rays, const tvm_render_desc* cfg, float* points, float* ts,
+                      float* step_sizes, void* stream) {
+  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_render(cfg, rays->count, false));
+  return launch_points(rays->origins, rays->directions, rays->count, sampler_args(*cfg), points, ts,
+                       step_sizes, as_stream(stream));
+}
+
+int tvm_composite_fwd(const float* sigmas, const float* step_sizes, int64_t rays, int32_t samples,
+                      float* p_exits, float* p_terminates, void* stream) {
+  TVM_REQUIRE(rays >= 0 && samples >= 1, TVM_ERR_SHAPE, "rays >= 0 and samples >= 1 required");
+  TVM_REQUIRE(rays == 0 || (sigmas && step_sizes), TVM_ERR_INVALID, "NULL pointer");
+  return launch_segment_fwd(sigmas, step_sizes, rays, samples, p_exits, p_terminates, as_stream(stream));
+}
+
+int tvm_composite_bwd(const float* sigmas, const float* step_sizes, int64_t rays, int32_t samples,
+                      const float* grad_p_exits, const float* grad_p_terminates, float* grad_sigmas,
+                      void* stream) {
+  TVM_REQUIRE(rays >= 0 && samples >= 1 && samples <= 8192, TVM_ERR_SHAPE, "samples outside [1, 8192]");
+  TVM_REQUIRE(rays == 0 || (sigmas && step_sizes && grad_sigmas), TVM_ERR_INVALID, "NULL pointer");
+  return launch_segment_bwd(sigmas, step_sizes, rays, samples, grad_p_exits, grad_p_terminates,
+                            grad_sigmas, as_stream(stream));
+}
+
+int tvm_topk_select(const float* p, const float* gumbel, int32_t gumbel_per_ray, int64_t rays,
+                    int32_t samples, int32_t k, int32_t* indices, void* stream) {
+  TVM_REQUIRE(rays >= 0 && samples >= 1 && samples <= 8192, TVM_ERR_SHAPE, "samples outside [1, 8192]");
+  TVM_REQUIRE(k >= 1 && k <= samples && k <= 1024, TVM_ERR_SHAPE, "k=%d must be in [1, min(N, 1024)]", k);
+  TVM_REQUIRE(rays == 0 || (p && gumbel && indices), TVM_ERR_INVALID, "NULL pointer");
+  return launch_topk(p, gumbel, gumbel_per_ray, rays, samples, k, indices, as_stream(stream));
+}
+
+size_t tvm_mlp_workspace_size(const tvm_model_desc* model, int64_t n) {
+  if (validate_model(model) != TVM_OK || n < 0) return 0;
+  // Forward activations plus the rgb / pre-sigmoid gradient tvm_mlp_bwd recomputes.
+  return mlp_workspace_bytes(mlp_dims(*model), n) + (size_t)n * 6 * sizeof(float) + 1024;
+}
+
+int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* features,
+                const float* viewdirs, int64_t n, float* rgb, void* workspace, size_t workspace_bytes,
+                void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(n == 0 || (params && features && viewdirs && rgb && workspace), TVM_ERR_INVALID,
+              "NULL pointer");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  Workspace ws{static_cast<char*>(workspace), workspace_bytes, 0, false};
+  return mlp_forward(mlp_dims(*model), mlp_weights(L, static_cast<const float*>(params)), features,
+                     viewdirs, 1, n, rgb, ws, false, as_stream(stream));
+}
+
+int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
+                const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
+                void* grads, void* workspace, size_t workspace_bytes, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(n == 0 || (params && features && viewdirs && grad_rgb && grads && workspace),
+              TVM_ERR_INVALID, "NULL pointer");
+  if (n == 0) return TVM_OK;
+  tvm_param_layout L;
+  make_layout(*model, L);
+  const MlpDims d = mlp_dims(*model);
+  const MlpWeights w = mlp_weights(L, static_cast<const float*>(params));
+  cudaStream_t st = as_stream(stream);
+  // Recompute the forward (activations are not kept across ABI calls), then backward.
+  Workspace ws{static_cast<char*>(workspace), workspace_bytes, 0, false};
+  float* rgb = ws.take<float>(n * 3);
+  float* dz = ws.take<float>(n * 3);
+  const size_t off = ws.used;
+  TVM_REQUIRE(ws.ok(), TVM_ERR_WORKSPACE, "workspace too small");
+  TVM_TRY(mlp_forward(d, w, features, viewdirs, 1, n, rgb, ws, true, st));
+  TVM_TRY(launch_sigmoid_bwd(rgb, grad_rgb, n, dz, st));
+  Workspace ws2{static_cast<char*>(workspace), workspace_bytes, off, false};
+  return mlp_backward(d, w, mlp_grads(L, static_cast<float*>(grads)), features, n, dz, grad_features,
+                      ws2, st);
+}
+
+size_t tvm_render_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
+  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true) != TVM_OK || rays < 0) return 0;
+  return pass_bytes(*model, *cfg, rays, false);
+}
+
+size_t tvm_train_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
+  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true) != TVM_OK || rays < 0) return 0;
+  return pass_bytes(*model, *cfg, rays, true);
+}
+
+static int validate_params(const tvm_model_desc* m, const void* params, const void* shadow) {
+  TVM_REQUIRE(params != nullptr, TVM_ERR_INVALID, "params is NULL");
+  TVM_REQUIRE(aligned(params, 16), TVM_ERR_ALIGN, "params must be 16-byte aligned");
+  if (m->dtype == TVM_BF16) {
+    TVM_REQUIRE(shadow != nullptr, TVM_ERR_INVALID, "BF16 model needs the bf16 shadow buffer");
+    TVM_REQUIRE(aligned(shadow, 16), TVM_ERR_ALIGN, "shadow must be 16-byte aligned");
+  }
+  return TVM_OK;
+}
+
+int tvm_render_fwd(const tvm_model_desc* model, const void* params, const void* shadow,
+                   const tvm_rays* rays, const tvm_render_desc* cfg, float* out, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_render(cfg, rays->count, true));
+  TVM_TRY(validate_params(model, params, shadow));
+  TVM_REQUIRE(rays->count == 0 || (out && workspace), TVM_ERR_INVALID, "out/workspace NULL");
+  return run_pass(*model, static_cast<const float*>(params), shadow, nullptr, *rays, nullptr, *cfg,
+                  nullptr, out, workspace, workspace_bytes, as_stream(stream));
+}
+
+int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, const void* shadow, void* grads,
+                      const tvm_rays* rays, const float* colors, const tvm_render_desc* cfg,
+                      float* loss_out, void* workspace, size_t workspace_bytes, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_render(cfg, rays->count, true));
+  TVM_TRY(validate_params(model, params, shadow));
+  TVM_REQUIRE(cfg->mode == TVM_MODE_RGB, TVM_ERR_INVALID, "training needs RGB mode");
+  TVM_REQUIRE(grads && aligned(grads, 16), TVM_ERR_ALIGN, "grads NULL or not 16-byte aligned");
+  TVM_REQUIRE(rays->count == 0 || (colors && loss_out && workspace), TVM_ERR_INVALID, "NULL pointer");
+  cudaStream_t st = as_stream(stream);
+  if (loss_out) {
+    cudaError_t e = cudaMemsetAsync(loss_out, 0, sizeof(float), st);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+  }
+  return run_pass(*model, static_cast<const float*>(params), shadow, static_cast<float*>(grads), *rays,
+                  colors, *cfg, loss_out, nullptr, workspace, workspace_bytes, st);
+}
+
+int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* mu, void* nu,
+                  const tvm_adam_desc* adam, void* shadow, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(params && grads && mu && nu && adam, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(params, 16) && aligned(grads, 16) && aligned(mu, 16) && aligned(nu, 16),
+              TVM_ERR_ALIGN, "Adam buffers must be 16-byte aligned");
+  TVM_REQUIRE(adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  cudaStream_t st = as_stream(stream);
+  TVM_TRY(launch_adam(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
+                      static_cast<float*>(nu), L.total, L.mlp_begin, *adam, st));
+  if (shadow && model->dtype == TVM_BF16)
+    TVM_TRY(launch_shadow(static_cast<const float*>(params), static_cast<__nv_bfloat16*>(shadow),
+                          L.shadow_total, st));
+  return TVM_OK;
+}
+
+int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(model->dtype == TVM_BF16, TVM_ERR_DTYPE, "shadow exists only for TVM_BF16 models");
+  TVM_REQUIRE(params && shadow, TVM_ERR_INVALID, "NULL pointer");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  return launch_shadow(static_cast<const float*>(params), static_cast<__nv_bfloat16*>(shadow),
+                       L.shadow_total, as_stream(stream));
+}
+
+int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void* grads, void* adam_mu,
+                   void* adam_nu, const tvm_adam_desc* adam, const tvm_rays* rays, const float* colors,
+                   const tvm_render_desc* cfg, float* loss_out, void* workspace, size_t workspace_bytes,
+                   void* stream) {
+  TVM_TRY(tvm_loss_and_grad(model, params, shadow, grads, rays, colors, cfg, loss_out, workspace,
+                            workspace_bytes, stream));
+  TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
+  phase_mark(10, as_stream(stream));
+  return TVM_OK;
+}
+
+}  // extern "C"

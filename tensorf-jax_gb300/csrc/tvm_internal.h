@@ -1,0 +1,91 @@
+// Internal launchers shared between the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tvm_common.cuh"
+#include "tvm_sampler.cuh"
+
+namespace tvm {
+
+// Field view with a typed storage pointer (dtype decides the cast).
+struct FieldView {
+  int G, C, dtype;
+  const void* lines;
+  const void* planes;
+};
+
+// ---- VM feature kernels (tvm_vm.cu) ----
+int launch_vm_features_fwd(const FieldView& f, const float* coords, int64_t n, float* out,
+                           cudaStream_t st);
+int launch_vm_features_bwd(const FieldView& f, const float* coords, int64_t n,
+                           const float* grad_out, float* glines, float* gplanes, cudaStream_t st);
+int launch_density_fwd(const FieldView& f, float shift, const float* origins, const float* dirs,
+                       int64_t R, const SamplerArgs& s, float* sigma, cudaStream_t st);
+int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
+                       const float* dirs, int64_t R, const SamplerArgs& s, const float* gsum,
+                       cudaStream_t st);
+int launch_appearance_fwd(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                          const SamplerArgs& s, const int32_t* sel_idx, int k, float* X0,
+                          cudaStream_t st);
+int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
+                          const float* dirs, int64_t R, const SamplerArgs& s,
+                          const int32_t* sel_idx, int k, const float* dX0, cudaStream_t st);
+int launch_points(const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                  float* points, float* ts, float* steps, cudaStream_t st);
+int launch_to_channel_last(int G, int C, const float* vec, const float* mat, int dtype, void* lines,
+                           void* planes, cudaStream_t st);
+int launch_to_channel_first(int G, int C, const float* lines, const float* planes, float* vec,
+                            float* mat, cudaStream_t st);
+
+// ---- compositing kernels (tvm_composite.cu) ----
+int launch_segment_fwd(const float* sigmas, const float* steps, int64_t R, int N, float* p_exits,
+                       float* p_term, cudaStream_t st);
+int launch_segment_bwd(const float* sigmas, const float* steps, int64_t R, int N, const float* g_pe,
+                       const float* g_pt, float* g_sigma, cudaStream_t st);
+int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t R, int N, int k,
+                int32_t* idx, cudaStream_t st);
+// Fused: sigma (R,N) -> selection (RGB) or distance (DIST modes).
+int launch_composite_select(const float* sigma, const float* origins, const float* dirs, int64_t R,
+                            const SamplerArgs& s, int mode, int k, const float* gumbel,
+                            int gumbel_per_ray, int32_t* sel_idx, float* w_sel, float* p_last,
+                            float* wsum, float* dist_out, cudaStream_t st);
+// Fused: per-ray colour, loss and the gradients entering the MLP and the compositing.
+int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last,
+                      const float* wsum, int64_t R, int k, const float* target, float* color_out,
+                      float* loss, float* dZ3, float* gw_sel, float* gP, cudaStream_t st);
+int launch_composite_bwd(const float* sigma, const float* origins, const float* dirs, int64_t R,
+                         const SamplerArgs& s, int k, const int32_t* sel_idx, const float* gw_sel,
+                         const float* gP, float* gsum, cudaStream_t st);
+
+// ---- MLP (tvm_mlp.cu) ----
+struct MlpDims {
+  int feat;    // 3*C_a
+  int squash;  // 27
+  int enc;     // encoded width (150 at n=2)
+  int units;   // 128
+  int nf, nv;  // fourier frequencies
+};
+struct MlpWeights {
+  const float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
+};
+struct MlpGrads {
+  float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
+};
+size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);
+// rgb = FeatureMlp(X0, viewdir). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...].
+int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st);
+// Needs the buffers kept by the preceding mlp_forward on the same workspace.
+// dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
+int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0,
+                 int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
+int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
+                       cudaStream_t st);
+
+// ---- Adam (tvm_adam.cu) ----
+int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
+                const tvm_adam_desc& a, cudaStream_t st);
+int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
+
+}  // namespace tvm

@@ -1,0 +1,480 @@
+// VM (vector-matrix) feature evaluation and its backward scatter.
+//
+// Reference: TensorVM.interpolate / TensorVMSingle.interpolate /
+// linear_interpolation_with_channel_axis (tensorf/tensor_vm.py:42-89, 140-167,
+// 226-250). Pair m of a tensor contributes feat[m*C + c] = line_m[c](u_a) *
+// plane_m[c](u_b, u_c): a linear lookup along one axis times a bilinear lookup on the
+// other two, with map_coordinates(order=1, mode="nearest") semantics.
+//
+// GB300 mapping: fields live channel-last ([G][C] rows per line, [G][G][C] per plane)
+// so every tap of a sample is C contiguous elements. Four lanes (a quad) own one
+// sample; lane q reads channels [q*C/4, (q+1)*C/4) of every tap with 16-byte vector
+// loads (float4, or uint4/uint2 of bf16), so a quad fetches whole 32-byte sectors and
+// a warp keeps 8 samples -- 144 independent 16-byte loads for density -- in flight.
+// The fields (17 MB density + 52 MB appearance in FP32 at G=300) stay resident in
+// the 126 MB L2; the kernels are bound by L2 gather bandwidth. Gradients go back with
+// 16-byte vector reductions (float4 atomicAdd, sm_90+) into FP32 buffers with the same
+// channel-last layout, so a quad's reduction covers whole sectors too.
+#include "tvm_internal.h"
+
+namespace tvm {
+
+template <typename T, int CPL>
+struct PairEval {
+  Tap tl, tr, tc;
+  float L[CPL], P[CPL];
+};
+
+// Evaluate pair m at grid coordinates (ul; ur, uc) for channels [ch0, ch0+CPL).
+template <typename T, int CPL>
+__device__ __forceinline__ void vm_pair_eval(const T* __restrict__ lines, const T* __restrict__ planes,
+                                             int G, int C, int m, float ul, float ur, float uc,
+                                             int ch0, PairEval<T, CPL>& e) {
+  e.tl = make_tap(ul, G);
+  e.tr = make_tap(ur, G);
+  e.tc = make_tap(uc, G);
+  const T* lb = lines + (int64_t)m * G * C + ch0;
+  const T* pb = planes + (int64_t)m * G * G * C + ch0;
+  float l0[CPL], l1[CPL], p00[CPL], p01[CPL], p10[CPL], p11[CPL];
+  load_chunk<CPL>(lb + (int64_t)e.tl.i0 * C, l0);
+  load_chunk<CPL>(lb + (int64_t)e.tl.i1 * C, l1);
+  load_chunk<CPL>(pb + ((int64_t)e.tr.i0 * G + e.tc.i0) * C, p00);
+  load_chunk<CPL>(pb + ((int64_t)e.tr.i0 * G + e.tc.i1) * C, p01);
+  load_chunk<CPL>(pb + ((int64_t)e.tr.i1 * G + e.tc.i0) * C, p10);
+  load_chunk<CPL>(pb + ((int64_t)e.tr.i1 * G + e.tc.i1) * C, p11);
+  // Corner weights are (row weight) * (column weight), summed in the corner order of
+  // jax's itertools.product loop: (0,0), (0,1), (1,0), (1,1).
+  const float w00 = e.tr.w0 * e.tc.w0, w01 = e.tr.w0 * e.tc.w1;
+  const float w10 = e.tr.w1 * e.tc.w0, w11 = e.tr.w1 * e.tc.w1;
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) {
+    e.L[j] = e.tl.w0 * l0[j] + e.tl.w1 * l1[j];
+    e.P[j] = w00 * p00[j] + w01 * p01[j] + w10 * p10[j] + w11 * p11[j];
+  }
+}
+
+// Scatter the gradient of pair m: d line tap += g * w_tap * P, d plane corner +=
+// g * w_corner * L (per channel g).
+template <typename T, int CPL>
+__device__ __forceinline__ void vm_pair_scatter(float* __restrict__ glines, float* __restrict__ gplanes,
+                                                int G, int C, int m, int ch0,
+                                                const PairEval<T, CPL>& e, const float (&g)[CPL]) {
+  float* lb = glines + (int64_t)m * G * C + ch0;
+  float* pb = gplanes + (int64_t)m * G * G * C + ch0;
+  float gl[CPL], gp[CPL];
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) gl[j] = g[j] * e.P[j] * e.tl.w0;
+  red_chunk<CPL>(lb + (int64_t)e.tl.i0 * C, gl);
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) gl[j] = g[j] * e.P[j] * e.tl.w1;
+  red_chunk<CPL>(lb + (int64_t)e.tl.i1 * C, gl);
+  const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
+  const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
+  const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) gp[j] = g[j] * e.L[j] * w[q];
+    red_chunk<CPL>(pb + ((int64_t)rows[q] * G + cols[q]) * C, gp);
+  }
+}
+
+__device__ __forceinline__ unsigned quad_mask() { return 0xFu << (threadIdx.x & 28); }
+
+__device__ __forceinline__ float quad_sum(float v) {
+  const unsigned qm = quad_mask();
+  v += __shfl_xor_sync(qm, v, 1);
+  v += __shfl_xor_sync(qm, v, 2);
+  return v;
+}
+
+// ---------------------------------------------------------------------------------
+// Seam: TensorVM.interpolate with explicit coordinates.
+// ---------------------------------------------------------------------------------
+template <typename T, int C>
+__global__ void __launch_bounds__(256) vm_features_fwd_kernel(const T* __restrict__ lines,
+                                                             const T* __restrict__ planes, int G,
+                                                             const float* __restrict__ coords,
+                                                             int64_t n, float* __restrict__ out) {
+  constexpr int CPL = C / 4;
+  const int64_t smp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (smp >= n) return;
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(__ldg(coords + a * n + smp), G);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) out[(int64_t)(m * C + sub * CPL + j) * n + smp] = e.L[j] * e.P[j];
+  }
+}
+
+template <typename T, int C>
+__global__ void __launch_bounds__(256) vm_features_bwd_kernel(const T* __restrict__ lines,
+                                                             const T* __restrict__ planes, int G,
+                                                             const float* __restrict__ coords,
+                                                             int64_t n, const float* __restrict__ gout,
+                                                             float* __restrict__ glines,
+                                                             float* __restrict__ gplanes) {
+  constexpr int CPL = C / 4;
+  const int64_t smp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (smp >= n) return;
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(__ldg(coords + a * n + smp), G);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+    float g[CPL];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) g[j] = __ldg(gout + (int64_t)(m * C + sub * CPL + j) * n + smp);
+    vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, g);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Fused density: sampler -> density VM -> sum -> softplus (render.py:177-207).
+// ---------------------------------------------------------------------------------
+template <typename T, int C>
+__global__ void __launch_bounds__(256) density_fwd_kernel(const T* __restrict__ lines,
+                                                         const T* __restrict__ planes, int G,
+                                                         float shift,
+                                                         const float* __restrict__ origins,
+                                                         const float* __restrict__ dirs,
+                                                         int64_t total, SamplerArgs s,
+                                                         float* __restrict__ sigma) {
+  constexpr int CPL = C / 4;
+  const int64_t smp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (smp >= total) return;
+  const int64_t r = smp / s.N;
+  const int i = (int)(smp - r * s.N);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, delta, x[3], u[3];
+  sample_t(g, s, r, i, t, delta);
+  sample_point(g, s, t, x);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  float acc = 0.f;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) acc += e.L[j] * e.P[j];
+  }
+  acc = quad_sum(acc);
+  if (sub == 0) sigma[smp] = softplus_f(acc + shift);
+}
+
+template <typename T, int C>
+__global__ void __launch_bounds__(256) density_bwd_kernel(const T* __restrict__ lines,
+                                                         const T* __restrict__ planes, int G,
+                                                         float* __restrict__ glines,
+                                                         float* __restrict__ gplanes,
+                                                         const float* __restrict__ origins,
+                                                         const float* __restrict__ dirs,
+                                                         int64_t total, SamplerArgs s,
+                                                         const float* __restrict__ gsum) {
+  constexpr int CPL = C / 4;
+  const int64_t smp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (smp >= total) return;
+  const float gs = __ldg(gsum + smp);
+  if (gs == 0.0f) return;  // the whole quad agrees: nothing to scatter
+  const int64_t r = smp / s.N;
+  const int i = (int)(smp - r * s.N);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, delta, x[3], u[3];
+  sample_t(g, s, r, i, t, delta);
+  sample_point(g, s, t, x);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  float gv[CPL];
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) gv[j] = gs;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+    vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Fused appearance gather for the selected samples (render.py:472-486): row
+// m = r*k + j uses sample sel_idx[m] of ray r; X0[m] = 3C features, mode-major.
+// ---------------------------------------------------------------------------------
+template <typename T, int C>
+__global__ void __launch_bounds__(256) appearance_fwd_kernel(const T* __restrict__ lines,
+                                                            const T* __restrict__ planes, int G,
+                                                            const float* __restrict__ origins,
+                                                            const float* __restrict__ dirs,
+                                                            int64_t rows, int k, SamplerArgs s,
+                                                            const int32_t* __restrict__ sel_idx,
+                                                            float* __restrict__ X0) {
+  constexpr int CPL = C / 4;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (row >= rows) return;
+  const int64_t r = row / k;
+  const int i = __ldg(sel_idx + row);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, delta, x[3], u[3];
+  sample_t(g, s, r, i, t, delta);
+  sample_point(g, s, t, x);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  float* dst = X0 + row * (3 * C) + sub * CPL;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) dst[m * C + j] = e.L[j] * e.P[j];
+  }
+}
+
+template <typename T, int C>
+__global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict__ lines,
+                                                            const T* __restrict__ planes, int G,
+                                                            float* __restrict__ glines,
+                                                            float* __restrict__ gplanes,
+                                                            const float* __restrict__ origins,
+                                                            const float* __restrict__ dirs,
+                                                            int64_t rows, int k, SamplerArgs s,
+                                                            const int32_t* __restrict__ sel_idx,
+                                                            const float* __restrict__ dX0) {
+  constexpr int CPL = C / 4;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (row >= rows) return;
+  const int64_t r = row / k;
+  const int i = __ldg(sel_idx + row);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, delta, x[3], u[3];
+  sample_t(g, s, r, i, t, delta);
+  sample_point(g, s, t, x);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  const float* src = dX0 + row * (3 * C) + sub * CPL;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> e;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+    float gv[CPL];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) gv[j] = __ldg(src + m * C + j);
+    vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Sampler seam and layout conversion.
+// ---------------------------------------------------------------------------------
+__global__ void points_kernel(const float* __restrict__ origins, const float* __restrict__ dirs,
+                              int64_t total, SamplerArgs s, float* __restrict__ points,
+                              float* __restrict__ ts, float* __restrict__ steps) {
+  const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (smp >= total) return;
+  const int64_t r = smp / s.N;
+  const int i = (int)(smp - r * s.N);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, delta, x[3];
+  sample_t(g, s, r, i, t, delta);
+  sample_point(g, s, t, x);
+  if (points) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) points[a * total + smp] = x[a];
+  }
+  if (ts) ts[smp] = t;
+  if (steps) steps[smp] = delta;
+}
+
+template <typename T>
+__device__ __forceinline__ T cvt_from_f(float v);
+template <>
+__device__ __forceinline__ float cvt_from_f<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 cvt_from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// (3, C, G) -> [3][G][C] and (3, C, G, G) -> [3][G][G][C].
+template <typename T>
+__global__ void to_channel_last_kernel(int G, int C, const float* __restrict__ vec,
+                                       const float* __restrict__ mat, T* __restrict__ lines,
+                                       T* __restrict__ planes) {
+  const int64_t nl = 3LL * G * C, np = 3LL * G * G * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nl + np;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nl) {
+      int64_t c = e % C, x = (e / C) % G, m = e / ((int64_t)C * G);
+      lines[e] = cvt_from_f<T>(vec[(m * C + c) * G + x]);
+    } else {
+      int64_t q = e - nl;
+      int64_t c = q % C, col = (q / C) % G, row = (q / ((int64_t)C * G)) % G,
+              m = q / ((int64_t)C * G * G);
+      planes[q] = cvt_from_f<T>(mat[((m * C + c) * G + row) * G + col]);
+    }
+  }
+}
+
+__global__ void to_channel_first_kernel(int G, int C, const float* __restrict__ lines,
+                                        const float* __restrict__ planes, float* __restrict__ vec,
+                                        float* __restrict__ mat) {
+  const int64_t nl = 3LL * G * C, np = 3LL * G * G * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nl + np;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (e < nl) {
+      int64_t c = e % C, x = (e / C) % G, m = e / ((int64_t)C * G);
+      vec[(m * C + c) * G + x] = lines[e];
+    } else {
+      int64_t q = e - nl;
+      int64_t c = q % C, col = (q / C) % G, row = (q / ((int64_t)C * G)) % G,
+              m = q / ((int64_t)C * G * G);
+      mat[((m * C + c) * G + row) * G + col] = planes[q];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Dispatch.
+// ---------------------------------------------------------------------------------
+#define TVM_DISPATCH_C(C_, ...)                                                   \
+  switch (C_) {                                                                   \
+    case 8: { constexpr int CC = 8; __VA_ARGS__; break; }                         \
+    case 16: { constexpr int CC = 16; __VA_ARGS__; break; }                       \
+    case 24: { constexpr int CC = 24; __VA_ARGS__; break; }                       \
+    case 48: { constexpr int CC = 48; __VA_ARGS__; break; }                       \
+    default:                                                                      \
+      set_error("channels=%d not compiled (supported: 8, 16, 24, 48)", (int)(C_)); \
+      return TVM_ERR_UNSUPPORTED;                                                 \
+  }
+
+#define TVM_DISPATCH_FIELD(f, ...)                                                           \
+  do {                                                                                       \
+    if ((f).dtype == TVM_F32) {                                                              \
+      using TT = float;                                                                      \
+      const TT* L_ = static_cast<const TT*>((f).lines);                                      \
+      const TT* P_ = static_cast<const TT*>((f).planes);                                     \
+      TVM_DISPATCH_C((f).C, __VA_ARGS__);                                                    \
+    } else if ((f).dtype == TVM_BF16) {                                                      \
+      using TT = __nv_bfloat16;                                                              \
+      const TT* L_ = static_cast<const TT*>((f).lines);                                      \
+      const TT* P_ = static_cast<const TT*>((f).planes);                                     \
+      TVM_DISPATCH_C((f).C, __VA_ARGS__);                                                    \
+    } else {                                                                                 \
+      set_error("field dtype %d not supported", (f).dtype);                                  \
+      return TVM_ERR_DTYPE;                                                                  \
+    }                                                                                        \
+  } while (0)
+
+static inline unsigned quad_blocks(int64_t items) { return (unsigned)ceil_div(items * 4, 256); }
+
+int launch_vm_features_fwd(const FieldView& f, const float* coords, int64_t n, float* out,
+                           cudaStream_t st) {
+  if (n == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (vm_features_fwd_kernel<TT, CC><<<quad_blocks(n), 256, 0, st>>>(
+                             L_, P_, f.G, coords, n, out)));
+  return check_launch("vm_features_fwd");
+}
+
+int launch_vm_features_bwd(const FieldView& f, const float* coords, int64_t n,
+                           const float* grad_out, float* glines, float* gplanes, cudaStream_t st) {
+  if (n == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (vm_features_bwd_kernel<TT, CC><<<quad_blocks(n), 256, 0, st>>>(
+                             L_, P_, f.G, coords, n, grad_out, glines, gplanes)));
+  return check_launch("vm_features_bwd");
+}
+
+int launch_density_fwd(const FieldView& f, float shift, const float* origins, const float* dirs,
+                       int64_t R, const SamplerArgs& s, float* sigma, cudaStream_t st) {
+  const int64_t total = R * s.N;
+  if (total == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (density_fwd_kernel<TT, CC><<<quad_blocks(total), 256, 0, st>>>(
+                             L_, P_, f.G, shift, origins, dirs, total, s, sigma)));
+  return check_launch("density_fwd");
+}
+
+int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
+                       const float* dirs, int64_t R, const SamplerArgs& s, const float* gsum,
+                       cudaStream_t st) {
+  const int64_t total = R * s.N;
+  if (total == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (density_bwd_kernel<TT, CC><<<quad_blocks(total), 256, 0, st>>>(
+                             L_, P_, f.G, glines, gplanes, origins, dirs, total, s, gsum)));
+  return check_launch("density_bwd");
+}
+
+int launch_appearance_fwd(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                          const SamplerArgs& s, const int32_t* sel_idx, int k, float* X0,
+                          cudaStream_t st) {
+  const int64_t rows = R * k;
+  if (rows == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (appearance_fwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
+                             L_, P_, f.G, origins, dirs, rows, k, s, sel_idx, X0)));
+  return check_launch("appearance_fwd");
+}
+
+int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
+                          const float* dirs, int64_t R, const SamplerArgs& s,
+                          const int32_t* sel_idx, int k, const float* dX0, cudaStream_t st) {
+  const int64_t rows = R * k;
+  if (rows == 0) return TVM_OK;
+  TVM_DISPATCH_FIELD(f, (appearance_bwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
+                             L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx,
+                             dX0)));
+  return check_launch("appearance_bwd");
+}
+
+int launch_points(const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                  float* points, float* ts, float* steps, cudaStream_t st) {
+  const int64_t total = R * s.N;
+  if (total == 0) return TVM_OK;
+  points_kernel<<<(unsigned)ceil_div(total, 256), 256, 0, st>>>(origins, dirs, total, s, points,
+                                                                 ts, steps);
+  return check_launch("sample_points");
+}
+
+int launch_to_channel_last(int G, int C, const float* vec, const float* mat, int dtype, void* lines,
+                           void* planes, cudaStream_t st) {
+  const int64_t n = 3LL * G * C * (G + 1);
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
+  if (dtype == TVM_F32) {
+    to_channel_last_kernel<float><<<blocks, 256, 0, st>>>(G, C, vec, mat, (float*)lines,
+                                                          (float*)planes);
+  } else if (dtype == TVM_BF16) {
+    to_channel_last_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(
+        G, C, vec, mat, (__nv_bfloat16*)lines, (__nv_bfloat16*)planes);
+  } else {
+    set_error("to_channel_last: dtype %d not supported", dtype);
+    return TVM_ERR_DTYPE;
+  }
+  return check_launch("to_channel_last");
+}
+
+int launch_to_channel_first(int G, int C, const float* lines, const float* planes, float* vec,
+                            float* mat, cudaStream_t st) {
+  const int64_t n = 3LL * G * C * (G + 1);
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
+  to_channel_first_kernel<<<blocks, 256, 0, st>>>(G, C, lines, planes, vec, mat);
+  return check_launch("to_channel_first");
+}
+
+}  // namespace tvm

@@ -1,0 +1,461 @@
+"""GB300 twin of ``tensorf/render.py``.
+
+Same public names as the reference (``RenderMode``, ``RenderConfig``,
+``LearnableParams``, ``render_rays``, ``render_rays_batched``,
+``compute_segment_probabilities``, ``sample_points_along_ray_within_bbox``), backed by
+the C ABI. Differences at the boundary, all deliberate:
+
+* Randomness: the reference threads a JAX PRNG key; here ``prng_key`` is a
+  :class:`NoiseKey` (seed, stream) from which the device draws sample jitter and the
+  Gumbel noise of the weighted choice, or a :class:`RenderNoise` holding explicit arrays
+  (so the reference's own draws can be replayed bit for bit).
+* Parameters: ``LearnableParams`` owns one flat FP32 parameter buffer (plus a bf16
+  shadow of the field tensors in BF16 mode); ``density_tensor``,
+  ``appearance_tensor`` and ``appearance_mlp_params`` are views into it.
+* ``density_shift`` (default +10.0, render.py:207) is a keyword.
+* ``RenderMode.DIST_MEDIAN`` returns the distance of the first sample where
+  1 - p_exit > 0.5 (+inf if none). The reference formula (render.py:248-267) returns
+  NaN for every ray that terminates, because it multiplies 0 by inf.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import math
+from typing import Dict, Optional, Sequence, Tuple, Union
+
+import numpy as onp
+import torch
+
+from . import _lib, cameras, networks
+from ._util import ptr, require_cuda, stream_handle, workspace
+from .tensor_vm import TensorVM
+
+
+class RenderMode(enum.Enum):
+    RGB = enum.auto()
+    DIST_MEDIAN = enum.auto()
+    DIST_MEAN = enum.auto()
+
+
+_MODE_CODE = {RenderMode.RGB: _lib.TVM_MODE_RGB, RenderMode.DIST_MEDIAN: _lib.TVM_MODE_DIST_MEDIAN,
+              RenderMode.DIST_MEAN: _lib.TVM_MODE_DIST_MEAN}
+
+
+@dataclasses.dataclass(frozen=True)
+class RenderConfig:
+    """render.py:26-36."""
+    near: float
+    far: float
+    mode: RenderMode
+    density_samples_per_ray: int
+    appearance_samples_per_ray: int
+
+
+@dataclasses.dataclass(frozen=True)
+class ModelSpec:
+    """Sizes of the two VM tensors and the FeatureMlp, and the arithmetic mode."""
+    grid_dim: int
+    density_feat_dim: int = 16
+    appearance_feat_dim: int = 48
+    feature_n_freqs: int = 2
+    viewdir_n_freqs: int = 2
+    squash_dim: int = 27
+    units: int = 128
+    precision: str = "fp32"  # "fp32" or "bf16"
+
+    def desc(self) -> _lib.ModelDesc:
+        return _lib.ModelDesc(grid_dim=self.grid_dim, density_channels=self.density_feat_dim,
+                              appearance_channels=self.appearance_feat_dim,
+                              feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs,
+                              squash_dim=self.squash_dim, units=self.units,
+                              dtype=_lib.TVM_BF16 if self.precision == "bf16" else _lib.TVM_F32)
+
+    def mlp(self) -> networks.FeatureMlp:
+        return networks.FeatureMlp(feature_squash_dim=self.squash_dim, units=self.units,
+                                   feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs)
+
+
+def param_layout(spec: ModelSpec) -> _lib.ParamLayout:
+    lay = _lib.ParamLayout()
+    md = spec.desc()
+    _lib.call("tvm_get_param_layout", ctypes.byref(md), ctypes.byref(lay))
+    return lay
+
+
+class LearnableParams:
+    """render.py:39-46: appearance MLP params, appearance tensor, density tensor and the
+    scene-contraction flag, held in one flat device buffer."""
+
+    def __init__(self, spec: ModelSpec, params: torch.Tensor, shadow: Optional[torch.Tensor] = None,
+                 scene_contraction: bool = False):
+        self.spec = spec
+        self.layout = param_layout(spec)
+        if params.numel() != self.layout.total or params.dtype != torch.float32 or not params.is_cuda:
+            raise ValueError("params must be a CUDA float32 buffer of layout.total elements")
+        self.params = params
+        if spec.precision == "bf16" and shadow is None:
+            shadow = torch.empty(self.layout.shadow_total, dtype=torch.bfloat16, device=params.device)
+            self._md = spec.desc()
+            self.refresh_shadow()
+        self.shadow = shadow
+        self.scene_contraction = scene_contraction
+        self._md = spec.desc()
+
+    # ---- views -----------------------------------------------------------------
+    def model_desc(self) -> _lib.ModelDesc:
+        return self._md
+
+    def _seg(self, off: int, shape, buf=None) -> torch.Tensor:
+        buf = self.params if buf is None else buf
+        n = int(onp.prod(shape))
+        return buf[off:off + n].view(*shape)
+
+    def field_views(self, which: str, buf: Optional[torch.Tensor] = None):
+        L, s = self.layout, self.spec
+        g = s.grid_dim
+        c = s.density_feat_dim if which == "density" else s.appearance_feat_dim
+        lo = L.density_lines if which == "density" else L.appearance_lines
+        po = L.density_planes if which == "density" else L.appearance_planes
+        return self._seg(lo, (3, g, c), buf), self._seg(po, (3, g, g, c), buf)
+
+    @property
+    def density_tensor(self) -> TensorVM:
+        return TensorVM(*self.field_views("density"))
+
+    @property
+    def appearance_tensor(self) -> TensorVM:
+        return TensorVM(*self.field_views("appearance"))
+
+    def mlp_views(self, buf: Optional[torch.Tensor] = None) -> Dict[str, Dict[str, torch.Tensor]]:
+        L, s = self.layout, self.spec
+        enc = L.encoded_dim
+        f = 3 * s.appearance_feat_dim
+        return {
+            "Dense_0": {"kernel": self._seg(L.mlp_w0, (f, s.squash_dim), buf)},
+            "Dense_1": {"kernel": self._seg(L.mlp_w1, (enc, s.units), buf), "bias": self._seg(L.mlp_b1, (s.units,), buf)},
+            "Dense_2": {"kernel": self._seg(L.mlp_w2, (s.units, s.units), buf), "bias": self._seg(L.mlp_b2, (s.units,), buf)},
+            "Dense_3": {"kernel": self._seg(L.mlp_w3, (s.units, 3), buf), "bias": self._seg(L.mlp_b3, (3,), buf)},
+        }
+
+    @property
+    def appearance_mlp_params(self):
+        return self.mlp_views()
+
+    # ---- construction ----------------------------------------------------------
+    @staticmethod
+    def initialize(spec: ModelSpec, seed: int = 94709, scene_contraction: bool = False,
+                   device="cuda") -> "LearnableParams":
+        """TrainState.initialize's parameter init (training.py:35-99): N(0, 0.1^2)
+        field tensors, flax-style MLP init."""
+        require_cuda()
+        gen = torch.Generator().manual_seed(seed)
+        g = spec.grid_dim
+        ref = {
+            "density": (torch.randn((3, spec.density_feat_dim, g), generator=gen) * 0.1,
+                        torch.randn((3, spec.density_feat_dim, g, g), generator=gen) * 0.1),
+            "appearance": (torch.randn((3, spec.appearance_feat_dim, g), generator=gen) * 0.1,
+                           torch.randn((3, spec.appearance_feat_dim, g, g), generator=gen) * 0.1),
+            "mlp": spec.mlp().init_params(3 * spec.appearance_feat_dim, gen),
+        }
+        return LearnableParams.from_reference(spec, ref, scene_contraction, device)
+
+    @staticmethod
+    def from_reference(spec: ModelSpec, ref: dict, scene_contraction: bool = False,
+                       device="cuda") -> "LearnableParams":
+        """From reference-layout arrays: ref['density'] = (vector (3,C,G), matrix
+        (3,C,G,G)), ref['appearance'] likewise, ref['mlp'] = flax tree."""
+        require_cuda()
+        lay = param_layout(spec)
+        params = torch.zeros(lay.total, dtype=torch.float32, device=device)
+        lp = LearnableParams.__new__(LearnableParams)
+        lp.spec, lp.layout, lp.params, lp.shadow, lp.scene_contraction = spec, lay, params, None, scene_contraction
+        lp._md = spec.desc()
+        for which in ("density", "appearance"):
+            vec, mat = ref[which]
+            lines, planes = lp.field_views(which)
+            g, c = spec.grid_dim, lines.shape[-1]
+            v = vec.to(device=device, dtype=torch.float32).contiguous()
+            m = mat.to(device=device, dtype=torch.float32).contiguous()
+            _lib.call("tvm_vm_to_channel_last", g, c, ptr(v), ptr(m), _lib.TVM_F32, ptr(lines), ptr(planes),
+                      stream_handle())
+        views = lp.mlp_views()
+        for layer, d in ref["mlp"].items():
+            for name, val in d.items():
+                views[layer][name].copy_(torch.as_tensor(val, dtype=torch.float32))
+        if spec.precision == "bf16":
+            lp.shadow = torch.empty(lay.shadow_total, dtype=torch.bfloat16, device=device)
+            lp.refresh_shadow()
+        return lp
+
+    def to_reference(self, buf: Optional[torch.Tensor] = None) -> dict:
+        """Reference-layout CPU float32 copies of params (or of a same-layout buffer
+        such as gradients)."""
+        out = {}
+        for which in ("density", "appearance"):
+            lines, planes = self.field_views(which, buf)
+            out[which] = (lines.permute(0, 2, 1).contiguous().cpu(), planes.permute(0, 3, 1, 2).contiguous().cpu())
+        out["mlp"] = {k: {n: t.detach().cpu().clone() for n, t in d.items()} for k, d in self.mlp_views(buf).items()}
+        return out
+
+    def refresh_shadow(self) -> None:
+        if self.spec.precision == "bf16":
+            _lib.call("tvm_refresh_shadow", ctypes.byref(self._md), ptr(self.params), ptr(self.shadow),
+                      stream_handle())
+
+
+# ---------------------------------------------------------------------------------
+# Randomness.
+# ---------------------------------------------------------------------------------
+@dataclasses.dataclass(frozen=True)
+class NoiseKey:
+    """Stand-in for a JAX PRNG key: a seed and a stream id. ``split`` derives two
+    independent keys, like ``jax.random.split``; the device draws the noise."""
+    seed: int
+    stream: int = 0
+
+    def split(self) -> Tuple["NoiseKey", "NoiseKey"]:
+        return NoiseKey(self.seed, self.stream * 2 + 1), NoiseKey(self.seed, self.stream * 2 + 2)
+
+    def uniform(self, n: int, device="cuda") -> torch.Tensor:
+        out = torch.empty(n, dtype=torch.float32, device=device)
+        _lib.call("tvm_noise_fill", ptr(out), n, self.seed & (2**64 - 1), self.stream & (2**64 - 1), 0, stream_handle())
+        return out
+
+    def gumbel(self, n: int, device="cuda") -> torch.Tensor:
+        out = torch.empty(n, dtype=torch.float32, device=device)
+        _lib.call("tvm_noise_fill", ptr(out), n, self.seed & (2**64 - 1), self.stream & (2**64 - 1), 1, stream_handle())
+        return out
+
+
+@dataclasses.dataclass
+class RenderNoise:
+    """Explicit noise: ``jitter`` (N,) shared by all rays (bounded scenes, as the
+    reference draws it) or (R, N); ``gumbel`` (N,) shared or (R, N)."""
+    jitter: Optional[torch.Tensor]
+    gumbel: Optional[torch.Tensor]
+
+
+def draw_noise(key: NoiseKey, rays: int, config: RenderConfig, scene_contraction: bool) -> RenderNoise:
+    """Draw the noise render_rays needs from a key: the sample key drives the jitter
+    ((N,) shared for bounded scenes, (R, N) for contracted ones, render.py:158-160,
+    375-379) and the rgb key the Gumbel noise shared by every ray (render.py:461-469)."""
+    sample_key, rgb_key = key.split()
+    n = config.density_samples_per_ray
+    jitter = sample_key.uniform(rays * n if scene_contraction else n)
+    if scene_contraction:
+        jitter = jitter.view(rays, n)
+    gumbel = rgb_key.gumbel(n) if config.mode is RenderMode.RGB else None
+    return RenderNoise(jitter=jitter, gumbel=gumbel)
+
+
+# ---------------------------------------------------------------------------------
+# Descriptors.
+# ---------------------------------------------------------------------------------
+def contracted_schedule(near: float, far: float, n: int) -> onp.ndarray:
+    """render.py:127-151: linear close half, heuristic far half (float64 -> float32)."""
+    close_n = n // 2
+    far_n = n - close_n
+    close_ts = onp.linspace(near, near + 1.0, close_n).astype(onp.float32)
+    far_start = near + 1.0 + 1.0 / close_n
+    k = 10.0
+    far_deltas = (1.0 / (1.0 - onp.linspace(0.0, 1.0 - 1 / ((far - far_start) / k + 1), far_n)) - 1.0) \
+        * onp.linspace(1.0, k, far_n)
+    return onp.concatenate([close_ts, (far_start + far_deltas).astype(onp.float32)])
+
+
+def disparity_schedule(near: float, far: float, n: int) -> onp.ndarray:
+    """Samples linear in disparity between near and far."""
+    s = onp.linspace(0.0, 1.0, n)
+    return (1.0 / ((1.0 - s) / near + s / far)).astype(onp.float32)
+
+
+def _aabb6(aabb) -> Sequence[float]:
+    a = torch.as_tensor(aabb, dtype=torch.float32).reshape(2, 3).cpu()
+    return [float(v) for v in a[0]] + [float(v) for v in a[1]]
+
+
+def make_render_desc(config: RenderConfig, aabb, noise: RenderNoise, rays: int, scene_contraction: bool,
+                     schedule: Optional[torch.Tensor], density_shift: float, mode: Optional[RenderMode] = None):
+    mode = config.mode if mode is None else mode
+    d = _lib.RenderDesc()
+    d.density_samples = config.density_samples_per_ray
+    d.appearance_samples = config.appearance_samples_per_ray
+    d.mode = _MODE_CODE[mode]
+    d.sampler = _lib.TVM_SAMPLER_CONTRACT if scene_contraction else _lib.TVM_SAMPLER_BBOX
+    d.density_shift = density_shift
+    for i, v in enumerate(_aabb6(aabb)):
+        d.aabb[i] = v
+    d.schedule = ptr(schedule).value if schedule is not None else None
+    d.jitter = ptr(noise.jitter).value if noise.jitter is not None else None
+    d.jitter_per_ray = int(noise.jitter is not None and noise.jitter.dim() == 2 and not scene_contraction)
+    d.gumbel = ptr(noise.gumbel).value if noise.gumbel is not None else None
+    d.gumbel_per_ray = int(noise.gumbel is not None and noise.gumbel.dim() == 2)
+    return d
+
+
+def rays_struct(rays: "cameras.Rays3D") -> _lib.Rays:
+    o = rays.origins.reshape(-1, 3)
+    dvec = rays.directions.reshape(-1, 3)
+    return _lib.Rays(count=o.shape[0], origins=ptr(o, torch.float32, "origins"),
+                     directions=ptr(dvec, torch.float32, "directions"))
+
+
+def _schedule_for(config: RenderConfig, scene_contraction: bool, schedule) -> Optional[torch.Tensor]:
+    if not scene_contraction:
+        return None
+    if schedule is None:
+        schedule = contracted_schedule(config.near, config.far, config.density_samples_per_ray)
+    return torch.as_tensor(schedule, dtype=torch.float32, device="cuda").contiguous()
+
+
+# ---------------------------------------------------------------------------------
+# render_rays.
+# ---------------------------------------------------------------------------------
+def render_rays(appearance_mlp: networks.FeatureMlp, learnable_params: LearnableParams, aabb,
+                rays_wrt_world: "cameras.Rays3D", prng_key: Union[NoiseKey, RenderNoise],
+                config: RenderConfig, *, density_shift: float = 10.0, schedule=None) -> torch.Tensor:
+    """render.py:105-279. Output (R, 3) for RGB, (R,) for distances."""
+    require_cuda()
+    o = rays_wrt_world.origins.reshape(-1, 3)
+    r = o.shape[0]
+    sc = learnable_params.scene_contraction
+    noise = prng_key if isinstance(prng_key, RenderNoise) else draw_noise(prng_key, r, config, sc)
+    sched = _schedule_for(config, sc, schedule)
+    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift)
+    md = learnable_params.model_desc()
+    rs = rays_struct(rays_wrt_world)
+    nbytes = _lib.load().tvm_render_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
+    if nbytes == 0:
+        raise ValueError("invalid render configuration: " + _lib.load().tvm_last_error_message().decode())
+    ws = workspace(nbytes, o.device)
+    shape = (r, 3) if config.mode is RenderMode.RGB else (r,)
+    out = torch.empty(shape, dtype=torch.float32, device=o.device)
+    _lib.call("tvm_render_fwd", ctypes.byref(md), ptr(learnable_params.params), ptr(learnable_params.shadow),
+              ctypes.byref(rs), ctypes.byref(desc), ptr(out), ptr(ws), ws.numel(), stream_handle())
+    return out
+
+
+def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: LearnableParams, aabb,
+                        rays_wrt_world: "cameras.Rays3D", prng_key, config: RenderConfig, *,
+                        batch_size: int = 4096, use_tqdm: bool = False, density_shift: float = 10.0,
+                        to_host: bool = True):
+    """render.py:49-102: chunks of ``batch_size`` rays, concatenated. Rays stay on the
+    device; ``to_host`` returns a NumPy array like the reference."""
+    batch_axes = rays_wrt_world.origins.shape[:-1]
+    o = rays_wrt_world.origins.reshape(-1, 3).to("cuda", torch.float32)
+    d = rays_wrt_world.directions.reshape(-1, 3).to("cuda", torch.float32)
+    total = o.shape[0]
+    outs = []
+    for start in range(0, total, batch_size):
+        chunk = cameras.Rays3D(origins=o[start:start + batch_size], directions=d[start:start + batch_size])
+        outs.append(render_rays(appearance_mlp, learnable_params, aabb, chunk, prng_key, config,
+                                density_shift=density_shift))
+    out = torch.cat(outs, dim=0)
+    out = out.reshape(tuple(batch_axes) + tuple(out.shape[1:]))
+    return out.cpu().numpy() if to_host else out
+
+
+def loss_and_grad(learnable_params: LearnableParams, grads: torch.Tensor, aabb, rays_wrt_world,
+                  colors: torch.Tensor, noise: RenderNoise, config: RenderConfig, *, density_shift: float = 10.0,
+                  schedule=None) -> torch.Tensor:
+    """MSE of render_rays against colors and its gradient, ACCUMULATED into ``grads``
+    (flat layout). Returns the loss as a device scalar."""
+    o = rays_wrt_world.origins.reshape(-1, 3)
+    r = o.shape[0]
+    sc = learnable_params.scene_contraction
+    sched = _schedule_for(config, sc, schedule)
+    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift)
+    md = learnable_params.model_desc()
+    rs = rays_struct(rays_wrt_world)
+    nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
+    if nbytes == 0:
+        raise ValueError("invalid configuration: " + _lib.load().tvm_last_error_message().decode())
+    ws = workspace(nbytes, o.device)
+    loss = torch.zeros(1, dtype=torch.float32, device=o.device)
+    _lib.call("tvm_loss_and_grad", ctypes.byref(md), ptr(learnable_params.params), ptr(learnable_params.shadow),
+              ptr(grads), ctypes.byref(rs), ptr(colors.contiguous()), ctypes.byref(desc), ptr(loss), ptr(ws),
+              ws.numel(), stream_handle())
+    return loss
+
+
+# ---------------------------------------------------------------------------------
+# Seams.
+# ---------------------------------------------------------------------------------
+@dataclasses.dataclass
+class SegmentProbabilities:
+    """render.py:282-297."""
+    p_exits: torch.Tensor
+    p_terminates: torch.Tensor
+
+    def get_batch_axes(self):
+        return tuple(self.p_exits.shape)
+
+
+class _Segment(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sigmas, steps):
+        r, n = sigmas.shape
+        pe = torch.empty_like(sigmas)
+        pt = torch.empty_like(sigmas)
+        _lib.call("tvm_composite_fwd", ptr(sigmas), ptr(steps), r, n, ptr(pe), ptr(pt), stream_handle())
+        ctx.save_for_backward(sigmas, steps)
+        return pe, pt
+
+    @staticmethod
+    def backward(ctx, gpe, gpt):
+        sigmas, steps = ctx.saved_tensors
+        r, n = sigmas.shape
+        gs = torch.empty_like(sigmas)
+        _lib.call("tvm_composite_bwd", ptr(sigmas), ptr(steps), r, n,
+                  ptr(gpe.contiguous()) if gpe is not None else ptr(None),
+                  ptr(gpt.contiguous()) if gpt is not None else ptr(None), ptr(gs), stream_handle())
+        return gs, None
+
+
+def compute_segment_probabilities(sigmas: torch.Tensor, step_sizes: torch.Tensor) -> SegmentProbabilities:
+    """render.py:300-347 (sigmas and step_sizes of shape (*, N))."""
+    batch = sigmas.shape
+    s = sigmas.reshape(-1, batch[-1]).to(torch.float32).contiguous()
+    st = step_sizes.reshape(-1, batch[-1]).to(torch.float32).contiguous()
+    pe, pt = _Segment.apply(s, st)
+    return SegmentProbabilities(pe.reshape(batch), pt.reshape(batch))
+
+
+def sample_points(rays_wrt_world: "cameras.Rays3D", aabb, config: RenderConfig, noise: RenderNoise,
+                  scene_contraction: bool = False, schedule=None):
+    """The sampler of render_rays (render.py:122-190) plus normalisation
+    (render.py:192-196): points (3, R, N) in [-1, 1], ts (R, N), step_sizes (R, N)."""
+    r = rays_wrt_world.origins.reshape(-1, 3).shape[0]
+    n = config.density_samples_per_ray
+    sched = _schedule_for(config, scene_contraction, schedule)
+    desc = make_render_desc(config, aabb, noise, r, scene_contraction, sched, 10.0, mode=RenderMode.DIST_MEAN)
+    rs = rays_struct(rays_wrt_world)
+    pts = torch.empty((3, r, n), dtype=torch.float32, device="cuda")
+    ts = torch.empty((r, n), dtype=torch.float32, device="cuda")
+    steps = torch.empty((r, n), dtype=torch.float32, device="cuda")
+    _lib.call("tvm_sample_points", ctypes.byref(rs), ctypes.byref(desc), ptr(pts), ptr(ts), ptr(steps),
+              stream_handle())
+    return pts, ts, steps
+
+
+def sample_points_along_ray_within_bbox(rays_wrt_world, aabb, samples_per_ray: int, jitter: Optional[torch.Tensor]):
+    """render.py:350-390 vmapped over rays; un-normalised points (3, R, N), ts (R, N)
+    and the per-ray step (R,)."""
+    cfg = RenderConfig(near=0.0, far=1.0, mode=RenderMode.DIST_MEAN, density_samples_per_ray=samples_per_ray,
+                       appearance_samples_per_ray=1)
+    pts, ts, steps = sample_points(rays_wrt_world, aabb, cfg, RenderNoise(jitter=jitter, gumbel=None))
+    a = torch.as_tensor(aabb, dtype=torch.float32, device="cuda").reshape(2, 3)
+    world = (pts / 2.0 + 0.5) * (a[1] - a[0])[:, None, None] + a[0][:, None, None]
+    return world, ts, steps[:, 0]
+
+
+def weighted_choice(p: torch.Tensor, gumbel: torch.Tensor, k: int) -> torch.Tensor:
+    """jax.random.choice(replace=False, p=p) per row with explicit Gumbel noise
+    (render.py:459-470): the k largest log(p) + g, largest first, ties -> lower index."""
+    r, n = p.shape
+    idx = torch.empty((r, k), dtype=torch.int32, device=p.device)
+    _lib.call("tvm_topk_select", ptr(p.contiguous()), ptr(gumbel.contiguous()), int(gumbel.dim() == 2), r, n, k,
+              ptr(idx), stream_handle())
+    return idx

@@ -1,0 +1,103 @@
+"""Seeded synthetic workloads.
+
+* ``sphere_rays`` -- rays whose origins are uniform on a sphere of radius 4, aimed at
+  the origin with N(0, 0.05^2) jitter on the direction, and uniform [0, 1) targets (the
+  CPU-runnable 4096-ray workload).
+* ``SphereScene`` -- an analytic scene of constant-density spheres (radius U[0.1, 0.4],
+  density 50, colour U[0, 1]) seen by seeded 800x800 pinhole cameras with focal length
+  1111 on a sphere of radius 4 around the origin. Target colours come from an FP64
+  quadrature (4096 midpoint samples per ray over the aabb segment) on the device. It
+  stands in for the Blender lego scene, which is not available here.
+* ``unbounded_rays`` -- origins within radius 1, directions uniform on the sphere.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import List, Tuple
+
+import numpy as onp
+import torch
+
+from . import _lib, cameras
+from ._util import ptr, stream_handle
+
+
+def sphere_rays(n: int, seed: int, radius: float = 4.0, jitter: float = 0.05):
+    rng = onp.random.default_rng(seed)
+    o = rng.normal(size=(n, 3))
+    o = o / onp.linalg.norm(o, axis=1, keepdims=True) * radius
+    d = -o + rng.normal(scale=jitter, size=(n, 3))
+    d = d / onp.linalg.norm(d, axis=1, keepdims=True)
+    colors = rng.uniform(size=(n, 3))
+    return o.astype(onp.float32), d.astype(onp.float32), colors.astype(onp.float32)
+
+
+def unbounded_rays(n: int, seed: int):
+    rng = onp.random.default_rng(seed)
+    v = rng.normal(size=(n, 3))
+    v /= onp.linalg.norm(v, axis=1, keepdims=True)
+    o = v * rng.uniform(size=(n, 1)) ** (1.0 / 3.0)
+    d = rng.normal(size=(n, 3))
+    d /= onp.linalg.norm(d, axis=1, keepdims=True)
+    return o.astype(onp.float32), d.astype(onp.float32)
+
+
+@dataclasses.dataclass
+class SphereScene:
+    centers: onp.ndarray  # (S, 3) float64
+    radii: onp.ndarray    # (S,)
+    colors: onp.ndarray   # (S, 3)
+    density: float = 50.0
+    aabb: Tuple[Tuple[float, ...], Tuple[float, ...]] = ((-1.5, -1.5, -1.5), (1.5, 1.5, 1.5))
+
+    @staticmethod
+    def random(seed: int, count: int = 32, extent: float = 1.0) -> "SphereScene":
+        rng = onp.random.default_rng(seed)
+        return SphereScene(centers=rng.uniform(-extent, extent, size=(count, 3)),
+                           radii=rng.uniform(0.1, 0.4, size=count),
+                           colors=rng.uniform(0.0, 1.0, size=(count, 3)))
+
+    def cameras(self, count: int, seed: int, width: int = 800, height: int = 800, focal: float = 1111.0,
+                radius: float = 4.0) -> List[cameras.Camera]:
+        rng = onp.random.default_rng(seed)
+        cams = []
+        for _ in range(count):
+            v = rng.normal(size=3)
+            v /= onp.linalg.norm(v)
+            R, eye = cameras.look_at(v * radius)
+            cams.append(cameras.Camera.from_focal(R, eye, width, height, focal))
+        return cams
+
+    def render(self, rays: cameras.Rays3D, n_samples: int = 4096) -> torch.Tensor:
+        """FP64 quadrature of the scene along each ray (tvm_sphere_scene_render)."""
+        dev = "cuda"
+        c = torch.as_tensor(self.centers, dtype=torch.float64, device=dev).contiguous()
+        r = torch.as_tensor(self.radii, dtype=torch.float64, device=dev).contiguous()
+        col = torch.as_tensor(self.colors, dtype=torch.float64, device=dev).contiguous()
+        aabb = torch.tensor(list(self.aabb[0]) + list(self.aabb[1]), dtype=torch.float32, device=dev)
+        o = rays.origins.reshape(-1, 3).contiguous()
+        d = rays.directions.reshape(-1, 3).contiguous()
+        out = torch.empty((o.shape[0], 3), dtype=torch.float32, device=dev)
+        rs = _lib.Rays(count=o.shape[0], origins=ptr(o), directions=ptr(d))
+        _lib.call("tvm_sphere_scene_render", ptr(c), ptr(r), ptr(col), len(self.radii), float(self.density),
+                  ptr(aabb), ctypes.byref(rs), n_samples, ptr(out), stream_handle())
+        return out
+
+    def training_rays(self, cams: List[cameras.Camera], total: int, seed: int,
+                      n_samples: int = 4096) -> Tuple[cameras.Rays3D, torch.Tensor]:
+        """``total`` random pixels over the cameras with their FP64 target colours."""
+        rng = onp.random.default_rng(seed)
+        per = [total // len(cams) + (1 if i < total % len(cams) else 0) for i in range(len(cams))]
+        os_, ds_ = [], []
+        for cam, n in zip(cams, per):
+            if n == 0:
+                continue
+            pix = torch.as_tensor(rng.integers(0, cam.image_width * cam.image_height, size=n), dtype=torch.int64)
+            rr = cam.pixel_rays_wrt_world(pix)
+            os_.append(rr.origins)
+            ds_.append(rr.directions)
+        rays = cameras.Rays3D(origins=torch.cat(os_), directions=torch.cat(ds_))
+        perm = torch.as_tensor(rng.permutation(total), device="cuda")
+        rays = cameras.Rays3D(origins=rays.origins[perm].contiguous(), directions=rays.directions[perm].contiguous())
+        return rays, self.render(rays, n_samples)

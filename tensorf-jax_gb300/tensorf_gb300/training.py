@@ -1,0 +1,138 @@
+"""GB300 twin of the training step of ``tensorf/training.py``.
+
+``TrainState`` owns the flat parameter buffer, its gradient and Adam moments, and
+runs one ``training_step`` as a single ``tvm_train_step`` call: sampling, density
+VM, compositing and selection, appearance VM, MLP, MSE loss, the full backward and the
+fused Adam update (training.py:101-205, 207-243). The learning-rate schedule and its
+reset after grid upsampling (training.py:158-181) are host arithmetic.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import Optional, Tuple
+
+import numpy as onp
+import torch
+
+from . import _lib, cameras, render, utils
+from ._util import ptr, stream_handle, workspace
+
+
+@dataclasses.dataclass(frozen=True)
+class OptimizerConfig:
+    """train_config.py:6-12."""
+    lr_init_tensor: float = 0.02
+    lr_init_mlp: float = 1e-3
+    lr_decay_iters: Optional[int] = None
+    lr_decay_target_ratio: float = 0.1
+    lr_upsample_reset: bool = True
+
+
+@dataclasses.dataclass(frozen=True)
+class TrainConfig:
+    """The fields of TensorfConfig (train_config.py:15-71) the step uses."""
+    minibatch_size: int = 4096
+    n_iters: int = 30000
+    optimizer: OptimizerConfig = OptimizerConfig()
+    initial_aabb_min: Tuple[float, float, float] = (-1.0, -1.0, -1.0)
+    initial_aabb_max: Tuple[float, float, float] = (1.0, 1.0, 1.0)
+    upsamp_iters: Tuple[int, ...] = (2000, 3000, 4000, 5500, 7000)
+    scene_contraction: bool = False
+    render_near: float = 0.05
+    render_far: float = 200.0
+    train_ray_sample_multiplier: float = 1.0
+    density_samples_per_ray: Optional[int] = None  # None: the reference heuristic
+    appearance_samples_per_ray: Optional[int] = None
+    density_shift: float = 10.0
+
+
+def lr_decay_coeff(step: int, cfg: TrainConfig) -> float:
+    """training.py:158-181 (optax.exponential_decay with end_value)."""
+    o = cfg.optimizer
+    if o.lr_upsample_reset:
+        deltas = [step - s for s in (0,) + tuple(cfg.upsamp_iters)]
+        s = min(d if d >= 0 else 2**31 - 1 for d in deltas)
+    else:
+        s = step
+    di = cfg.n_iters if o.lr_decay_iters is None else o.lr_decay_iters
+    if s <= 0:
+        return 1.0
+    v = float(onp.power(onp.float32(o.lr_decay_target_ratio), onp.float32(s) / onp.float32(di)))
+    return max(v, o.lr_decay_target_ratio)
+
+
+def sample_counts(grid_dim: int, cfg: TrainConfig) -> Tuple[int, int]:
+    """training.py:115-118 heuristic unless overridden."""
+    import math
+    n = cfg.density_samples_per_ray or int(math.sqrt(3 * grid_dim**2) * cfg.train_ray_sample_multiplier)
+    k = cfg.appearance_samples_per_ray or int(0.15 * n)
+    return n, k
+
+
+class TrainState:
+    """training.py:19-33 with the training step; mutated in place (the reference
+    donates its state, training.py:101)."""
+
+    def __init__(self, config: TrainConfig, learnable_params: render.LearnableParams, seed: int = 94709):
+        self.config = config
+        self.learnable_params = learnable_params
+        self.appearance_mlp = learnable_params.spec.mlp()
+        p = learnable_params.params
+        self.grads = torch.zeros_like(p)
+        self.mu = torch.zeros_like(p)
+        self.nu = torch.zeros_like(p)
+        self.aabb = torch.tensor([config.initial_aabb_min, config.initial_aabb_max], dtype=torch.float32)
+        self.prng_key = render.NoiseKey(seed)
+        self.step = 0
+        self.loss = torch.zeros(1, dtype=torch.float32, device=p.device)
+        self._ws = None
+        self._ws_key = None
+
+    @staticmethod
+    def initialize(config: TrainConfig, spec: render.ModelSpec, seed: int = 94709) -> "TrainState":
+        lp = render.LearnableParams.initialize(spec, seed=seed, scene_contraction=config.scene_contraction)
+        return TrainState(config, lp, seed=seed)
+
+    def render_config(self) -> render.RenderConfig:
+        n, k = sample_counts(self.learnable_params.spec.grid_dim, self.config)
+        return render.RenderConfig(near=self.config.render_near, far=self.config.render_far,
+                                   mode=render.RenderMode.RGB, density_samples_per_ray=n,
+                                   appearance_samples_per_ray=k)
+
+    def adam_desc(self, count: int) -> _lib.AdamDesc:
+        o = self.config.optimizer
+        return _lib.AdamDesc(lr_tensor=o.lr_init_tensor, lr_mlp=o.lr_init_mlp, b1=0.9, b2=0.99, eps=1e-8,
+                             lr_decay=lr_decay_coeff(self.step, self.config), count=count, _pad=0)
+
+    def training_step(self, rays: cameras.Rays3D, colors: torch.Tensor,
+                      noise: Optional[render.RenderNoise] = None, log: bool = True):
+        """One step: returns (self, log_data). ``noise`` replaces the key-drawn noise."""
+        cfg = self.render_config()
+        r = rays.origins.reshape(-1, 3).shape[0]
+        lp = self.learnable_params
+        if noise is None:
+            render_key, self.prng_key = self.prng_key.split()
+            noise = render.draw_noise(render_key, r, cfg, lp.scene_contraction)
+        sched = render._schedule_for(cfg, lp.scene_contraction, None)
+        desc = render.make_render_desc(cfg, self.aabb, noise, r, lp.scene_contraction, sched,
+                                       self.config.density_shift)
+        md = lp.model_desc()
+        key = (r, cfg)
+        if self._ws_key != key:
+            nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
+            self._ws = workspace(nbytes, lp.params.device)
+            self._ws_key = key
+        adam = self.adam_desc(self.step + 1)
+        rs = render.rays_struct(rays)
+        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self.grads),
+                  ptr(self.mu), ptr(self.nu), ctypes.byref(adam), ctypes.byref(rs), ptr(colors.contiguous()),
+                  ctypes.byref(desc), ptr(self.loss), ptr(self._ws), self._ws.numel(), stream_handle())
+        self.step += 1
+        log_data = {}
+        if log:
+            mse = float(self.loss.item())
+            log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
+                        "train/lr_tensor": adam.lr_decay * self.config.optimizer.lr_init_tensor,
+                        "train/lr_mlp": adam.lr_decay * self.config.optimizer.lr_init_mlp}
+        return self, log_data

@@ -1,0 +1,146 @@
+"""CPU tests of the C ABI: the library loads, exports every symbol the header
+declares, and rejects bad arguments with the documented codes before touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from tensorf_gb300 import _lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "tensorf_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"TVM_API\s+[\w\s\*]+?\b(tvm_\w+)\s*\(", text)))
+
+
+def test_header_declares_what_binding_declares():
+    assert set(declared_symbols()) == set(_lib.exported_symbols())
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert lib.tvm_abi_version() == 1
+
+
+def _model(**kw):
+    d = dict(grid_dim=16, density_channels=16, appearance_channels=48, feature_n_freqs=2, viewdir_n_freqs=2,
+             squash_dim=27, units=128, dtype=_lib.TVM_F32)
+    d.update(kw)
+    return _lib.ModelDesc(**d)
+
+
+def test_param_layout_sizes():
+    lay = _lib.ParamLayout()
+    md = _model(grid_dim=300)
+    _lib.call("tvm_get_param_layout", ctypes.byref(md), ctypes.byref(lay))
+    assert lay.encoded_dim == 150
+    assert lay.density_planes - lay.density_lines >= 3 * 300 * 16
+    n_field = 3 * 300 * 16 * 301 + 3 * 300 * 48 * 301
+    n_mlp = 144 * 27 + 150 * 128 + 128 + 128 * 128 + 128 + 128 * 3 + 3
+    assert n_field + n_mlp <= lay.total <= n_field + n_mlp + 64 * 11
+    assert lay.mlp_begin >= n_field and lay.mlp_w0 == lay.mlp_begin
+    assert lay.shadow_total == 0
+
+
+def test_bf16_layout_has_shadow():
+    lay = _lib.ParamLayout()
+    md = _model(dtype=_lib.TVM_BF16)
+    _lib.call("tvm_get_param_layout", ctypes.byref(md), ctypes.byref(lay))
+    assert lay.shadow_total == lay.mlp_begin
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(density_channels=12), -5),
+    (dict(grid_dim=1), -2),
+    (dict(dtype=7), -3),
+    (dict(units=0), -2),
+])
+def test_bad_model_rejected(kw, code):
+    lay = _lib.ParamLayout()
+    md = _model(**kw)
+    st = _lib.load().tvm_get_param_layout(ctypes.byref(md), ctypes.byref(lay))
+    assert st == code
+    assert _lib.load().tvm_last_error_message()
+
+
+def _render(**kw):
+    d = _lib.RenderDesc()
+    d.density_samples = kw.get("N", 64)
+    d.appearance_samples = kw.get("k", 8)
+    d.mode = kw.get("mode", _lib.TVM_MODE_RGB)
+    d.sampler = kw.get("sampler", _lib.TVM_SAMPLER_BBOX)
+    d.density_shift = 10.0
+    for i, v in enumerate(kw.get("aabb", [-1, -1, -1, 1, 1, 1])):
+        d.aabb[i] = v
+    d.gumbel = kw.get("gumbel", 0x1000)
+    return d
+
+
+@pytest.mark.parametrize("kw", [
+    dict(k=65),                       # k > N
+    dict(k=0),
+    dict(N=0),
+    dict(aabb=[1, -1, -1, -1, 1, 1]),  # min > max
+    dict(gumbel=None),                # RGB without noise
+    dict(sampler=1),                  # contraction without schedule / jitter
+    dict(mode=9),
+])
+def test_bad_render_rejected_before_launch(kw):
+    md = _model()
+    rd = _render(**kw)
+    rays = _lib.Rays(count=4, origins=0x1000, directions=0x2000)
+    st = _lib.load().tvm_render_fwd(ctypes.byref(md), ctypes.c_void_p(0x1000), None, ctypes.byref(rays),
+                                    ctypes.byref(rd), ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), 1 << 20, None)
+    assert st in (-1, -2, -5), st
+    assert _lib.load().tvm_render_workspace_size(ctypes.byref(md), ctypes.byref(rd), 4) == 0
+
+
+def test_null_and_alignment_checks():
+    lib = _lib.load()
+    md = _model()
+    rd = _render()
+    rays = _lib.Rays(count=4, origins=0x1000, directions=0x2000)
+    st = lib.tvm_render_fwd(ctypes.byref(md), None, None, ctypes.byref(rays), ctypes.byref(rd),
+                            ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), 1 << 20, None)
+    assert st == -1
+    st = lib.tvm_render_fwd(ctypes.byref(md), ctypes.c_void_p(0x1004), None, ctypes.byref(rays), ctypes.byref(rd),
+                            ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), 1 << 20, None)
+    assert st == -4
+    bf = _model(dtype=_lib.TVM_BF16)
+    st = lib.tvm_render_fwd(ctypes.byref(bf), ctypes.c_void_p(0x1000), None, ctypes.byref(rays), ctypes.byref(rd),
+                            ctypes.c_void_p(0x1000), ctypes.c_void_p(0x1000), 1 << 20, None)
+    assert st == -1  # BF16 needs its shadow buffer
+
+
+def test_topk_and_composite_argument_checks():
+    lib = _lib.load()
+    assert lib.tvm_topk_select(ctypes.c_void_p(16), ctypes.c_void_p(16), 0, 4, 8, 9, ctypes.c_void_p(16), None) == -2
+    assert lib.tvm_topk_select(None, None, 0, 4, 8, 2, None, None) == -1
+    assert lib.tvm_composite_fwd(None, None, 4, 8, None, None, None) == -1
+    assert lib.tvm_composite_bwd(ctypes.c_void_p(16), ctypes.c_void_p(16), 4, 0, None, None,
+                                 ctypes.c_void_p(16), None) == -2
+
+
+def test_zero_rays_is_a_no_op():
+    lib = _lib.load()
+    md = _model()
+    rd = _render()
+    rays = _lib.Rays(count=0, origins=None, directions=None)
+    assert lib.tvm_render_fwd(ctypes.byref(md), ctypes.c_void_p(0x1000), None, ctypes.byref(rays),
+                              ctypes.byref(rd), None, None, 0, None) == 0
+    assert lib.tvm_topk_select(None, None, 0, 0, 8, 2, None, None) == 0
+
+
+def test_workspace_sizes_are_monotone_in_rays():
+    lib = _lib.load()
+    md = _model()
+    rd = _render()
+    a = lib.tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(rd), 1024)
+    b = lib.tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(rd), 4096)
+    c = lib.tvm_render_workspace_size(ctypes.byref(md), ctypes.byref(rd), 4096)
+    assert 0 < a < b and 0 < c < b

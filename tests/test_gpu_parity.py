@@ -1,0 +1,343 @@
+"""GPU parity: every CUDA entry point against the float64 CPU oracle on the same
+(float32-rounded) inputs and noise. Tolerances: 1e-4 relative for FP32 forward
+outputs, exact indices for the top-k selection (rays whose k-th / (k+1)-th keys lie
+within 1e-5 of each other are near-ties whose order float rounding may flip and are
+excluded from the exact comparison; they must stay rare)."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import tensorf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+
+
+def _rel_err(a, b):
+    a = torch.as_tensor(a, dtype=torch.float64).cpu()
+    b = torch.as_tensor(b, dtype=torch.float64).cpu()
+    return float((a - b).abs().max() / (b.abs().max() + 1e-30))
+
+
+@pytest.fixture(scope="module")
+def tg():
+    import tensorf_gb300
+    from tensorf_gb300 import cameras, render, scene, tensor_vm, training
+    tensorf_gb300.load_library()
+    return tensorf_gb300
+
+
+def _ref_params(G, Cd, Ca, seed, nf=2, nv=2):
+    gen = torch.Generator().manual_seed(seed)
+    p = {"density": O.vm_init(G, Cd, gen, torch.float32), "appearance": O.vm_init(G, Ca, gen, torch.float32),
+         "mlp": O.mlp_init(3 * Ca, nf, nv, gen, dtype=torch.float32)}
+    return p
+
+
+def _to64(p):
+    return {"density": tuple(t.double() for t in p["density"]), "appearance": tuple(t.double() for t in p["appearance"]),
+            "mlp": {k: {n: t.double() for n, t in d.items()} for k, d in p["mlp"].items()}}
+
+
+def _rays(R, seed):
+    from tensorf_gb300 import scene
+    o, d, c = scene.sphere_rays(R, seed)
+    return torch.tensor(o), torch.tensor(d), torch.tensor(c)
+
+
+@pytest.mark.parametrize("C", [8, 16, 24, 48])
+def test_vm_features_fwd_bwd(tg, C):
+    from tensorf_gb300.tensor_vm import TensorVM
+    gen = torch.Generator().manual_seed(C)
+    vec, mat = O.vm_init(17, C, gen, torch.float32)
+    coords = (torch.rand((3, 3000), generator=gen) * 2.6 - 1.3).float()  # includes out-of-range
+    coords[:, :6] = torch.tensor([[-1.0, 1.0, 0.0, -1.3, 1.3, 0.999999]] * 3)
+    vm = TensorVM.from_reference(vec, mat)
+    lines = vm.lines.clone().requires_grad_(True)
+    planes = vm.planes.clone().requires_grad_(True)
+    vm2 = TensorVM(lines, planes)
+    out = vm2.interpolate(coords.cuda())
+    ref_vec = vec.double().requires_grad_(True)
+    ref_mat = mat.double().requires_grad_(True)
+    ref = O.vm_interpolate(ref_vec, ref_mat, coords.double())
+    assert _rel_err(out, ref) < 1e-5
+    g = torch.randn(ref.shape, generator=gen, dtype=torch.float64)
+    (ref * g).sum().backward()
+    (out * g.float().cuda()).sum().backward()
+    gl = lines.grad.permute(0, 2, 1).cpu()
+    gp = planes.grad.permute(0, 3, 1, 2).cpu()
+    assert _rel_err(gl, ref_vec.grad) < 1e-5
+    assert _rel_err(gp, ref_mat.grad) < 1e-5
+
+
+def test_vm_features_bf16_storage(tg):
+    from tensorf_gb300.tensor_vm import TensorVM
+    gen = torch.Generator().manual_seed(3)
+    vec, mat = O.vm_init(33, 16, gen, torch.float32)
+    coords = torch.rand((3, 5000), generator=gen) * 2 - 1
+    vm = TensorVM.from_reference(vec, mat, dtype=torch.bfloat16)
+    out = vm.interpolate(coords.cuda())
+    ref = O.vm_interpolate(vec.bfloat16().double(), mat.bfloat16().double(), coords.double())
+    assert _rel_err(out, ref) < 1e-5
+
+
+def test_sample_points_bbox_and_contract(tg):
+    from tensorf_gb300 import cameras, render
+    o, d, _ = _rays(300, 1)
+    o[0] = torch.tensor([5.0, 5.0, 5.0])  # misses the box
+    d[0] = torch.tensor([1.0, 0.0, 0.0])
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
+    N = 96
+    jit = torch.rand(N, generator=torch.Generator().manual_seed(2))
+    rays = cameras.Rays3D(o.cuda(), d.cuda())
+    cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, N, 8)
+    pts, ts, st = render.sample_points(rays, aabb, cfg, render.RenderNoise(jit.cuda(), None))
+    rp, rts, rst = O.sample_points_bbox(o.double(), d.double(), aabb.double(), N, jit.double())
+    assert _rel_err(ts, rts) < 1e-5 and _rel_err(st, rst) < 1e-5
+    assert _rel_err(pts, O.normalize_points(rp, aabb.double())) < 1e-5
+    # Contracted sampler with the reference's heuristic schedule.
+    uo, ud = [torch.tensor(a) for a in tg.scene.unbounded_rays(200, 4)]
+    sched = torch.tensor(render.contracted_schedule(0.05, 200.0, N))
+    jit2 = torch.rand((200, N), generator=torch.Generator().manual_seed(3))
+    raysu = cameras.Rays3D(uo.cuda(), ud.cuda())
+    aabb2 = torch.tensor([[-2.0] * 3, [2.0] * 3])
+    pts2, ts2, st2 = render.sample_points(raysu, aabb2, cfg, render.RenderNoise(jit2.cuda(), None), True, sched)
+    rp2, rts2, rst2 = O.sample_points_contracted(uo.double(), ud.double(), sched.double(), jit2.double())
+    assert _rel_err(ts2, rts2) < 1e-5 and _rel_err(st2, rst2) < 1e-5
+    assert _rel_err(pts2, O.normalize_points(rp2, aabb2.double())) < 1e-5
+    np.testing.assert_allclose(sched.numpy(), O.contracted_schedule(0.05, 200.0, N))
+
+
+def test_composite_fwd_bwd(tg):
+    from tensorf_gb300 import render
+    gen = torch.Generator().manual_seed(7)
+    for R, N in [(37, 1), (64, 33), (128, 512), (8, 1000)]:
+        sig = (torch.rand((R, N), generator=gen) * 30).float()
+        st = (torch.rand((R, N), generator=gen) * 0.02).float()
+        s = sig.cuda().requires_grad_(True)
+        probs = render.compute_segment_probabilities(s, st.cuda())
+        s64 = sig.double().requires_grad_(True)
+        pe, pt = O.compute_segment_probabilities(s64, st.double())
+        assert _rel_err(probs.p_exits, pe) < 1e-5 and _rel_err(probs.p_terminates, pt) < 1e-5
+        g1 = torch.randn((R, N), generator=gen, dtype=torch.float64)
+        g2 = torch.randn((R, N), generator=gen, dtype=torch.float64)
+        ((pe * g1).sum() + (pt * g2).sum()).backward()
+        ((probs.p_exits * g1.float().cuda()).sum() + (probs.p_terminates * g2.float().cuda()).sum()).backward()
+        assert _rel_err(s.grad, s64.grad) < 1e-4
+
+
+def test_topk_exact_with_ties(tg):
+    from tensorf_gb300 import render
+    gen = torch.Generator().manual_seed(11)
+    R, N, k = 64, 512, 64
+    p = torch.rand((R, N), generator=gen).float()
+    p[:, ::7] = 0.0  # -inf keys
+    p[:4] = torch.tensor([0.25, 0.5]).repeat(N // 2)  # exact ties
+    p[4] = 0.0  # every key -inf: the k lowest indices
+    g = torch.zeros(N)
+    g[N // 2:] = -torch.log(-torch.log(torch.rand(N // 2, generator=gen)))
+    idx = render.weighted_choice(p.cuda(), g.cuda(), k).cpu().long()
+    ref = O.choice_without_replacement(p, g, k)
+    keys = O.gumbel_topk_keys(p.double(), g.double())
+    srt = torch.sort(keys, dim=-1, descending=True).values
+    margin = (srt[:, k - 1] - srt[:, k]).abs()
+    ok = (margin > 1e-5) | ~torch.isfinite(margin) | (margin == 0)
+    assert ok.float().mean() > 0.9
+    assert torch.equal(idx[ok], ref[ok])
+    assert idx[4].tolist() == list(range(k))
+    # Per-ray Gumbel noise.
+    g2 = -torch.log(-torch.log(torch.rand((R, N), generator=gen)))
+    idx2 = render.weighted_choice(p.cuda(), g2.cuda(), 5).cpu().long()
+    assert torch.equal(idx2[5:], O.choice_without_replacement(p, g2, 5)[5:])
+
+
+def test_mlp_fwd_bwd(tg):
+    from tensorf_gb300 import render
+    spec = render.ModelSpec(grid_dim=8, density_feat_dim=16, appearance_feat_dim=48)
+    ref = _ref_params(8, 16, 48, 5)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    gen = torch.Generator().manual_seed(9)
+    n = 1000
+    feats = (torch.randn((n, 144), generator=gen) * 0.1).float()
+    vd = torch.nn.functional.normalize(torch.randn((n, 3), generator=gen), dim=-1).float()
+    f = feats.cuda().requires_grad_(True)
+    out = spec.mlp().apply(lp, f, vd.cuda())
+    mlp64 = {k: {nm: t.double().requires_grad_(True) for nm, t in d.items()} for k, d in ref["mlp"].items()}
+    f64 = feats.double().requires_grad_(True)
+    r64 = O.feature_mlp(mlp64, f64, vd.double(), 2, 2)
+    assert _rel_err(out, r64) < RTOL
+    g = torch.randn((n, 3), generator=gen, dtype=torch.float64)
+    (r64 * g).sum().backward()
+    (out * g.float().cuda()).sum().backward()
+    assert _rel_err(f.grad, f64.grad) < 1e-4
+
+
+def _near_tie_free(ref_aux, k):
+    keys = torch.log(ref_aux["p_terminates"].detach()) + ref_aux["gumbel"]
+    srt = torch.sort(keys, dim=-1, descending=True).values
+    if k >= keys.shape[1]:
+        return torch.ones(keys.shape[0], dtype=torch.bool)
+    margin = srt[:, k - 1] - srt[:, k]
+    return (margin > 1e-5) | ~torch.isfinite(margin)
+
+
+def _problem(seed, G=32, R=256, N=128, k=32, Cd=16, Ca=48):
+    ref = _ref_params(G, Cd, Ca, seed)
+    o, d, c = _rays(R, seed)
+    rng = np.random.default_rng(seed)
+    jit = torch.tensor(rng.uniform(size=N), dtype=torch.float32)
+    gum = torch.tensor(-np.log(-np.log(rng.uniform(1e-7, 1, size=N))), dtype=torch.float32)
+    return ref, o, d, c, jit, gum
+
+
+@pytest.mark.parametrize("shift", [10.0, -1.0])
+def test_render_rays_rgb_matches_oracle(tg, shift):
+    from tensorf_gb300 import cameras, render
+    G, R, N, k = 32, 256, 128, 32
+    ref, o, d, c, jit, gum = _problem(1, G=G, R=R, N=N, k=k)
+    spec = render.ModelSpec(grid_dim=G)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
+    cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, N, k)
+    out = render.render_rays(spec.mlp(), lp, aabb, cameras.Rays3D(o.cuda(), d.cuda()),
+                             render.RenderNoise(jit.cuda(), gum.cuda()), cfg, density_shift=shift)
+    r64, aux = O.render_rays(_to64(ref), aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
+                             density_shift=shift, return_aux=True)
+    aux["gumbel"] = gum.double()
+    ok = _near_tie_free(aux, k)
+    assert ok.float().mean() > 0.95
+    assert _rel_err(out.cpu()[ok], r64[ok]) < RTOL
+
+
+@pytest.mark.parametrize("mode", ["dist_mean", "dist_median"])
+def test_render_rays_distance_modes(tg, mode):
+    from tensorf_gb300 import cameras, render
+    G, R, N = 32, 256, 128
+    ref, o, d, c, jit, gum = _problem(2, G=G, R=R, N=N)
+    spec = render.ModelSpec(grid_dim=G)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
+    m = render.RenderMode.DIST_MEAN if mode == "dist_mean" else render.RenderMode.DIST_MEDIAN
+    cfg = render.RenderConfig(0.05, 200.0, m, N, 8)
+    out = render.render_rays(spec.mlp(), lp, aabb, cameras.Rays3D(o.cuda(), d.cuda()),
+                             render.RenderNoise(jit.cuda(), None), cfg, density_shift=-2.0).cpu()
+    r64 = O.render_rays(_to64(ref), aabb.double(), o.double(), d.double(), N, 8, jit.double(), gum.double(),
+                        density_shift=-2.0, mode=mode)
+    fin = torch.isfinite(r64)
+    assert torch.equal(torch.isfinite(out), fin)
+    assert _rel_err(out[fin], r64[fin]) < RTOL
+
+
+def test_loss_and_grad_matches_oracle_autograd(tg):
+    from tensorf_gb300 import cameras, render
+    G, R, N, k = 24, 192, 96, 24
+    ref, o, d, c, jit, gum = _problem(3, G=G, R=R, N=N, k=k)
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
+    shift = -1.0
+    # Keep only rays without near-ties so both sides select the same samples.
+    ref64 = _to64(ref)
+    _, aux = O.render_rays(ref64, aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
+                           density_shift=shift, return_aux=True)
+    aux["gumbel"] = gum.double()
+    ok = _near_tie_free(aux, k)
+    o, d, c = o[ok], d[ok], c[ok]
+    spec = render.ModelSpec(grid_dim=G)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    grads = torch.zeros_like(lp.params)
+    cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, N, k)
+    loss = render.loss_and_grad(lp, grads, aabb, cameras.Rays3D(o.cuda(), d.cuda()), c.cuda(),
+                                render.RenderNoise(jit.cuda(), gum.cuda()), cfg, density_shift=shift)
+    leaves = []
+    for t in (ref64["density"][0], ref64["density"][1], ref64["appearance"][0], ref64["appearance"][1]):
+        t.requires_grad_(True)
+        leaves.append(t)
+    for lay in ref64["mlp"].values():
+        for t in lay.values():
+            t.requires_grad_(True)
+    out = O.render_rays(ref64, aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
+                        density_shift=shift)
+    L = O.mse(out, c.double())
+    L.backward()
+    assert abs(float(loss.item()) - float(L)) <= RTOL * float(L)
+    g = lp.to_reference(grads)
+    pairs = [(g["density"][0], ref64["density"][0].grad), (g["density"][1], ref64["density"][1].grad),
+             (g["appearance"][0], ref64["appearance"][0].grad), (g["appearance"][1], ref64["appearance"][1].grad)]
+    for layer in ref64["mlp"]:
+        for nm in ref64["mlp"][layer]:
+            pairs.append((g["mlp"][layer][nm], ref64["mlp"][layer][nm].grad))
+    for got, want in pairs:
+        assert _rel_err(got, want) < 2e-4, (_rel_err(got, want))
+
+
+def test_train_step_adam_update(tg):
+    from tensorf_gb300 import cameras, render, training
+    G, R, N, k = 16, 128, 64, 16
+    ref, o, d, c, jit, gum = _problem(4, G=G, R=R, N=N, k=k)
+    aabb = ((-1.5,) * 3, (1.5,) * 3)
+    spec = render.ModelSpec(grid_dim=G)
+    cfg = training.TrainConfig(initial_aabb_min=aabb[0], initial_aabb_max=aabb[1], density_samples_per_ray=N,
+                               appearance_samples_per_ray=k, n_iters=1000)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    ts = training.TrainState(cfg, lp)
+    p0 = lp.params.clone()
+    noise = render.RenderNoise(jit.cuda(), gum.cuda())
+    # Gradient the step will use.
+    grads = torch.zeros_like(lp.params)
+    render.loss_and_grad(lp, grads, torch.tensor(aabb), cameras.Rays3D(o.cuda(), d.cuda()), c.cuda(), noise,
+                         ts.render_config())
+    ts.training_step(cameras.Rays3D(o.cuda(), d.cuda()), c.cuda(), noise=noise)
+    assert float(ts.grads.abs().max()) == 0.0  # zeroed for the next step
+    lay = lp.layout
+    ref_p, _, _ = O.adam_update(p0.double().cpu(), grads.double().cpu(), torch.zeros(lay.total, dtype=torch.float64),
+                                torch.zeros(lay.total, dtype=torch.float64), 1, lr=0.02, lr_decay=1.0)
+    ref_p_mlp, _, _ = O.adam_update(p0.double().cpu(), grads.double().cpu(),
+                                    torch.zeros(lay.total, dtype=torch.float64),
+                                    torch.zeros(lay.total, dtype=torch.float64), 1, lr=1e-3, lr_decay=1.0)
+    ref_p[lay.mlp_begin:] = ref_p_mlp[lay.mlp_begin:]
+    # Elements with |g| tiny relative to eps differ in their sign decision; compare
+    # the update on elements with a clear gradient.
+    gg = grads.double().cpu()
+    clear = gg.abs() > 1e-6
+    upd = (lp.params.double().cpu() - p0.double().cpu())[clear]
+    want = (ref_p - p0.double().cpu())[clear]
+    assert _rel_err(upd, want) < 1e-3
+
+
+def test_sphere_scene_quadrature_matches_oracle(tg):
+    from tensorf_gb300 import cameras, scene
+    sc = scene.SphereScene.random(0, count=32)
+    cams = sc.cameras(2, seed=1)
+    pix = torch.tensor([0, 400 * 800 + 400, 399 * 800 + 401, 123456, 640000 - 1, 300 * 800 + 500])
+    rays = cams[0].pixel_rays_wrt_world(pix)
+    got = sc.render(rays, 4096).cpu().double().numpy()
+    o = rays.origins.cpu().double().numpy()
+    dd = rays.directions.cpu().double().numpy()
+    t0, t1 = O.ray_segment_from_bounding_box(torch.tensor(o), torch.tensor(dd), torch.tensor(sc.aabb, dtype=torch.float64))
+    want = O.sphere_scene_quadrature(o, dd, sc.centers, sc.radii, sc.colors, 50.0, t0.numpy(), t1.numpy(), 4096)
+    np.testing.assert_allclose(got, want, atol=1e-5)
+
+
+def test_camera_rays_match_oracle(tg):
+    from tensorf_gb300 import cameras
+    R, t = cameras.look_at([0.3, -4.0, 1.0])
+    cam = cameras.Camera.from_focal(R, t, 800, 800, 1111.0)
+    rays = cam.pixel_rays_wrt_world()
+    o, d = O.camera_pixel_rays(cam.K, cam.R_world_camera, cam.t_world_camera, 800, 800)
+    np.testing.assert_allclose(rays.directions.cpu().numpy(), d, atol=1e-6)
+    np.testing.assert_allclose(rays.origins.cpu().numpy(), o, atol=1e-6)
+
+
+def test_noise_fill_statistics(tg):
+    from tensorf_gb300 import render
+    k = render.NoiseKey(123)
+    u = k.uniform(1 << 20).cpu()
+    assert float(u.min()) >= 0.0 and float(u.max()) < 1.0
+    assert abs(float(u.mean()) - 0.5) < 2e-3
+    g = k.gumbel(1 << 20).cpu()
+    assert abs(float(g.mean()) - 0.5772156649) < 5e-3
+    a, b = k.split()
+    assert not torch.equal(a.uniform(64).cpu(), b.uniform(64).cpu())
+    assert torch.equal(k.uniform(64).cpu(), k.uniform(64).cpu())
