@@ -89,7 +89,16 @@ typedef struct {
   int32_t squash_dim;          /* FeatureMlp.feature_squash_dim, 27 */
   int32_t units;               /* FeatureMlp.units, 128 */
   int32_t dtype;               /* arithmetic/storage mode: TVM_F32, TVM_BF16, TVM_F64 */
+  int32_t mlp_math;            /* TVM_MLP_DEFAULT or TVM_MLP_SIMT_F32 (TVM_F32 models only) */
+  int32_t _pad;
 } tvm_model_desc;
+
+/* MLP arithmetic. DEFAULT: TVM_F32 models run the dense layers on tcgen05 tensor
+ * cores with a 3-pass split-tf32 product (hi*hi + hi*lo + lo*hi, ~22 significant bits
+ * per input, fp32 accumulation), TVM_BF16 models with one bf16 pass. SIMT_F32: plain
+ * FP32 FMA on the CUDA cores. */
+#define TVM_MLP_DEFAULT 0
+#define TVM_MLP_SIMT_F32 1
 
 /* Offsets (in elements of the master dtype: float, or double for TVM_F64) of every
  * parameter segment inside one flat parameter buffer. Grad, Adam mu and nu buffers
@@ -222,6 +231,18 @@ TVM_API int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const f
 TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
                 const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
                 void* grads, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Plain GEMM on the tensor-core path used by the MLP (exposed for testing):
+ * D[M x N] (+)= A(m,k) * B(k,n), A(m,k) = a_trans ? A[k*lda + m] : A[m*lda + k],
+ * B(k,n) = b_trans ? B[n*ldb + k] : B[k*ldb + n]; all float32 in memory. math: 0 =
+ * tcgen05 bf16, 1 = tcgen05 split-tf32 (FP32-accurate), 2 = FP32 SIMT. accumulate:
+ * 0 overwrites D, 1 adds into D atomically (K is then split across CTAs). */
+TVM_API int tvm_gemm(int32_t math, int32_t a_trans, int32_t b_trans, int64_t M, int32_t N, int64_t K,
+                     const float* A, int64_t lda, const float* B, int64_t ldb, float* D, int64_t ldd,
+                     int32_t accumulate, void* stream);
+/* Copy the device status word into *out (host) and clear it: bit 0 = a bounded
+ * tensor-core wait gave up (results of that call are invalid). */
+TVM_API int tvm_device_status(int32_t* out, void* stream);
 
 /* ---- fused render_rays / training_step ---------------------------------------------- */
 /* render_rays (render.py:105-279) for one chunk of rays. out: (R, 3) for RGB, (R,) for

@@ -58,10 +58,12 @@ static int validate_model(const tvm_model_desc* m) {
   TVM_REQUIRE(m->feature_n_freqs >= 0 && m->feature_n_freqs <= 16 && m->viewdir_n_freqs >= 0 &&
                   m->viewdir_n_freqs <= 16,
               TVM_ERR_SHAPE, "fourier frequencies must be in [0, 16]");
-  TVM_REQUIRE(m->squash_dim >= 1 && m->squash_dim <= 256 && m->units >= 1 && m->units <= 1024,
+  TVM_REQUIRE(m->squash_dim >= 1 && m->squash_dim <= 64 && m->units >= 1 && m->units <= 1024,
               TVM_ERR_SHAPE, "squash_dim / units out of range");
   TVM_REQUIRE(m->dtype == TVM_F32 || m->dtype == TVM_BF16, TVM_ERR_DTYPE,
               "model dtype %d not supported (TVM_F32, TVM_BF16)", m->dtype);
+  TVM_REQUIRE(m->mlp_math == TVM_MLP_DEFAULT || (m->mlp_math == TVM_MLP_SIMT_F32 && m->dtype == TVM_F32),
+              TVM_ERR_INVALID, "mlp_math=%d invalid for dtype %d", m->mlp_math, m->dtype);
   return TVM_OK;
 }
 
@@ -147,6 +149,7 @@ static MlpDims mlp_dims(const tvm_model_desc& m) {
   d.units = m.units;
   d.nf = m.feature_n_freqs;
   d.nv = m.viewdir_n_freqs;
+  d.math = (m.dtype == TVM_BF16) ? 0 : (m.mlp_math == TVM_MLP_SIMT_F32 ? 2 : 1);
   return d;
 }
 
@@ -513,6 +516,27 @@ int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* sh
   make_layout(*model, L);
   return launch_shadow(static_cast<const float*>(params), static_cast<__nv_bfloat16*>(shadow),
                        L.shadow_total, as_stream(stream));
+}
+
+int tvm_gemm(int32_t math, int32_t a_trans, int32_t b_trans, int64_t M, int32_t N, int64_t K, const float* A,
+             int64_t lda, const float* B, int64_t ldb, float* D, int64_t ldd, int32_t accumulate, void* stream) {
+  TVM_REQUIRE(math >= 0 && math <= 2, TVM_ERR_INVALID, "math must be 0, 1 or 2");
+  TVM_REQUIRE(M >= 0 && N >= 0 && K >= 0 && M < (1LL << 31) && K < (1LL << 40), TVM_ERR_SHAPE, "bad sizes");
+  if (M == 0 || N == 0) return TVM_OK;
+  TVM_REQUIRE(A && B && D, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(ldd >= N && lda >= 1 && ldb >= 1, TVM_ERR_SHAPE, "bad leading dimensions");
+  if (K == 0 && !accumulate) {
+    cudaError_t e = cudaMemset2DAsync(D, ldd * sizeof(float), 0, N * sizeof(float), M, as_stream(stream));
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+    return TVM_OK;
+  }
+  return gemm_any(math, a_trans != 0, b_trans != 0, M, N, K, A, lda, B, ldb, D, ldd, accumulate != 0,
+                  as_stream(stream));
+}
+
+int tvm_device_status(int32_t* out, void* stream) {
+  TVM_REQUIRE(out != nullptr, TVM_ERR_INVALID, "out is NULL");
+  return device_status(out, as_stream(stream));
 }
 
 int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void* grads, void* adam_mu,

@@ -65,6 +65,7 @@ struct MlpDims {
   int enc;     // encoded width (150 at n=2)
   int units;   // 128
   int nf, nv;  // fourier frequencies
+  int math;    // 0: tcgen05 bf16, 1: tcgen05 split-tf32 (FP32-accurate), 2: FP32 SIMT
 };
 struct MlpWeights {
   const float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
@@ -80,6 +81,9 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0,
                  int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
+int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
+             const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
+int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
 

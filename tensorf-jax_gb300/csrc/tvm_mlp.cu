@@ -11,8 +11,10 @@
 // with one atomic per output per chunk. Activations (H0..H2) are kept in the
 // workspace for the backward.
 #include <algorithm>
+#include <type_traits>
 
 #include "tvm_internal.h"
+#include "tvm_tcgemm.cuh"
 
 namespace tvm {
 
@@ -20,10 +22,27 @@ namespace {
 constexpr int BM = 64, BN = 64, BK = 16;
 constexpr float kHalfPi = 1.57079632679489661923f;
 
+// Epilogues. operator() handles one element; vec4 four consecutive columns of one row
+// (n..n+3, clipped at N), with one 16-byte access when the address allows it.
+template <class E>
+__device__ __forceinline__ void vec4_scalar(const E& e, int64_t m, int n, const float (&v)[4], int N) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (n + j < N) e(m, n + j, v[j]);
+}
+__device__ __forceinline__ bool vec_ok(const float* p, int n, int N) {
+  return n + 3 < N && (reinterpret_cast<uintptr_t>(p) & 15) == 0;
+}
+
 struct EpiStore {
   float* C;
   int ldc;
   __device__ void operator()(int64_t m, int n, float v) const { C[m * ldc + n] = v; }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
+    float* p = C + m * ldc + n;
+    if (vec_ok(p, n, N)) *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    else vec4_scalar(*this, m, n, v, N);
+  }
 };
 // act: 0 none, 1 relu, 2 sigmoid
 struct EpiBiasAct {
@@ -31,11 +50,17 @@ struct EpiBiasAct {
   int ldc;
   const float* bias;
   int act;
-  __device__ void operator()(int64_t m, int n, float v) const {
+  __device__ float f(int n, float v) const {
     if (bias) v = v + __ldg(bias + n);
     if (act == 1) v = fmaxf(v, 0.0f);
     if (act == 2) v = 1.0f / (1.0f + expf(-v));
-    C[m * ldc + n] = v;
+    return v;
+  }
+  __device__ void operator()(int64_t m, int n, float v) const { C[m * ldc + n] = f(n, v); }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
+    float* p = C + m * ldc + n;
+    if (vec_ok(p, n, N)) *reinterpret_cast<float4*>(p) = make_float4(f(n, v[0]), f(n + 1, v[1]), f(n + 2, v[2]), f(n + 3, v[3]));
+    else vec4_scalar(*this, m, n, v, N);
   }
 };
 // C = v * (H > 0): backward through a ReLU whose output is H.
@@ -47,11 +72,27 @@ struct EpiReluMask {
   __device__ void operator()(int64_t m, int n, float v) const {
     C[m * ldc + n] = (__ldg(H + m * ldh + n) > 0.0f) ? v : 0.0f;
   }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
+    float* p = C + m * ldc + n;
+    const float* h = H + m * ldh + n;
+    if (vec_ok(p, n, N) && (reinterpret_cast<uintptr_t>(h) & 15) == 0) {
+      const float4 hv = __ldg(reinterpret_cast<const float4*>(h));
+      *reinterpret_cast<float4*>(p) = make_float4(hv.x > 0.f ? v[0] : 0.f, hv.y > 0.f ? v[1] : 0.f,
+                                                  hv.z > 0.f ? v[2] : 0.f, hv.w > 0.f ? v[3] : 0.f);
+    } else {
+      vec4_scalar(*this, m, n, v, N);
+    }
+  }
 };
 struct EpiAtomic {
   float* C;
   int ldc;
   __device__ void operator()(int64_t m, int n, float v) const { atomicAdd(C + m * ldc + n, v); }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
+    float* p = C + m * ldc + n;
+    if (vec_ok(p, n, N)) atomicAdd(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+    else vec4_scalar(*this, m, n, v, N);
+  }
 };
 }  // namespace
 
@@ -134,49 +175,76 @@ static int gemm(int64_t M, int N, int64_t K, const float* A, int64_t lda, const 
   return check_launch("sgemm");
 }
 
-// X1[m][sq..enc) from X1[m][0..sq) (= H0) and the view direction.
-__global__ void pe_fwd_kernel(float* __restrict__ X1, int ld, int64_t M, int sq, int enc, int nf,
-                              int nv, const float* __restrict__ dirs, int rows_per_dir) {
+// One dense product with the model's arithmetic: SIMT FP32, tcgen05 bf16 or tcgen05
+// split-bf16.
+// kc < 0 asks for a split-K reduction sized for the GPU (the epilogue accumulates).
+template <bool AT, bool BT, class Epi>
+static int mm(int math, int64_t M, int N, int64_t K, const float* A, int64_t lda, const float* B, int64_t ldb,
+              Epi epi, cudaStream_t st, int64_t kc = 0) {
+  if (kc < 0) kc = (math == 2) ? 4096 : splitk_chunk(M, K);
+  if (math == 2) return gemm<AT, BT>(M, N, K, A, lda, B, ldb, epi, st, kc);
+  if (math == 1) return tc_gemm<AT, BT, tcg::FMT_TF32, true>(M, N, K, A, lda, B, ldb, epi, st, kc);
+  return tc_gemm<AT, BT, tcg::FMT_BF16, false>(M, N, K, A, lda, B, ldb, epi, st, kc);
+}
+
+// X1[m][sq..enc) from X1[m][0..sq) (= H0) and the view direction
+// (networks.py:68-76). A block owns 32 rows: their H0 and directions go to shared
+// memory, then consecutive threads write consecutive columns of a row.
+constexpr int PE_ROWS = 32;
+__global__ void __launch_bounds__(256) pe_fwd_kernel(float* __restrict__ X1, int ld, int64_t M, int sq, int enc,
+                                                    int nf, int nv, const float* __restrict__ dirs,
+                                                    int rows_per_dir) {
+  __shared__ float h[PE_ROWS][65];
+  __shared__ float dv[PE_ROWS][3];
+  const int64_t m0 = (int64_t)blockIdx.x * PE_ROWS;
+  const int nrows = (int)(M - m0 < PE_ROWS ? M - m0 : PE_ROWS);
+  for (int e = threadIdx.x; e < nrows * sq; e += blockDim.x) {
+    const int r = e / sq, j = e - r * sq;
+    h[r][j] = X1[(m0 + r) * ld + j];
+  }
+  for (int e = threadIdx.x; e < nrows * 3; e += blockDim.x) {
+    const int r = e / 3, a = e - r * 3;
+    dv[r][a] = __ldg(dirs + ((m0 + r) / rows_per_dir) * 3 + a);
+  }
+  __syncthreads();
   const int width = enc - sq;
-  const int64_t total = M * width;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t m = e / width;
-    const int c = sq + (int)(e - m * width);
-    const float* d = dirs + (m / rows_per_dir) * 3;
+  const int f_end = sq + 3 + sq * 2 * nf;
+  for (int e = threadIdx.x; e < nrows * width; e += blockDim.x) {
+    const int r = e / width;
+    const int c = sq + (e - r * width);
     float v;
     if (c < sq + 3) {
-      v = __ldg(d + (c - sq));
-    } else if (c < sq + 3 + sq * 2 * nf) {
+      v = dv[r][c - sq];
+    } else if (c < f_end) {
       const int q = c - (sq + 3);
-      const int j = q / (2 * nf), f = q % (2 * nf);
-      const float h = X1[m * ld + j];
-      const float x = h * (float)(1 << (f % nf));
+      const int j = q / (2 * nf), f = q - j * 2 * nf;
+      const float x = h[r][j] * (float)(1 << (f % nf));
       v = sinf(f < nf ? x : x + kHalfPi);
     } else {
-      const int q = c - (sq + 3 + sq * 2 * nf);
-      const int j = q / (2 * nv), f = q % (2 * nv);
-      const float x = __ldg(d + j) * (float)(1 << (f % nv));
+      const int q = c - f_end;
+      const int j = q / (2 * nv), f = q - j * 2 * nv;
+      const float x = dv[r][j] * (float)(1 << (f % nv));
       v = sinf(f < nv ? x : x + kHalfPi);
     }
-    X1[m * ld + c] = v;
+    X1[(m0 + r) * ld + c] = v;
   }
 }
 
-// dH0[m][j] = dX1[m][j] + sum_f dX1[m][PE(j,f)] * d PE / d h.
-__global__ void pe_bwd_kernel(const float* __restrict__ dX1, int ld, const float* __restrict__ X1,
-                              int64_t M, int sq, int nf, float* __restrict__ dH0) {
-  const int64_t total = M * sq;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t m = e / sq;
-    const int j = (int)(e - m * sq);
-    const float h = __ldg(X1 + m * ld + j);
+// dH0[m][j] = dX1[m][j] + sum_f dX1[m][PE(j,f)] * d PE / d h (one thread per (m, j)).
+__global__ void __launch_bounds__(256) pe_bwd_kernel(const float* __restrict__ dX1, int ld,
+                                                    const float* __restrict__ X1, int64_t M, int sq, int nf,
+                                                    float* __restrict__ dH0) {
+  const int64_t m0 = (int64_t)blockIdx.x * PE_ROWS;
+  const int nrows = (int)(M - m0 < PE_ROWS ? M - m0 : PE_ROWS);
+  for (int e = threadIdx.x; e < nrows * sq; e += blockDim.x) {
+    const int r = e / sq, j = e - r * sq;
+    const int64_t m = m0 + r;
+    const float hv = __ldg(X1 + m * ld + j);
     float g = __ldg(dX1 + m * ld + j);
     const float* pe = dX1 + m * ld + sq + 3 + j * 2 * nf;
     for (int f = 0; f < nf; ++f) {
       const float sc = (float)(1 << f);
-      const float x = h * sc;
+      const float x = hv * sc;
       g += __ldg(pe + f) * cosf(x) * sc;
       g += __ldg(pe + nf + f) * cosf(x + kHalfPi) * sc;
     }
@@ -228,7 +296,6 @@ size_t mlp_workspace_bytes(const MlpDims& d, int64_t M) {
   return ws.used + 256;
 }
 
-static unsigned ew_blocks(int64_t n) { return (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 32); }
 
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st) {
@@ -239,15 +306,15 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
     return TVM_ERR_WORKSPACE;
   }
   const int l1 = ld_x1(d);
-  TVM_TRY((gemm<false, false>(M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, l1}, st)));
-  pe_fwd_kernel<<<ew_blocks(M * (d.enc - d.squash)), 256, 0, st>>>(b.X1, l1, M, d.squash, d.enc, d.nf,
-                                                                     d.nv, dirs, rows_per_dir);
+  TVM_TRY((mm<false, false>(d.math, M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, l1}, st)));
+  pe_fwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.X1, l1, M, d.squash, d.enc, d.nf, d.nv, dirs,
+                                                                 rows_per_dir);
   TVM_TRY(check_launch("pe_fwd"));
-  TVM_TRY((gemm<false, false>(M, d.units, d.enc, b.X1, l1, w.w1, d.units,
+  TVM_TRY((mm<false, false>(d.math, M, d.units, d.enc, b.X1, l1, w.w1, d.units,
                               EpiBiasAct{b.H1, d.units, w.b1, 1}, st)));
-  TVM_TRY((gemm<false, false>(M, d.units, d.units, b.H1, d.units, w.w2, d.units,
+  TVM_TRY((mm<false, false>(d.math, M, d.units, d.units, b.H1, d.units, w.w2, d.units,
                               EpiBiasAct{b.H2, d.units, w.b2, 1}, st)));
-  TVM_TRY((gemm<false, false>(M, 3, d.units, b.H2, d.units, w.w3, 3, EpiBiasAct{rgb, 3, w.b3, 2}, st)));
+  TVM_TRY((mm<false, false>(d.math, M, 3, d.units, b.H2, d.units, w.w3, 3, EpiBiasAct{rgb, 3, w.b3, 2}, st)));
   return TVM_OK;
 }
 
@@ -259,34 +326,35 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     return TVM_ERR_WORKSPACE;
   }
   const int l1 = ld_x1(d);
-  const int64_t kc = 4096;  // rows per split-K chunk of the weight gradients
+  const int64_t kc = -1;  // weight gradients: split-K over the rows, sized per GEMM
   // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
-  TVM_TRY((gemm<false, true>(M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
-  TVM_TRY((gemm<true, false>(d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+  TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
+  TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
   // Layer 2.
-  TVM_TRY((gemm<false, true>(M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
+  TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
                              EpiReluMask{b.dH1, d.units, b.H1, d.units}, st)));
-  TVM_TRY((gemm<true, false>(d.units, d.units, M, b.H1, d.units, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
+  TVM_TRY((mm<true, false>(d.math, d.units, d.units, M, b.H1, d.units, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
   // Layer 1.
-  TVM_TRY((gemm<false, true>(M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
-  TVM_TRY((gemm<true, false>(d.enc, d.units, M, b.X1, l1, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
+  TVM_TRY((mm<false, true>(d.math, M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
+  TVM_TRY((mm<true, false>(d.math, d.enc, d.units, M, b.X1, l1, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
   // Bias gradients.
   {
-    dim3 grid3(1, (unsigned)ceil_div(M, kc));
-    colsum_kernel<<<grid3, 128, 0, st>>>(dZ3, 3, M, 3, kc, g.b3);
+    const int64_t cs = 128;  // rows per colsum block: M/128 blocks keep every SM busy
+    dim3 grid3(1, (unsigned)ceil_div(M, cs));
+    colsum_kernel<<<grid3, 32, 0, st>>>(dZ3, 3, M, 3, cs, g.b3);
     TVM_TRY(check_launch("colsum"));
-    dim3 gridu((unsigned)ceil_div(d.units, 128), (unsigned)ceil_div(M, kc));
-    colsum_kernel<<<gridu, 128, 0, st>>>(b.dH2, d.units, M, d.units, kc, g.b2);
+    dim3 gridu((unsigned)ceil_div(d.units, 128), (unsigned)ceil_div(M, cs));
+    colsum_kernel<<<gridu, 128, 0, st>>>(b.dH2, d.units, M, d.units, cs, g.b2);
     TVM_TRY(check_launch("colsum"));
-    colsum_kernel<<<gridu, 128, 0, st>>>(b.dH1, d.units, M, d.units, kc, g.b1);
+    colsum_kernel<<<gridu, 128, 0, st>>>(b.dH1, d.units, M, d.units, cs, g.b1);
     TVM_TRY(check_launch("colsum"));
   }
   // Fourier encoding backward, then layer 0.
-  pe_bwd_kernel<<<ew_blocks(M * d.squash), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0);
+  pe_bwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0);
   TVM_TRY(check_launch("pe_bwd"));
-  TVM_TRY((gemm<true, false>(d.feat, d.squash, M, X0, d.feat, b.dH0, d.squash, EpiAtomic{g.w0, d.squash}, st, kc)));
+  TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, d.squash, EpiAtomic{g.w0, d.squash}, st, kc)));
   if (dX0) {
-    TVM_TRY((gemm<false, true>(M, d.feat, d.squash, b.dH0, d.squash, w.w0, d.squash, EpiStore{dX0, d.feat}, st)));
+    TVM_TRY((mm<false, true>(d.math, M, d.feat, d.squash, b.dH0, d.squash, w.w0, d.squash, EpiStore{dX0, d.feat}, st)));
   }
   return TVM_OK;
 }
@@ -297,6 +365,44 @@ int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float
   if (n == 0) return TVM_OK;
   sigmoid_bwd_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(rgb, grad_rgb, n, dZ3);
   return check_launch("sigmoid_bwd");
+}
+
+}  // namespace tvm
+
+namespace tvm {
+
+int device_status(int32_t* out, cudaStream_t st) {
+  int32_t v = 0;
+  cudaError_t e = cudaMemcpyFromSymbolAsync(&v, g_tc_status, sizeof(int32_t), 0, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) {
+    const int32_t zero = 0;
+    e = cudaMemcpyToSymbolAsync(g_tc_status, &zero, sizeof(int32_t), 0, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_error("device_status: %s", cudaGetErrorString(e));
+    return TVM_ERR_LAUNCH;
+  }
+  *out = v;
+  return TVM_OK;
+}
+
+int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
+             const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st) {
+  const int ldc = (int)ldd;
+  const int64_t kc = accumulate ? -1 : 0;
+#define TVM_GEMM_CASE(AT_, BT_)                                                                     \
+  if (at == AT_ && bt == BT_) {                                                                     \
+    if (accumulate) return mm<AT_, BT_>(math, M, N, K, A, lda, B, ldb, EpiAtomic{D, ldc}, st, kc); \
+    return mm<AT_, BT_>(math, M, N, K, A, lda, B, ldb, EpiStore{D, ldc}, st);                    \
+  }
+  TVM_GEMM_CASE(false, false)
+  TVM_GEMM_CASE(false, true)
+  TVM_GEMM_CASE(true, false)
+  TVM_GEMM_CASE(true, true)
+#undef TVM_GEMM_CASE
+  return TVM_ERR_INVALID;
 }
 
 }  // namespace tvm

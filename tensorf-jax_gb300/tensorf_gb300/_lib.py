@@ -26,6 +26,7 @@ ERROR_NAMES = {
     -9: "TVM_ERR_WORKSPACE",
 }
 TVM_F32, TVM_BF16, TVM_F64 = 0, 1, 2
+TVM_MLP_DEFAULT, TVM_MLP_SIMT_F32 = 0, 1
 TVM_MODE_RGB, TVM_MODE_DIST_MEDIAN, TVM_MODE_DIST_MEAN = 0, 1, 2
 TVM_SAMPLER_BBOX, TVM_SAMPLER_CONTRACT = 0, 1
 
@@ -38,7 +39,7 @@ class VmField(ctypes.Structure):
 class ModelDesc(ctypes.Structure):
     _fields_ = [("grid_dim", c_int32), ("density_channels", c_int32), ("appearance_channels", c_int32),
                 ("feature_n_freqs", c_int32), ("viewdir_n_freqs", c_int32), ("squash_dim", c_int32),
-                ("units", c_int32), ("dtype", c_int32)]
+                ("units", c_int32), ("dtype", c_int32), ("mlp_math", c_int32), ("_pad", c_int32)]
 
 
 class ParamLayout(ctypes.Structure):
@@ -85,6 +86,9 @@ _SIGNATURES = {
                               c_size_t, c_void_p]),
     "tvm_mlp_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                               c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tvm_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int64, c_int32, c_int64, c_void_p, c_int64, c_void_p,
+                           c_int64, c_void_p, c_int64, c_int32, c_void_p]),
+    "tvm_device_status": (c_int32, [POINTER(c_int32), c_void_p]),
     "tvm_render_workspace_size": (c_size_t, [POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
     "tvm_render_fwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, POINTER(Rays), POINTER(RenderDesc),
                                  c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -64,13 +64,15 @@ class ModelSpec:
     squash_dim: int = 27
     units: int = 128
     precision: str = "fp32"  # "fp32" or "bf16"
+    mlp_math: str = "tensor"  # "tensor" (tcgen05; split-bf16 in fp32 mode) or "simt" (fp32 only)
 
     def desc(self) -> _lib.ModelDesc:
         return _lib.ModelDesc(grid_dim=self.grid_dim, density_channels=self.density_feat_dim,
                               appearance_channels=self.appearance_feat_dim,
                               feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs,
                               squash_dim=self.squash_dim, units=self.units,
-                              dtype=_lib.TVM_BF16 if self.precision == "bf16" else _lib.TVM_F32)
+                              dtype=_lib.TVM_BF16 if self.precision == "bf16" else _lib.TVM_F32,
+                              mlp_math=_lib.TVM_MLP_SIMT_F32 if self.mlp_math == "simt" else _lib.TVM_MLP_DEFAULT)
 
     def mlp(self) -> networks.FeatureMlp:
         return networks.FeatureMlp(feature_squash_dim=self.squash_dim, units=self.units,

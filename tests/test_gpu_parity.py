@@ -17,8 +17,9 @@ RTOL = 1e-4
 
 
 def _rel_err(a, b):
-    a = torch.as_tensor(a, dtype=torch.float64).cpu()
-    b = torch.as_tensor(b, dtype=torch.float64).cpu()
+    a = torch.as_tensor(a.detach() if torch.is_tensor(a) else a, dtype=torch.float64).cpu()
+    b = torch.as_tensor(b.detach() if torch.is_tensor(b) else b, dtype=torch.float64).cpu()
+    assert a.numel() > 0 and a.shape == b.shape
     return float((a - b).abs().max() / (b.abs().max() + 1e-30))
 
 
@@ -216,6 +217,7 @@ def test_render_rays_rgb_matches_oracle(tg, shift):
 def test_render_rays_distance_modes(tg, mode):
     from tensorf_gb300 import cameras, render
     G, R, N = 32, 256, 128
+    shift = 0.0  # optical depth ~2 across the box: most rays terminate inside it
     ref, o, d, c, jit, gum = _problem(2, G=G, R=R, N=N)
     spec = render.ModelSpec(grid_dim=G)
     lp = render.LearnableParams.from_reference(spec, ref)
@@ -223,9 +225,17 @@ def test_render_rays_distance_modes(tg, mode):
     m = render.RenderMode.DIST_MEAN if mode == "dist_mean" else render.RenderMode.DIST_MEDIAN
     cfg = render.RenderConfig(0.05, 200.0, m, N, 8)
     out = render.render_rays(spec.mlp(), lp, aabb, cameras.Rays3D(o.cuda(), d.cuda()),
-                             render.RenderNoise(jit.cuda(), None), cfg, density_shift=-2.0).cpu()
-    r64 = O.render_rays(_to64(ref), aabb.double(), o.double(), d.double(), N, 8, jit.double(), gum.double(),
-                        density_shift=-2.0, mode=mode)
+                             render.RenderNoise(jit.cuda(), None), cfg, density_shift=shift).cpu()
+    r64, aux = O.render_rays(_to64(ref), aabb.double(), o.double(), d.double(), N, 8, jit.double(), gum.double(),
+                             density_shift=shift, mode=mode, return_aux=True)
+    if mode == "dist_median":
+        # Rays whose 1 - p_exit passes within 1e-5 of 0.5 may cross at a neighbouring
+        # sample under float32 rounding; compare the others exactly.
+        margin = (1.0 - aux["p_exits"] - 0.5).abs().min(dim=-1).values
+        keep = margin > 1e-5
+        assert keep.float().mean() > 0.95
+        out, r64 = out[keep], r64[keep]
+        assert torch.isfinite(r64).float().mean() > 0.5  # most rays terminate
     fin = torch.isfinite(r64)
     assert torch.equal(torch.isfinite(out), fin)
     assert _rel_err(out[fin], r64[fin]) < RTOL
