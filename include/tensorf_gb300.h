@@ -68,6 +68,8 @@ extern "C" {
 /* Samplers. */
 #define TVM_SAMPLER_BBOX 0     /* render.py:175-186, 350-434 */
 #define TVM_SAMPLER_CONTRACT 1 /* render.py:122-173 (schedule supplied by caller) */
+#define TVM_SAMPLER_PROPOSAL 2 /* proposal-guided: samples resampled from a proposal network */
+#define TVM_SAMPLER_EXPLICIT 3 /* internal: per-sample distances and lengths given */
 
 /* One VM-decomposed tensor (TensorVM, tensor_vm.py:14-40). */
 typedef struct {
@@ -90,6 +92,9 @@ typedef struct {
   int32_t units;               /* FeatureMlp.units, 128 */
   int32_t dtype;               /* arithmetic/storage mode: TVM_F32, TVM_BF16, TVM_F64 */
   int32_t mlp_math;            /* TVM_MLP_DEFAULT or TVM_MLP_SIMT_F32 (TVM_F32 models only) */
+  int32_t proposal_grid;       /* proposal VM grid (e.g. 64); 0 = no proposal network */
+  int32_t proposal_rank;       /* proposal components per pair: 4 */
+  int32_t proposal_units;      /* proposal MLP hidden width (16 -> units -> 1): 64 */
   int32_t _pad;
 } tvm_model_desc;
 
@@ -108,12 +113,15 @@ typedef struct {
   int64_t density_lines, density_planes;
   int64_t appearance_lines, appearance_planes;
   int64_t mlp_w0, mlp_w1, mlp_b1, mlp_w2, mlp_b2, mlp_w3, mlp_b3;
+  int64_t proposal_lines, proposal_planes;                  /* tensor lr group */
+  int64_t proposal_w1, proposal_b1, proposal_w2, proposal_b2; /* MLP lr group */
   int64_t mlp_begin; /* first MLP element: [0, mlp_begin) is the tensor lr group */
   int64_t total;
   /* BF16 mode: element offsets of the bf16 shadow copies of the field tensors inside
    * the shadow buffer; 0 otherwise. */
   int64_t shadow_density_lines, shadow_density_planes;
   int64_t shadow_appearance_lines, shadow_appearance_planes;
+  int64_t shadow_proposal_lines, shadow_proposal_planes;
   int64_t shadow_total;
   int32_t encoded_dim; /* MLP input width after the fourier encoding (150 for n=2) */
   int32_t _pad;
@@ -142,6 +150,14 @@ typedef struct {
   int32_t jitter_per_ray;     /* BBOX only: 1 if jitter is (R, N) instead of (N,) */
   int32_t gumbel_per_ray;     /* 1 if gumbel is (R, N), 0 if (N,) shared (reference) */
   const float* gumbel;        /* Gumbel noise of jax.random.choice (render.py:461-469) */
+  /* PROPOSAL sampler: Np proposal bins per ray (uniform over the aabb segment, or the
+   * caller's Np+1 edges in `schedule` when `contract` is set), N main samples resampled
+   * from the proposal histogram; `jitter` is then (R, N), one per main interval. */
+  int32_t proposal_samples;      /* Np */
+  int32_t contract;              /* 1: unbounded scene, L-inf contraction to [-2,2]^3 */
+  const float* proposal_jitter;  /* (R, Np) uniforms, one per proposal bin */
+  float proposal_shift;          /* added before the proposal softplus */
+  float proposal_loss_weight;    /* weight of the proposal bound loss (training) */
 } tvm_render_desc;
 
 /* Adam hyper-parameters (training.py:207-243; optax.scale_by_adam). */

@@ -455,3 +455,117 @@ def sphere_scene_quadrature(origins: onp.ndarray, directions: onp.ndarray, cente
         w = trans * alpha
         out[r] = (w[:, None] * col).sum(0) + trans[-1] * (1.0 - alpha[-1])
     return out
+
+
+# ----------------------------------------------------------------------------------
+# Proposal-guided sampling. The reference has no proposal network (render.py:126); this
+# restates the build's own design (mip-NeRF 360-style proposal sampling) so that its
+# kernels and gradients can be checked.
+# ----------------------------------------------------------------------------------
+def proposal_edges(origins, directions, aabb, n_bins: int, edges=None):
+    """(R, Np+1) bin edges: t_min + j * step over the aabb segment, or given edges."""
+    r = origins.shape[0]
+    if edges is not None:
+        return edges[None, :].to(origins.dtype).expand(r, n_bins + 1)
+    t_min, t_max = ray_segment_from_bounding_box(origins, directions, aabb, 1e-3)
+    step = (t_max - t_min) / n_bins
+    j = torch.arange(n_bins + 1, dtype=origins.dtype)
+    return t_min[:, None] + j[None, :] * step[:, None]
+
+
+def proposal_forward(prop, origins, directions, aabb, n_bins: int, jitter, shift: float = 0.0,
+                     contract: bool = False, edges=None):
+    """Proposal densities and weights. prop: {'vector' (3,4,Gp), 'matrix' (3,4,Gp,Gp),
+    'w1' (16,U), 'b1' (U,), 'w2' (U,1), 'b2' (1,)}; jitter (R, Np).
+    Returns (edges (R,Np+1), weights (R,Np), sigma (R,Np), features (R,Np,16))."""
+    e = proposal_edges(origins, directions, aabb, n_bins, edges)
+    length = e[:, 1:] - e[:, :-1]
+    t = e[:, :-1] + jitter * length
+    pts = origins[:, None, :] + directions[:, None, :] * t[:, :, None]
+    if contract:
+        pts = contract_points(pts)
+    x = normalize_points(pts.permute(2, 0, 1), aabb)  # (3, R, Np)
+    feats = vm_interpolate(prop["vector"], prop["matrix"], x).permute(1, 2, 0)  # (R, Np, 12)
+    xp = x.permute(1, 2, 0)
+    X = torch.cat([feats, xp, xp.abs().amax(-1, keepdim=True)], dim=-1)
+    h = torch.relu(X @ prop["w1"] + prop["b1"])
+    z = (h @ prop["w2"])[..., 0] + prop["b2"][0]
+    sigma = softplus(z + shift)
+    _, w = compute_segment_probabilities(sigma, length)
+    return e, w, sigma, X
+
+
+def resample(edges, w, n_main: int, jitter):
+    """Main intervals at the quantiles i/N of w + (0.01 * sum w + 1e-4) / Np, one
+    jittered sample each. Returns (t (R,N), delta (R,N), bins (R,N+1)). Resampling
+    carries no gradient: the main field's loss does not train the proposal."""
+    r, nb = w.shape
+    w = w.detach()
+    edges = edges.detach()
+    tot = w.sum(-1, keepdim=True)
+    q = w + (0.01 * tot + 1e-4) / nb
+    cdf = torch.cat([torch.zeros((r, 1), dtype=w.dtype), torch.cumsum(q, -1)], -1)
+    Q = cdf[:, -1:]
+    s_edges = torch.empty((r, n_main + 1), dtype=w.dtype)
+    bins = torch.empty((r, n_main + 1), dtype=torch.int64)
+    for i in range(n_main + 1):
+        if i == 0:
+            bins[:, 0] = 0
+            s_edges[:, 0] = edges[:, 0]
+            continue
+        if i == n_main:
+            bins[:, i] = nb - 1
+            s_edges[:, i] = edges[:, nb]
+            continue
+        target = Q[:, 0] * (i / n_main)
+        b = torch.searchsorted(cdf[:, :nb].contiguous(), target[:, None].contiguous(), right=True)[:, 0] - 1
+        b = b.clamp(0, nb - 1)
+        ar = torch.arange(r)
+        qb = cdf[ar, b + 1] - cdf[ar, b]
+        f = ((target - cdf[ar, b]) / qb).clamp(0.0, 1.0)
+        s_edges[:, i] = edges[ar, b] + f * (edges[ar, b + 1] - edges[ar, b])
+        bins[:, i] = b
+    a, bnd = s_edges[:, :-1], torch.maximum(s_edges[:, 1:], s_edges[:, :-1])
+    delta = bnd - a
+    return a + jitter * delta, delta, bins
+
+
+def proposal_loss(w_main, w_prop, bins, weight: float = 1.0):
+    """lambda/R * sum_i max(0, w_i - bound_i)^2 / (w_i + 1e-7) with bound_i the
+    proposal mass over bins [bins_i, bins_{i+1}]; w_main carries no gradient."""
+    r = w_main.shape[0]
+    C = torch.cat([torch.zeros((r, 1), dtype=w_prop.dtype), torch.cumsum(w_prop, -1)], -1)
+    lo, hi = bins[:, :-1], bins[:, 1:]
+    bound = torch.gather(C, 1, hi + 1) - torch.gather(C, 1, lo)
+    wm = w_main.detach()
+    d = torch.clamp(wm - bound, min=0.0)
+    return weight / r * torch.sum(d * d / (wm + 1e-7))
+
+
+def render_explicit(params, aabb, origins, directions, ts, deltas, appearance_samples: int, gumbel,
+                    n_freqs_feat=2, n_freqs_view=2, density_shift=10.0, contract=False, return_aux=False):
+    """render_rays' RGB path (render.py:192-246) on given sample distances and lengths."""
+    r, n = ts.shape
+    pts = origins[:, None, :] + directions[:, None, :] * ts[:, :, None]
+    if contract:
+        pts = contract_points(pts)
+    points = normalize_points(pts.permute(2, 0, 1), aabb)
+    dvec, dmat = params["density"]
+    feat = vm_interpolate(dvec, dmat, points)
+    sigmas = softplus(torch.sum(feat, dim=0) + density_shift)
+    p_exits, p_term = compute_segment_probabilities(sigmas, deltas)
+    k = appearance_samples
+    idx = choice_without_replacement(p_term.detach(), gumbel, k)
+    ar = torch.arange(r)[:, None]
+    vis = points[:, ar, idx]
+    avec, amat = params["appearance"]
+    afeat = vm_interpolate(avec, amat, vis).permute(1, 2, 0).reshape(r * k, -1)
+    viewdirs = directions[:, None, :].expand(r, k, 3).reshape(-1, 3)
+    vis_rgb = feature_mlp(params["mlp"], afeat, viewdirs, n_freqs_feat, n_freqs_view).reshape(r, k, 3)
+    sampled = p_term[ar, idx]
+    unbias = (1.0 - p_exits[:, -1] + 1e-8) / (torch.sum(sampled, dim=1) + 1e-8)
+    expected = torch.sum(vis_rgb * sampled[:, :, None], dim=1) * unbias[:, None]
+    out = expected + p_exits[:, -1:]
+    if return_aux:
+        return out, {"p_terminates": p_term, "p_exits": p_exits, "gumbel": gumbel}
+    return out

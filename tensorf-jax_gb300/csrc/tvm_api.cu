@@ -64,6 +64,12 @@ static int validate_model(const tvm_model_desc* m) {
               "model dtype %d not supported (TVM_F32, TVM_BF16)", m->dtype);
   TVM_REQUIRE(m->mlp_math == TVM_MLP_DEFAULT || (m->mlp_math == TVM_MLP_SIMT_F32 && m->dtype == TVM_F32),
               TVM_ERR_INVALID, "mlp_math=%d invalid for dtype %d", m->mlp_math, m->dtype);
+  if (m->proposal_grid != 0) {
+    TVM_REQUIRE(m->proposal_grid >= 2 && m->proposal_grid <= 1024, TVM_ERR_SHAPE, "proposal_grid=%d outside [2, 1024]",
+                m->proposal_grid);
+    TVM_REQUIRE(m->proposal_rank == 4, TVM_ERR_UNSUPPORTED, "proposal_rank must be 4");
+    TVM_REQUIRE(m->proposal_units >= 1 && m->proposal_units <= 256, TVM_ERR_SHAPE, "proposal_units outside [1, 256]");
+  }
   return TVM_OK;
 }
 
@@ -77,6 +83,11 @@ static void make_layout(const tvm_model_desc& m, tvm_param_layout& L) {
   L.density_planes = seg(off, 3 * G * G * Cd);
   L.appearance_lines = seg(off, 3 * G * Ca);
   L.appearance_planes = seg(off, 3 * G * G * Ca);
+  const int64_t Gp = m.proposal_grid, Cp = m.proposal_rank;
+  if (Gp > 0) {
+    L.proposal_lines = seg(off, 3 * Gp * Cp);
+    L.proposal_planes = seg(off, 3 * Gp * Gp * Cp);
+  }
   L.mlp_begin = off;
   L.mlp_w0 = seg(off, 3 * Ca * m.squash_dim);
   L.mlp_w1 = seg(off, (int64_t)enc * m.units);
@@ -85,12 +96,20 @@ static void make_layout(const tvm_model_desc& m, tvm_param_layout& L) {
   L.mlp_b2 = seg(off, m.units);
   L.mlp_w3 = seg(off, (int64_t)m.units * 3);
   L.mlp_b3 = seg(off, 3);
+  if (Gp > 0) {
+    L.proposal_w1 = seg(off, 16LL * m.proposal_units);
+    L.proposal_b1 = seg(off, m.proposal_units);
+    L.proposal_w2 = seg(off, m.proposal_units);
+    L.proposal_b2 = seg(off, 1);
+  }
   L.total = off;
   if (m.dtype == TVM_BF16) {
     L.shadow_density_lines = L.density_lines;
     L.shadow_density_planes = L.density_planes;
     L.shadow_appearance_lines = L.appearance_lines;
     L.shadow_appearance_planes = L.appearance_planes;
+    L.shadow_proposal_lines = L.proposal_lines;
+    L.shadow_proposal_planes = L.proposal_planes;
     L.shadow_total = L.mlp_begin;
   }
   L.encoded_dim = enc;
@@ -105,12 +124,25 @@ static int validate_rays(const tvm_rays* rays) {
   return TVM_OK;
 }
 
-static int validate_render(const tvm_render_desc* c, int64_t R, bool need_select) {
+static int validate_render(const tvm_render_desc* c, int64_t R, bool need_select,
+                           const tvm_model_desc* m = nullptr) {
   TVM_REQUIRE(c != nullptr, TVM_ERR_INVALID, "render descriptor is NULL");
+  if (c->sampler == TVM_SAMPLER_PROPOSAL) {
+    TVM_REQUIRE(m == nullptr || m->proposal_grid > 0, TVM_ERR_INVALID,
+                "proposal sampler needs a model with a proposal network");
+    TVM_REQUIRE(c->proposal_samples >= 2 && c->proposal_samples <= 512, TVM_ERR_SHAPE,
+                "proposal_samples=%d outside [2, 512]", c->proposal_samples);
+    TVM_REQUIRE(c->density_samples <= 512, TVM_ERR_SHAPE, "proposal-guided density_samples must be <= 512");
+    TVM_REQUIRE(c->proposal_jitter != nullptr && c->jitter != nullptr, TVM_ERR_INVALID,
+                "proposal sampler needs proposal_jitter (R, Np) and jitter (R, N)");
+    TVM_REQUIRE(!c->contract || c->schedule != nullptr, TVM_ERR_INVALID,
+                "unbounded proposal sampling needs the Np+1 bin edges in schedule");
+  }
   TVM_REQUIRE(c->density_samples >= 1 && c->density_samples <= 8192, TVM_ERR_SHAPE,
               "density_samples=%d outside [1, 8192]", c->density_samples);
-  TVM_REQUIRE(c->sampler == TVM_SAMPLER_BBOX || c->sampler == TVM_SAMPLER_CONTRACT, TVM_ERR_INVALID,
-              "unknown sampler %d", c->sampler);
+  TVM_REQUIRE(c->sampler == TVM_SAMPLER_BBOX || c->sampler == TVM_SAMPLER_CONTRACT ||
+                  c->sampler == TVM_SAMPLER_PROPOSAL,
+              TVM_ERR_INVALID, "unknown sampler %d", c->sampler);
   TVM_REQUIRE(c->mode == TVM_MODE_RGB || c->mode == TVM_MODE_DIST_MEAN || c->mode == TVM_MODE_DIST_MEDIAN,
               TVM_ERR_INVALID, "unknown mode %d", c->mode);
   for (int a = 0; a < 3; ++a)
@@ -188,6 +220,9 @@ struct PassBufs {
   float* sigma;
   int32_t* sel;
   float *w_sel, *p_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
+  // proposal-guided sampling
+  float *Xp, *Hp, *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *dHp, *dXp, *loss_p;
+  int32_t* bins;
 };
 
 static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, int64_t R,
@@ -211,6 +246,26 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
     b.gsum = ws.take<float>(R * N);
     b.dX0 = ws.take<float>(M * F);
   }
+  if (c.sampler == TVM_SAMPLER_PROPOSAL) {
+    const int64_t S = R * c.proposal_samples;
+    const int64_t U = m.proposal_units;
+    b.Xp = ws.take<float>(S * 16);
+    b.Hp = ws.take<float>(S * U);
+    b.sig_p = ws.take<float>(S);
+    b.delta_p = ws.take<float>(S);
+    b.w_p = ws.take<float>(S);
+    b.t_main = ws.take<float>(R * N);
+    b.d_main = ws.take<float>(R * N);
+    b.bins = ws.take<int32_t>(R * (N + 1));
+    if (backward) {
+      b.w_dense = ws.take<float>(R * N);
+      b.g_wp = ws.take<float>(S);
+      b.dz_p = ws.take<float>(S);
+      b.dHp = ws.take<float>(S * U);
+      b.dXp = ws.take<float>(S * 16);
+      b.loss_p = ws.take<float>(1);
+    }
+  }
   return b;
 }
 
@@ -219,6 +274,27 @@ static size_t pass_bytes(const tvm_model_desc& m, const tvm_render_desc& c, int6
   carve_pass(m, c, R, backward, ws);
   const int64_t k = (c.mode == TVM_MODE_RGB) ? c.appearance_samples : 0;
   return ws.used + 256 + mlp_workspace_bytes(mlp_dims(m), R * k) + 256;
+}
+
+static FieldView proposal_field(const tvm_model_desc& m, const tvm_param_layout& L, const float* p,
+                                const void* shadow) {
+  if (m.dtype == TVM_BF16 && shadow) {
+    const __nv_bfloat16* s = static_cast<const __nv_bfloat16*>(shadow);
+    return FieldView{m.proposal_grid, m.proposal_rank, TVM_BF16, s + L.shadow_proposal_lines,
+                     s + L.shadow_proposal_planes};
+  }
+  return FieldView{m.proposal_grid, m.proposal_rank, TVM_F32, p + L.proposal_lines, p + L.proposal_planes};
+}
+
+// Sampler of the proposal bins: bounded scenes use the aabb segment (Np uniform bins),
+// unbounded ones the caller's edges with contraction.
+static SamplerArgs proposal_sampler(const tvm_render_desc& c) {
+  SamplerArgs s{};
+  s.sampler = c.contract ? TVM_SAMPLER_EXPLICIT : TVM_SAMPLER_BBOX;
+  s.contract = c.contract;
+  s.N = c.proposal_samples;
+  for (int a = 0; a < 6; ++a) s.aabb[a] = c.aabb[a];
+  return s;
 }
 
 // render_rays forward, and (if grads != null) the loss and backward of training_step.
@@ -233,7 +309,30 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   PassBufs b = carve_pass(m, c, R, backward, ws);
   TVM_REQUIRE(ws.ok(), TVM_ERR_WORKSPACE, "workspace too small (%zu bytes)", ws_bytes);
   if (R == 0) return TVM_OK;
-  const SamplerArgs s = sampler_args(c);
+  const MlpDims d = mlp_dims(m);
+  SamplerArgs s = sampler_args(c);
+  const bool proposal = c.sampler == TVM_SAMPLER_PROPOSAL;
+  const SamplerArgs sp = proposal ? proposal_sampler(c) : SamplerArgs{};
+  const float* edges = (proposal && c.contract) ? c.schedule : nullptr;
+  const int64_t S = R * c.proposal_samples;
+  if (proposal) {
+    // Proposal network forward, then resampling into explicit main samples.
+    const FieldView fp = proposal_field(m, L, params, shadow);
+    TVM_TRY(launch_prop_features(fp, rays.origins, rays.directions, R, sp, edges, c.proposal_jitter, b.Xp,
+                                 b.delta_p, st));
+    TVM_TRY(prop_mlp_forward(d.math, b.Xp, S, m.proposal_units, params + L.proposal_w1, params + L.proposal_b1,
+                             params + L.proposal_w2, params + L.proposal_b2, c.proposal_shift, b.Hp, b.sig_p, st));
+    TVM_TRY(launch_segment_fwd(b.sig_p, b.delta_p, R, c.proposal_samples, nullptr, b.w_p, st));
+    TVM_TRY(launch_resample(b.w_p, rays.origins, rays.directions, R, sp, edges, c.density_samples, c.jitter,
+                            b.t_main, b.d_main, b.bins, st));
+    s = SamplerArgs{};
+    s.sampler = TVM_SAMPLER_EXPLICIT;
+    s.N = c.density_samples;
+    for (int a = 0; a < 6; ++a) s.aabb[a] = c.aabb[a];
+    s.ts = b.t_main;
+    s.deltas = b.d_main;
+    s.contract = c.contract;
+  }
   const FieldView fd = density_field(m, L, params, shadow);
   const FieldView fa = appearance_field(m, L, params, shadow);
   const int k = c.appearance_samples;
@@ -243,16 +342,16 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(1, st);
   if (c.mode != TVM_MODE_RGB) {
     TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, 0, nullptr, 0,
-                                    nullptr, nullptr, nullptr, nullptr, out, st));
+                                    nullptr, nullptr, nullptr, nullptr, out, nullptr, st));
     phase_mark(2, st);
     return TVM_OK;
   }
   TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
-                                  c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.wsum, nullptr, st));
+                                  c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.wsum, nullptr,
+                                  (proposal && backward) ? b.w_dense : nullptr, st));
   phase_mark(2, st);
   TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(3, st);
-  const MlpDims d = mlp_dims(m);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
   TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, backward, st));
@@ -278,6 +377,20 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
                              rays.directions, R, s, b.gsum, st));
   phase_mark(9, st);
+  if (proposal) {
+    // Proposal bound loss on the main weights, then the proposal network backward.
+    cudaError_t e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), st);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+    TVM_TRY(launch_prop_loss(b.w_dense, b.w_p, b.bins, R, c.proposal_samples, c.density_samples,
+                             c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, st));
+    TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, st));
+    TVM_TRY(prop_mlp_backward(d.math, b.Xp, S, m.proposal_units, params + L.proposal_w1, params + L.proposal_w2,
+                              b.Hp, b.dz_p, b.dHp, b.dXp, grads + L.proposal_w1, grads + L.proposal_b1,
+                              grads + L.proposal_w2, grads + L.proposal_b2, st));
+    const FieldView fp = proposal_field(m, L, params, shadow);
+    TVM_TRY(launch_prop_vm_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins,
+                               rays.directions, R, sp, edges, c.proposal_jitter, b.dXp, st));
+  }
   return TVM_OK;
 }
 
@@ -365,6 +478,8 @@ int tvm_sample_points(const tvm_rays* rays, const tvm_render_desc* cfg, float* p
                       float* step_sizes, void* stream) {
   TVM_TRY(validate_rays(rays));
   TVM_TRY(validate_render(cfg, rays->count, false));
+  TVM_REQUIRE(cfg->sampler != TVM_SAMPLER_PROPOSAL, TVM_ERR_UNSUPPORTED,
+              "tvm_sample_points covers the bbox and contracted samplers");
   return launch_points(rays->origins, rays->directions, rays->count, sampler_args(*cfg), points, ts,
                        step_sizes, as_stream(stream));
 }
@@ -440,12 +555,12 @@ int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* fe
 }
 
 size_t tvm_render_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
-  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true) != TVM_OK || rays < 0) return 0;
+  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true, model) != TVM_OK || rays < 0) return 0;
   return pass_bytes(*model, *cfg, rays, false);
 }
 
 size_t tvm_train_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
-  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true) != TVM_OK || rays < 0) return 0;
+  if (validate_model(model) != TVM_OK || validate_render(cfg, rays, true, model) != TVM_OK || rays < 0) return 0;
   return pass_bytes(*model, *cfg, rays, true);
 }
 
@@ -464,7 +579,7 @@ int tvm_render_fwd(const tvm_model_desc* model, const void* params, const void* 
                    size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
   TVM_TRY(validate_rays(rays));
-  TVM_TRY(validate_render(cfg, rays->count, true));
+  TVM_TRY(validate_render(cfg, rays->count, true, model));
   TVM_TRY(validate_params(model, params, shadow));
   TVM_REQUIRE(rays->count == 0 || (out && workspace), TVM_ERR_INVALID, "out/workspace NULL");
   return run_pass(*model, static_cast<const float*>(params), shadow, nullptr, *rays, nullptr, *cfg,
@@ -476,7 +591,7 @@ int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, const voi
                       float* loss_out, void* workspace, size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
   TVM_TRY(validate_rays(rays));
-  TVM_TRY(validate_render(cfg, rays->count, true));
+  TVM_TRY(validate_render(cfg, rays->count, true, model));
   TVM_TRY(validate_params(model, params, shadow));
   TVM_REQUIRE(cfg->mode == TVM_MODE_RGB, TVM_ERR_INVALID, "training needs RGB mode");
   TVM_REQUIRE(grads && aligned(grads, 16), TVM_ERR_ALIGN, "grads NULL or not 16-byte aligned");

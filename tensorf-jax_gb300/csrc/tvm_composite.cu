@@ -223,7 +223,8 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
                                         int mode, int k, int P, const float* __restrict__ gumbel,
                                         int gumbel_per_ray, int32_t* __restrict__ sel_idx,
                                         float* __restrict__ w_sel, float* __restrict__ p_last_out,
-                                        float* __restrict__ wsum_out, float* __restrict__ dist_out) {
+                                        float* __restrict__ wsum_out, float* __restrict__ dist_out,
+                                        float* __restrict__ w_dense) {
   extern __shared__ unsigned char smem_b[];
   const int N = s.N;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,6 +247,7 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
     const float prev = __shfl_up_sync(0xffffffffu, incl, 1);
     const float excl = (lane == 0) ? carry : prev;
     const float w = (1.0f - expf(sv)) * expf(excl);
+    if (w_dense && valid) w_dense[r * N + i] = w;
     if (mode == TVM_MODE_RGB) {
       if (valid) {
         wbuf[i] = w;
@@ -404,6 +406,20 @@ int launch_segment_bwd(const float* sigmas, const float* steps, int64_t R, int N
   return check_launch("segment_bwd");
 }
 
+int launch_segment_bwd_sum(const float* sigmas, const float* steps, int64_t R, int N, const float* g_pt,
+                           float* g_sum, cudaStream_t st) {
+  if (R == 0) return TVM_OK;
+  const size_t per_warp = (size_t)N * 3 * sizeof(float);
+  const int warps = warps_for_smem(per_warp);
+  const size_t smem = per_warp * warps;
+  TVM_TRY(set_smem((const void*)composite_bwd_kernel<false, true>, smem));
+  SamplerArgs s{};
+  s.N = N;
+  composite_bwd_kernel<false, true><<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(
+      sigmas, steps, nullptr, nullptr, R, s, nullptr, g_pt, 0, nullptr, nullptr, nullptr, g_sum);
+  return check_launch("segment_bwd_sum");
+}
+
 int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t R, int N, int k,
                 int32_t* idx, cudaStream_t st) {
   if (R == 0) return TVM_OK;
@@ -420,7 +436,7 @@ int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t
 int launch_composite_select(const float* sigma, const float* origins, const float* dirs, int64_t R,
                             const SamplerArgs& s, int mode, int k, const float* gumbel,
                             int gumbel_per_ray, int32_t* sel_idx, float* w_sel, float* p_last,
-                            float* wsum, float* dist_out, cudaStream_t st) {
+                            float* wsum, float* dist_out, float* w_dense, cudaStream_t st) {
   if (R == 0) return TVM_OK;
   const int P = (mode == TVM_MODE_RGB) ? next_pow2(k) : 1;
   const size_t per_warp = (size_t)s.N * 8 + (size_t)P * 8;
@@ -429,7 +445,7 @@ int launch_composite_select(const float* sigma, const float* origins, const floa
   TVM_TRY(set_smem((const void*)composite_select_kernel, smem));
   composite_select_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(
       sigma, origins, dirs, R, s, mode, k, P, gumbel, gumbel_per_ray, sel_idx, w_sel, p_last, wsum,
-      dist_out);
+      dist_out, w_dense);
   return check_launch("composite_select");
 }
 

@@ -49,7 +49,10 @@ int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t
 int launch_composite_select(const float* sigma, const float* origins, const float* dirs, int64_t R,
                             const SamplerArgs& s, int mode, int k, const float* gumbel,
                             int gumbel_per_ray, int32_t* sel_idx, float* w_sel, float* p_last,
-                            float* wsum, float* dist_out, cudaStream_t st);
+                            float* wsum, float* dist_out, float* w_dense, cudaStream_t st);
+// Dense backward with explicit step sizes into dL/d(pre-softplus sum).
+int launch_segment_bwd_sum(const float* sigmas, const float* steps, int64_t R, int N, const float* g_pt,
+                           float* g_sum, cudaStream_t st);
 // Fused: per-ray colour, loss and the gradients entering the MLP and the compositing.
 int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last,
                       const float* wsum, int64_t R, int k, const float* target, float* color_out,
@@ -86,6 +89,24 @@ int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const floa
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
+
+int prop_mlp_forward(int math, const float* X, int64_t M, int units, const float* w1, const float* b1,
+                     const float* w2, const float* b2, float shift, float* H, float* sigma, cudaStream_t st);
+int prop_mlp_backward(int math, const float* X, int64_t M, int units, const float* w1, const float* w2,
+                      const float* H, const float* dz, float* dH, float* dX, float* gw1, float* gb1, float* gw2,
+                      float* gb2, cudaStream_t st);
+
+// ---- proposal network (tvm_proposal.cu) ----
+int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                         const float* edges, const float* jitter, float* X, float* delta, cudaStream_t st);
+int launch_prop_vm_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
+                       int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dX,
+                       cudaStream_t st);
+int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                    const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
+                    cudaStream_t st);
+int launch_prop_loss(const float* wmain, const float* wprop, const int32_t* bins, int64_t R, int Np, int Nm,
+                     float scale, float* loss, float* gprop, cudaStream_t st);
 
 // ---- Adam (tvm_adam.cu) ----
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,

@@ -84,6 +84,14 @@ struct EpiReluMask {
     }
   }
 };
+// out[m] = softplus(v + b + shift): the proposal density head (single column).
+struct EpiSoftplus {
+  float* out;
+  const float* bias;
+  float shift;
+  __device__ void operator()(int64_t m, int n, float v) const { out[m] = softplus_f(v + __ldg(bias) + shift); }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const { vec4_scalar(*this, m, n, v, N); }
+};
 struct EpiAtomic {
   float* C;
   int ldc;
@@ -403,6 +411,34 @@ int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const floa
   TVM_GEMM_CASE(true, true)
 #undef TVM_GEMM_CASE
   return TVM_ERR_INVALID;
+}
+
+}  // namespace tvm
+
+namespace tvm {
+
+// Proposal MLP 16 -> units -> 1 (see tvm_proposal.cu): H = relu(X W1 + b1),
+// sigma = softplus(H W2 + b2 + shift).
+int prop_mlp_forward(int math, const float* X, int64_t M, int units, const float* w1, const float* b1,
+                     const float* w2, const float* b2, float shift, float* H, float* sigma, cudaStream_t st) {
+  TVM_TRY((mm<false, false>(math, M, units, 16, X, 16, w1, units, EpiBiasAct{H, units, b1, 1}, st)));
+  return mm<false, false>(math, M, 1, units, H, units, w2, 1, EpiSoftplus{sigma, b2, shift}, st);
+}
+
+// Backward from dz = dL/d(pre-softplus): weight gradients ACCUMULATE, dX overwritten.
+int prop_mlp_backward(int math, const float* X, int64_t M, int units, const float* w1, const float* w2,
+                      const float* H, const float* dz, float* dH, float* dX, float* gw1, float* gb1, float* gw2,
+                      float* gb2, cudaStream_t st) {
+  TVM_TRY((mm<false, true>(math, M, units, 1, dz, 1, w2, 1, EpiReluMask{dH, units, H, units}, st)));
+  TVM_TRY((mm<true, false>(math, units, 1, M, H, units, dz, 1, EpiAtomic{gw2, 1}, st, -1)));
+  TVM_TRY((mm<false, true>(math, M, 16, units, dH, units, w1, units, EpiStore{dX, 16}, st)));
+  TVM_TRY((mm<true, false>(math, 16, units, M, X, 16, dH, units, EpiAtomic{gw1, units}, st, -1)));
+  const int64_t cs = 128;
+  colsum_kernel<<<dim3(1, (unsigned)ceil_div(M, cs)), 32, 0, st>>>(dz, 1, M, 1, cs, gb2);
+  TVM_TRY(check_launch("colsum"));
+  colsum_kernel<<<dim3((unsigned)ceil_div(units, 128), (unsigned)ceil_div(M, cs)), 128, 0, st>>>(dH, units, M, units,
+                                                                                                  cs, gb1);
+  return check_launch("colsum");
 }
 
 }  // namespace tvm

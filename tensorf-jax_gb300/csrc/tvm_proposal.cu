@@ -1,0 +1,347 @@
+// Proposal network: a density-only VM tensor (rank 4 per pair, small grid) plus a
+// 16 -> 64 -> 1 MLP that predicts where along each ray the full field is worth
+// evaluating. The reference has no such component (render.py:126 notes that "an
+// occupancy grid or proposal network would really help us here"); the design follows
+// the proposal sampling of mip-NeRF 360 (Barron et al., 2022):
+//
+//  * proposal bins: Np bins per ray over the aabb segment (bounded scenes) or over
+//    caller-given edges (unbounded scenes), one jittered sample per bin;
+//  * proposal density sigma^ = softplus(MLP([12 VM features, x, y, z, |x|_inf]) + shift),
+//    weights w^ by the same log-space compositing as the main field;
+//  * resampling: N+1 edges at the quantiles i/N of the bin histogram (w^ plus a 1%
+//    uniform floor), one jittered main sample per resulting interval;
+//  * training: the main field's weights w_i (no gradient) must not exceed the
+//    proposal mass over the bins their interval overlaps,
+//    L = lambda/R * sum_i max(0, w_i - bound_i)^2 / (w_i + 1e-7), gradient into w^ only.
+//
+// The MLP layers run on the shared tensor-core GEMM (tvm_mlp.cu); these kernels are
+// the per-sample VM features and their scatter, the resampler and the loss.
+#include "tvm_internal.h"
+
+namespace tvm {
+
+constexpr int PROP_C = 4;      // components per pair
+constexpr int PROP_IN = 16;    // MLP input width
+constexpr int PROP_MAXN = 512; // max proposal bins / main samples per ray
+
+// Bin edge j (0..Np) of a ray: t_min + j * step over its aabb segment (step = segment
+// length / Np, as the bounded sampler computes it), or the caller's edges.
+__device__ __forceinline__ float prop_edge(const RayGeom& g, const float* edges, int j) {
+  return edges ? __ldg(edges + j) : g.t_min + (float)j * g.step;
+}
+
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, float (&v)[4]);
+template <>
+__device__ __forceinline__ void load4<float>(const float* p, float (&v)[4]) {
+  const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <>
+__device__ __forceinline__ void load4<__nv_bfloat16>(const __nv_bfloat16* p, float (&v)[4]) {
+  const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.x));
+  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&q.y));
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+struct PropPair {
+  Tap tl, tr, tc;
+  float L[4], P[4];
+};
+
+template <typename T>
+__device__ __forceinline__ void prop_pair(const T* lines, const T* planes, int G, int m, float ul, float ur, float uc,
+                                          PropPair& e) {
+  e.tl = make_tap(ul, G);
+  e.tr = make_tap(ur, G);
+  e.tc = make_tap(uc, G);
+  const T* lb = lines + (int64_t)m * G * PROP_C;
+  const T* pb = planes + (int64_t)m * G * G * PROP_C;
+  float l0[4], l1[4], p00[4], p01[4], p10[4], p11[4];
+  load4<T>(lb + e.tl.i0 * PROP_C, l0);
+  load4<T>(lb + e.tl.i1 * PROP_C, l1);
+  load4<T>(pb + ((int64_t)e.tr.i0 * G + e.tc.i0) * PROP_C, p00);
+  load4<T>(pb + ((int64_t)e.tr.i0 * G + e.tc.i1) * PROP_C, p01);
+  load4<T>(pb + ((int64_t)e.tr.i1 * G + e.tc.i0) * PROP_C, p10);
+  load4<T>(pb + ((int64_t)e.tr.i1 * G + e.tc.i1) * PROP_C, p11);
+  const float w00 = e.tr.w0 * e.tc.w0, w01 = e.tr.w0 * e.tc.w1, w10 = e.tr.w1 * e.tc.w0, w11 = e.tr.w1 * e.tc.w1;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    e.L[c] = e.tl.w0 * l0[c] + e.tl.w1 * l1[c];
+    e.P[c] = w00 * p00[c] + w01 * p01[c] + w10 * p10[c] + w11 * p11[c];
+  }
+}
+
+// Geometry of proposal sample (r, j): world distance, bin length, normalised point.
+__device__ __forceinline__ void prop_sample(const RayGeom& g, const SamplerArgs& s, const float* edges, int Np,
+                                            const float* jitter, int64_t r, int j, float& t, float& len,
+                                            float (&x)[3]) {
+  const float e0 = prop_edge(g, edges, j);
+  const float e1 = prop_edge(g, edges, j + 1);
+  len = e1 - e0;
+  t = e0 + __ldg(jitter + r * Np + j) * len;
+  sample_point(g, s, t, x);
+}
+
+// Features X[s] = [12 VM features (pair-major), x, y, z, |x|_inf] and bin length.
+template <typename T>
+__global__ void prop_features_kernel(const T* __restrict__ lines, const T* __restrict__ planes, int G,
+                                     const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
+                                     SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter,
+                                     float* __restrict__ X, float* __restrict__ delta) {
+  const int Np = s.N;
+  const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (smp >= R * Np) return;
+  const int64_t r = smp / Np;
+  const int j = (int)(smp - r * Np);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, len, x[3];
+  prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  float out[PROP_IN];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PropPair e;
+    prop_pair<T>(lines, planes, G, m, u[a], u[b], u[c], e);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[m * 4 + q] = e.L[q] * e.P[q];
+  }
+  out[12] = x[0];
+  out[13] = x[1];
+  out[14] = x[2];
+  out[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
+  float4* dst = reinterpret_cast<float4*>(X + smp * PROP_IN);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  delta[smp] = len;
+}
+
+// Scatter dL/dX[:, 0:12] into the proposal field gradients (FP32).
+template <typename T>
+__global__ void prop_vm_bwd_kernel(const T* __restrict__ lines, const T* __restrict__ planes, int G,
+                                   float* __restrict__ glines, float* __restrict__ gplanes,
+                                   const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
+                                   SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter,
+                                   const float* __restrict__ dX) {
+  const int Np = s.N;
+  const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (smp >= R * Np) return;
+  const float4* g4 = reinterpret_cast<const float4*>(dX + smp * PROP_IN);
+  float gf[12];
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const float4 v = __ldg(g4 + q);
+    gf[4 * q] = v.x; gf[4 * q + 1] = v.y; gf[4 * q + 2] = v.z; gf[4 * q + 3] = v.w;
+  }
+  bool any = false;
+#pragma unroll
+  for (int q = 0; q < 12; ++q) any |= (gf[q] != 0.0f);
+  if (!any) return;
+  const int64_t r = smp / Np;
+  const int j = (int)(smp - r * Np);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, len, x[3];
+  prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PropPair e;
+    prop_pair<T>(lines, planes, G, m, u[a], u[b], u[c], e);
+    float* lb = glines + (int64_t)m * G * PROP_C;
+    float* pb = gplanes + (int64_t)m * G * G * PROP_C;
+    float v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.P[q] * e.tl.w0;
+    atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i0 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.P[q] * e.tl.w1;
+    atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i1 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+    const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
+    const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
+    const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.L[q] * w[k];
+      atomicAdd(reinterpret_cast<float4*>(pb + ((int64_t)rows[k] * G + cols[k]) * PROP_C),
+                make_float4(v[0], v[1], v[2], v[3]));
+    }
+  }
+}
+
+// Resampling, one warp per ray: histogram q_j = w^_j + (0.01 * sum w^ + 1e-4) / Np over
+// the Np bins, main edges at the quantiles i/N (i = 0..N) by linear interpolation
+// inside the bin, one main sample per interval at edge_i + jitter * length.
+__global__ void resample_kernel(const float* __restrict__ wprop, const float* __restrict__ origins,
+                                const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
+                                int Nm, const float* __restrict__ jitter, float* __restrict__ t_out,
+                                float* __restrict__ d_out, int32_t* __restrict__ bins) {
+  extern __shared__ float smem_f[];
+  const int Np = s.N;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* cdf = smem_f + warp * (2 * (Np + 1) + (Nm + 1));  // cdf[0..Np], edge[0..Np], sedge[0..Nm]
+  float* edge = cdf + (Np + 1);
+  float* sedge = edge + (Np + 1);
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (r >= R) return;
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float tot = 0.f;
+  for (int j = lane; j < Np; j += 32) tot += __ldg(wprop + r * Np + j);
+  tot = warp_sum(tot);
+  const float floor_w = (0.01f * tot + 1e-4f) / (float)Np;
+  float carry = 0.f;
+  if (lane == 0) cdf[0] = 0.f;
+  for (int base = 0; base < Np; base += 32) {
+    const int j = base + lane;
+    const float q = (j < Np) ? __ldg(wprop + r * Np + j) + floor_w : 0.f;
+    const float incl = warp_inclusive_scan(q, lane) + carry;
+    if (j < Np) cdf[j + 1] = incl;
+    carry = __shfl_sync(0xffffffffu, incl, 31);
+  }
+  for (int j = lane; j <= Np; j += 32) edge[j] = prop_edge(g, edges, j);
+  __syncwarp();
+  const float Q = carry;
+  for (int i = lane; i <= Nm; i += 32) {
+    int bin;
+    float e;
+    if (i == 0) {
+      bin = 0;
+      e = edge[0];
+    } else if (i == Nm) {
+      bin = Np - 1;
+      e = edge[Np];
+    } else {
+      const float target = Q * ((float)i / (float)Nm);
+      int lo = 0, hi = Np - 1;  // largest bin with cdf[bin] <= target
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cdf[mid] <= target) lo = mid; else hi = mid - 1;
+      }
+      bin = lo;
+      const float q = cdf[bin + 1] - cdf[bin];
+      const float f = q > 0.f ? fminf(fmaxf((target - cdf[bin]) / q, 0.f), 1.f) : 0.f;
+      e = edge[bin] + f * (edge[bin + 1] - edge[bin]);
+    }
+    sedge[i] = e;
+    bins[r * (Nm + 1) + i] = bin;
+  }
+  __syncwarp();
+  for (int i = lane; i < Nm; i += 32) {
+    const float a = sedge[i], b = fmaxf(sedge[i + 1], a);
+    const float len = b - a;
+    t_out[r * Nm + i] = a + __ldg(jitter + r * Nm + i) * len;
+    d_out[r * Nm + i] = len;
+  }
+}
+
+// Proposal bound loss and its gradient wrt w^ (one warp per ray).
+__global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* __restrict__ wprop,
+                                 const int32_t* __restrict__ bins, int64_t R, int Np, int Nm, float scale,
+                                 float* __restrict__ loss, float* __restrict__ gprop) {
+  extern __shared__ float smem_f[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* C = smem_f + warp * 2 * (Np + 2);
+  float* diff = C + (Np + 2);
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+  if (r >= R) return;
+  float carry = 0.f;
+  if (lane == 0) C[0] = 0.f;
+  for (int base = 0; base < Np; base += 32) {
+    const int j = base + lane;
+    const float q = (j < Np) ? __ldg(wprop + r * Np + j) : 0.f;
+    const float incl = warp_inclusive_scan(q, lane) + carry;
+    if (j < Np) C[j + 1] = incl;
+    carry = __shfl_sync(0xffffffffu, incl, 31);
+  }
+  for (int j = lane; j < Np + 2; j += 32) diff[j] = 0.f;
+  __syncwarp();
+  float my_loss = 0.f;
+  for (int i = lane; i < Nm; i += 32) {
+    const int lo = __ldg(bins + r * (Nm + 1) + i);
+    const int hi = __ldg(bins + r * (Nm + 1) + i + 1);
+    const float bound = C[hi + 1] - C[lo];
+    const float w = __ldg(wmain + r * Nm + i);
+    const float dd = fmaxf(w - bound, 0.f);
+    const float inv = 1.0f / (w + 1e-7f);
+    my_loss += dd * dd * inv;
+    const float gi = -2.0f * dd * inv * scale;
+    if (gi != 0.f) {
+      atomicAdd(&diff[lo], gi);
+      atomicAdd(&diff[hi + 1], -gi);
+    }
+  }
+  my_loss = warp_sum(my_loss);
+  if (lane == 0 && loss) atomicAdd(loss, my_loss * scale);
+  __syncwarp();
+  carry = 0.f;
+  for (int base = 0; base < Np; base += 32) {
+    const int j = base + lane;
+    const float v = (j < Np) ? diff[j] : 0.f;
+    const float incl = warp_inclusive_scan(v, lane) + carry;
+    if (j < Np) gprop[r * Np + j] = incl;
+    carry = __shfl_sync(0xffffffffu, incl, 31);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                         const float* edges, const float* jitter, float* X, float* delta, cudaStream_t st) {
+  const int64_t n = R * s.N;
+  if (n == 0) return TVM_OK;
+  const unsigned blocks = (unsigned)ceil_div(n, 128);
+  if (f.dtype == TVM_BF16)
+    prop_features_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(
+        (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, origins, dirs, R, s, edges, jitter, X, delta);
+  else
+    prop_features_kernel<float><<<blocks, 128, 0, st>>>((const float*)f.lines, (const float*)f.planes, f.G, origins,
+                                                        dirs, R, s, edges, jitter, X, delta);
+  return check_launch("prop_features");
+}
+
+int launch_prop_vm_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
+                       int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dX,
+                       cudaStream_t st) {
+  const int64_t n = R * s.N;
+  if (n == 0) return TVM_OK;
+  const unsigned blocks = (unsigned)ceil_div(n, 128);
+  if (f.dtype == TVM_BF16)
+    prop_vm_bwd_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>((const __nv_bfloat16*)f.lines,
+                                                              (const __nv_bfloat16*)f.planes, f.G, glines, gplanes,
+                                                              origins, dirs, R, s, edges, jitter, dX);
+  else
+    prop_vm_bwd_kernel<float><<<blocks, 128, 0, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines,
+                                                      gplanes, origins, dirs, R, s, edges, jitter, dX);
+  return check_launch("prop_vm_bwd");
+}
+
+int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
+                    const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
+                    cudaStream_t st) {
+  if (R == 0) return TVM_OK;
+  const int warps = 4;
+  const size_t smem = (size_t)warps * (2 * (s.N + 1) + (Nm + 1)) * sizeof(float);
+  resample_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(wprop, origins, dirs, R, s, edges, Nm, jitter,
+                                                                          t_out, d_out, bins);
+  return check_launch("resample");
+}
+
+int launch_prop_loss(const float* wmain, const float* wprop, const int32_t* bins, int64_t R, int Np, int Nm,
+                     float scale, float* loss, float* gprop, cudaStream_t st) {
+  if (R == 0) return TVM_OK;
+  const int warps = 4;
+  const size_t smem = (size_t)warps * 2 * (Np + 2) * sizeof(float);
+  prop_loss_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(wmain, wprop, bins, R, Np, Nm, scale, loss,
+                                                                           gprop);
+  return check_launch("prop_loss");
+}
+
+}  // namespace tvm

@@ -14,6 +14,9 @@ struct SamplerArgs {
   const float* schedule;  // CONTRACT: (N,)
   const float* jitter;    // BBOX: (N,) or (R,N) or NULL; CONTRACT: (R,N)
   int jitter_per_ray;     // BBOX only
+  const float* ts;        // EXPLICIT: (R,N) sample distances
+  const float* deltas;    // EXPLICIT: (R,N) segment lengths
+  int contract;           // EXPLICIT: contract points to [-2,2]^3 before normalising
 };
 
 struct RayGeom {
@@ -63,6 +66,9 @@ __device__ __forceinline__ void sample_t(const RayGeom& g, const SamplerArgs& s,
     tt = tt * g.step;
     t = g.t_min + tt;
     delta = g.step;
+  } else if (s.sampler == TVM_SAMPLER_EXPLICIT) {
+    t = __ldg(s.ts + r * s.N + i);
+    delta = __ldg(s.deltas + r * s.N + i);
   } else {
     // Fixed schedule, step = roll(ts,-1) - ts with the last copied from the one
     // before (render.py:154-155), jitter per sample (render.py:158-161).
@@ -81,7 +87,7 @@ __device__ __forceinline__ void sample_point(const RayGeom& g, const SamplerArgs
   float p[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) p[a] = g.o[a] + g.d[a] * t;
-  if (s.sampler == TVM_SAMPLER_CONTRACT) {
+  if (s.sampler == TVM_SAMPLER_CONTRACT || (s.sampler == TVM_SAMPLER_EXPLICIT && s.contract)) {
     float nrm = fmaxf(fabsf(p[0]), fmaxf(fabsf(p[1]), fabsf(p[2])));
     if (!(nrm <= 1.0f)) {
       float sc = 2.0f - 1.0f / nrm;

@@ -28,7 +28,7 @@ ERROR_NAMES = {
 TVM_F32, TVM_BF16, TVM_F64 = 0, 1, 2
 TVM_MLP_DEFAULT, TVM_MLP_SIMT_F32 = 0, 1
 TVM_MODE_RGB, TVM_MODE_DIST_MEDIAN, TVM_MODE_DIST_MEAN = 0, 1, 2
-TVM_SAMPLER_BBOX, TVM_SAMPLER_CONTRACT = 0, 1
+TVM_SAMPLER_BBOX, TVM_SAMPLER_CONTRACT, TVM_SAMPLER_PROPOSAL = 0, 1, 2
 
 
 class VmField(ctypes.Structure):
@@ -39,15 +39,19 @@ class VmField(ctypes.Structure):
 class ModelDesc(ctypes.Structure):
     _fields_ = [("grid_dim", c_int32), ("density_channels", c_int32), ("appearance_channels", c_int32),
                 ("feature_n_freqs", c_int32), ("viewdir_n_freqs", c_int32), ("squash_dim", c_int32),
-                ("units", c_int32), ("dtype", c_int32), ("mlp_math", c_int32), ("_pad", c_int32)]
+                ("units", c_int32), ("dtype", c_int32), ("mlp_math", c_int32), ("proposal_grid", c_int32),
+                ("proposal_rank", c_int32), ("proposal_units", c_int32), ("_pad", c_int32)]
 
 
 class ParamLayout(ctypes.Structure):
     _fields_ = [(n, c_int64) for n in (
         "density_lines", "density_planes", "appearance_lines", "appearance_planes",
-        "mlp_w0", "mlp_w1", "mlp_b1", "mlp_w2", "mlp_b2", "mlp_w3", "mlp_b3", "mlp_begin", "total",
+        "mlp_w0", "mlp_w1", "mlp_b1", "mlp_w2", "mlp_b2", "mlp_w3", "mlp_b3",
+        "proposal_lines", "proposal_planes", "proposal_w1", "proposal_b1", "proposal_w2", "proposal_b2",
+        "mlp_begin", "total",
         "shadow_density_lines", "shadow_density_planes", "shadow_appearance_lines",
-        "shadow_appearance_planes", "shadow_total")] + [("encoded_dim", c_int32), ("_pad", c_int32)]
+        "shadow_appearance_planes", "shadow_proposal_lines", "shadow_proposal_planes",
+        "shadow_total")] + [("encoded_dim", c_int32), ("_pad", c_int32)]
 
 
 class Rays(ctypes.Structure):
@@ -58,7 +62,9 @@ class RenderDesc(ctypes.Structure):
     _fields_ = [("density_samples", c_int32), ("appearance_samples", c_int32), ("mode", c_int32),
                 ("sampler", c_int32), ("density_shift", c_float), ("_pad0", c_float),
                 ("aabb", c_float * 6), ("schedule", c_void_p), ("jitter", c_void_p),
-                ("jitter_per_ray", c_int32), ("gumbel_per_ray", c_int32), ("gumbel", c_void_p)]
+                ("jitter_per_ray", c_int32), ("gumbel_per_ray", c_int32), ("gumbel", c_void_p),
+                ("proposal_samples", c_int32), ("contract", c_int32), ("proposal_jitter", c_void_p),
+                ("proposal_shift", c_float), ("proposal_loss_weight", c_float)]
 
 
 class AdamDesc(ctypes.Structure):

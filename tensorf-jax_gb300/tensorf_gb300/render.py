@@ -64,7 +64,9 @@ class ModelSpec:
     squash_dim: int = 27
     units: int = 128
     precision: str = "fp32"  # "fp32" or "bf16"
-    mlp_math: str = "tensor"  # "tensor" (tcgen05; split-bf16 in fp32 mode) or "simt" (fp32 only)
+    mlp_math: str = "tensor"  # "tensor" (tcgen05; split-tf32 in fp32 mode) or "simt" (fp32 only)
+    proposal_grid: int = 0    # proposal VM grid; 0 = no proposal network
+    proposal_units: int = 64
 
     def desc(self) -> _lib.ModelDesc:
         return _lib.ModelDesc(grid_dim=self.grid_dim, density_channels=self.density_feat_dim,
@@ -72,7 +74,9 @@ class ModelSpec:
                               feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs,
                               squash_dim=self.squash_dim, units=self.units,
                               dtype=_lib.TVM_BF16 if self.precision == "bf16" else _lib.TVM_F32,
-                              mlp_math=_lib.TVM_MLP_SIMT_F32 if self.mlp_math == "simt" else _lib.TVM_MLP_DEFAULT)
+                              mlp_math=_lib.TVM_MLP_SIMT_F32 if self.mlp_math == "simt" else _lib.TVM_MLP_DEFAULT,
+                              proposal_grid=self.proposal_grid, proposal_rank=4 if self.proposal_grid else 0,
+                              proposal_units=self.proposal_units)
 
     def mlp(self) -> networks.FeatureMlp:
         return networks.FeatureMlp(feature_squash_dim=self.squash_dim, units=self.units,
@@ -145,6 +149,16 @@ class LearnableParams:
     def appearance_mlp_params(self):
         return self.mlp_views()
 
+    def proposal_views(self, buf: Optional[torch.Tensor] = None) -> Dict[str, torch.Tensor]:
+        """The proposal network: field lines (3, Gp, 4) / planes (3, Gp, Gp, 4)
+        channel-last, MLP w1 (16, U), b1 (U,), w2 (U, 1), b2 (1,)."""
+        L, s = self.layout, self.spec
+        g, u = s.proposal_grid, s.proposal_units
+        return {"lines": self._seg(L.proposal_lines, (3, g, 4), buf),
+                "planes": self._seg(L.proposal_planes, (3, g, g, 4), buf),
+                "w1": self._seg(L.proposal_w1, (16, u), buf), "b1": self._seg(L.proposal_b1, (u,), buf),
+                "w2": self._seg(L.proposal_w2, (u, 1), buf), "b2": self._seg(L.proposal_b2, (1,), buf)}
+
     # ---- construction ----------------------------------------------------------
     @staticmethod
     def initialize(spec: ModelSpec, seed: int = 94709, scene_contraction: bool = False,
@@ -161,6 +175,8 @@ class LearnableParams:
                            torch.randn((3, spec.appearance_feat_dim, g, g), generator=gen) * 0.1),
             "mlp": spec.mlp().init_params(3 * spec.appearance_feat_dim, gen),
         }
+        if spec.proposal_grid:
+            ref["proposal"] = init_proposal(spec.proposal_grid, spec.proposal_units, gen)
         return LearnableParams.from_reference(spec, ref, scene_contraction, device)
 
     @staticmethod
@@ -186,6 +202,13 @@ class LearnableParams:
         for layer, d in ref["mlp"].items():
             for name, val in d.items():
                 views[layer][name].copy_(torch.as_tensor(val, dtype=torch.float32))
+        if spec.proposal_grid:
+            pv = lp.proposal_views()
+            pr = ref["proposal"]
+            pv["lines"].copy_(torch.as_tensor(pr["vector"], dtype=torch.float32).permute(0, 2, 1))
+            pv["planes"].copy_(torch.as_tensor(pr["matrix"], dtype=torch.float32).permute(0, 2, 3, 1))
+            for n in ("w1", "b1", "w2", "b2"):
+                pv[n].copy_(torch.as_tensor(pr[n], dtype=torch.float32).reshape(pv[n].shape))
         if spec.precision == "bf16":
             lp.shadow = torch.empty(lay.shadow_total, dtype=torch.bfloat16, device=device)
             lp.refresh_shadow()
@@ -199,6 +222,11 @@ class LearnableParams:
             lines, planes = self.field_views(which, buf)
             out[which] = (lines.permute(0, 2, 1).contiguous().cpu(), planes.permute(0, 3, 1, 2).contiguous().cpu())
         out["mlp"] = {k: {n: t.detach().cpu().clone() for n, t in d.items()} for k, d in self.mlp_views(buf).items()}
+        if self.spec.proposal_grid:
+            pv = self.proposal_views(buf)
+            out["proposal"] = {"vector": pv["lines"].permute(0, 2, 1).contiguous().cpu(),
+                               "matrix": pv["planes"].permute(0, 3, 1, 2).contiguous().cpu(),
+                               **{n: pv[n].detach().cpu().clone() for n in ("w1", "b1", "w2", "b2")}}
         return out
 
     def refresh_shadow(self) -> None:
@@ -234,21 +262,50 @@ class NoiseKey:
 @dataclasses.dataclass
 class RenderNoise:
     """Explicit noise: ``jitter`` (N,) shared by all rays (bounded scenes, as the
-    reference draws it) or (R, N); ``gumbel`` (N,) shared or (R, N)."""
+    reference draws it) or (R, N); ``gumbel`` (N,) shared or (R, N). Proposal-guided
+    sampling also needs ``proposal_jitter`` (R, Np) and a per-interval ``jitter`` (R, N)."""
     jitter: Optional[torch.Tensor]
     gumbel: Optional[torch.Tensor]
+    proposal_jitter: Optional[torch.Tensor] = None
 
 
-def draw_noise(key: NoiseKey, rays: int, config: RenderConfig, scene_contraction: bool) -> RenderNoise:
+@dataclasses.dataclass(frozen=True)
+class ProposalConfig:
+    """Proposal-guided sampling: ``samples`` proposal bins per ray resampled into the
+    RenderConfig's density_samples_per_ray main samples. Unbounded scenes take the
+    Np+1 bin edges from ``edges`` (default: linear in disparity over [near, far])."""
+    samples: int = 64
+    shift: float = 0.0
+    loss_weight: float = 1.0
+
+
+def init_proposal(grid: int, units: int, gen: torch.Generator) -> Dict[str, torch.Tensor]:
+    """Proposal network init: field N(0, 0.1^2) like the main field, kaiming-normal
+    first layer, lecun-normal head, zero biases (CPU float32, reference layout)."""
+    return {"vector": torch.randn((3, 4, grid), generator=gen) * 0.1,
+            "matrix": torch.randn((3, 4, grid, grid), generator=gen) * 0.1,
+            "w1": torch.randn((16, units), generator=gen) * math.sqrt(2.0 / 16),
+            "b1": torch.zeros(units), "w2": torch.randn((units, 1), generator=gen) * math.sqrt(1.0 / units),
+            "b2": torch.zeros(1)}
+
+
+def draw_noise(key: NoiseKey, rays: int, config: RenderConfig, scene_contraction: bool,
+               proposal: Optional[ProposalConfig] = None) -> RenderNoise:
     """Draw the noise render_rays needs from a key: the sample key drives the jitter
     ((N,) shared for bounded scenes, (R, N) for contracted ones, render.py:158-160,
-    375-379) and the rgb key the Gumbel noise shared by every ray (render.py:461-469)."""
+    375-379) and the rgb key the Gumbel noise shared by every ray (render.py:461-469).
+    Proposal-guided sampling draws per-ray jitter for both proposal bins and main
+    intervals."""
     sample_key, rgb_key = key.split()
     n = config.density_samples_per_ray
+    gumbel = rgb_key.gumbel(n) if config.mode is RenderMode.RGB else None
+    if proposal is not None:
+        k1, k2 = sample_key.split()
+        return RenderNoise(jitter=k1.uniform(rays * n).view(rays, n), gumbel=gumbel,
+                           proposal_jitter=k2.uniform(rays * proposal.samples).view(rays, proposal.samples))
     jitter = sample_key.uniform(rays * n if scene_contraction else n)
     if scene_contraction:
         jitter = jitter.view(rays, n)
-    gumbel = rgb_key.gumbel(n) if config.mode is RenderMode.RGB else None
     return RenderNoise(jitter=jitter, gumbel=gumbel)
 
 
@@ -279,13 +336,22 @@ def _aabb6(aabb) -> Sequence[float]:
 
 
 def make_render_desc(config: RenderConfig, aabb, noise: RenderNoise, rays: int, scene_contraction: bool,
-                     schedule: Optional[torch.Tensor], density_shift: float, mode: Optional[RenderMode] = None):
+                     schedule: Optional[torch.Tensor], density_shift: float, mode: Optional[RenderMode] = None,
+                     proposal: Optional[ProposalConfig] = None):
     mode = config.mode if mode is None else mode
     d = _lib.RenderDesc()
+    if proposal is not None:
+        d.sampler = _lib.TVM_SAMPLER_PROPOSAL
+        d.proposal_samples = proposal.samples
+        d.proposal_shift = proposal.shift
+        d.proposal_loss_weight = proposal.loss_weight
+        d.contract = int(scene_contraction)
+        d.proposal_jitter = ptr(noise.proposal_jitter).value if noise.proposal_jitter is not None else None
     d.density_samples = config.density_samples_per_ray
     d.appearance_samples = config.appearance_samples_per_ray
     d.mode = _MODE_CODE[mode]
-    d.sampler = _lib.TVM_SAMPLER_CONTRACT if scene_contraction else _lib.TVM_SAMPLER_BBOX
+    if proposal is None:
+        d.sampler = _lib.TVM_SAMPLER_CONTRACT if scene_contraction else _lib.TVM_SAMPLER_BBOX
     d.density_shift = density_shift
     for i, v in enumerate(_aabb6(aabb)):
         d.aabb[i] = v
@@ -304,11 +370,15 @@ def rays_struct(rays: "cameras.Rays3D") -> _lib.Rays:
                      directions=ptr(dvec, torch.float32, "directions"))
 
 
-def _schedule_for(config: RenderConfig, scene_contraction: bool, schedule) -> Optional[torch.Tensor]:
+def _schedule_for(config: RenderConfig, scene_contraction: bool, schedule,
+                  proposal: Optional[ProposalConfig] = None) -> Optional[torch.Tensor]:
     if not scene_contraction:
         return None
     if schedule is None:
-        schedule = contracted_schedule(config.near, config.far, config.density_samples_per_ray)
+        if proposal is not None:
+            schedule = disparity_schedule(config.near, config.far, proposal.samples + 1)
+        else:
+            schedule = contracted_schedule(config.near, config.far, config.density_samples_per_ray)
     return torch.as_tensor(schedule, dtype=torch.float32, device="cuda").contiguous()
 
 
@@ -317,15 +387,17 @@ def _schedule_for(config: RenderConfig, scene_contraction: bool, schedule) -> Op
 # ---------------------------------------------------------------------------------
 def render_rays(appearance_mlp: networks.FeatureMlp, learnable_params: LearnableParams, aabb,
                 rays_wrt_world: "cameras.Rays3D", prng_key: Union[NoiseKey, RenderNoise],
-                config: RenderConfig, *, density_shift: float = 10.0, schedule=None) -> torch.Tensor:
-    """render.py:105-279. Output (R, 3) for RGB, (R,) for distances."""
+                config: RenderConfig, *, density_shift: float = 10.0, schedule=None,
+                proposal: Optional[ProposalConfig] = None) -> torch.Tensor:
+    """render.py:105-279. Output (R, 3) for RGB, (R,) for distances. With ``proposal``
+    the density samples come from the proposal network (the model must have one)."""
     require_cuda()
     o = rays_wrt_world.origins.reshape(-1, 3)
     r = o.shape[0]
     sc = learnable_params.scene_contraction
-    noise = prng_key if isinstance(prng_key, RenderNoise) else draw_noise(prng_key, r, config, sc)
-    sched = _schedule_for(config, sc, schedule)
-    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift)
+    noise = prng_key if isinstance(prng_key, RenderNoise) else draw_noise(prng_key, r, config, sc, proposal)
+    sched = _schedule_for(config, sc, schedule, proposal)
+    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift, proposal=proposal)
     md = learnable_params.model_desc()
     rs = rays_struct(rays_wrt_world)
     nbytes = _lib.load().tvm_render_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
@@ -342,7 +414,7 @@ def render_rays(appearance_mlp: networks.FeatureMlp, learnable_params: Learnable
 def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: LearnableParams, aabb,
                         rays_wrt_world: "cameras.Rays3D", prng_key, config: RenderConfig, *,
                         batch_size: int = 4096, use_tqdm: bool = False, density_shift: float = 10.0,
-                        to_host: bool = True):
+                        to_host: bool = True, proposal: Optional[ProposalConfig] = None):
     """render.py:49-102: chunks of ``batch_size`` rays, concatenated. Rays stay on the
     device; ``to_host`` returns a NumPy array like the reference."""
     batch_axes = rays_wrt_world.origins.shape[:-1]
@@ -353,7 +425,7 @@ def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: L
     for start in range(0, total, batch_size):
         chunk = cameras.Rays3D(origins=o[start:start + batch_size], directions=d[start:start + batch_size])
         outs.append(render_rays(appearance_mlp, learnable_params, aabb, chunk, prng_key, config,
-                                density_shift=density_shift))
+                                density_shift=density_shift, proposal=proposal))
     out = torch.cat(outs, dim=0)
     out = out.reshape(tuple(batch_axes) + tuple(out.shape[1:]))
     return out.cpu().numpy() if to_host else out
@@ -361,14 +433,15 @@ def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: L
 
 def loss_and_grad(learnable_params: LearnableParams, grads: torch.Tensor, aabb, rays_wrt_world,
                   colors: torch.Tensor, noise: RenderNoise, config: RenderConfig, *, density_shift: float = 10.0,
-                  schedule=None) -> torch.Tensor:
+                  schedule=None, proposal: Optional[ProposalConfig] = None) -> torch.Tensor:
     """MSE of render_rays against colors and its gradient, ACCUMULATED into ``grads``
-    (flat layout). Returns the loss as a device scalar."""
+    (flat layout), plus the proposal bound loss's gradient when ``proposal`` is set.
+    Returns the MSE as a device scalar."""
     o = rays_wrt_world.origins.reshape(-1, 3)
     r = o.shape[0]
     sc = learnable_params.scene_contraction
-    sched = _schedule_for(config, sc, schedule)
-    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift)
+    sched = _schedule_for(config, sc, schedule, proposal)
+    desc = make_render_desc(config, aabb, noise, r, sc, sched, density_shift, proposal=proposal)
     md = learnable_params.model_desc()
     rs = rays_struct(rays_wrt_world)
     nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)

@@ -45,6 +45,7 @@ class TrainConfig:
     density_samples_per_ray: Optional[int] = None  # None: the reference heuristic
     appearance_samples_per_ray: Optional[int] = None
     density_shift: float = 10.0
+    proposal: Optional["render.ProposalConfig"] = None  # proposal-guided sampling
 
 
 def lr_decay_coeff(step: int, cfg: TrainConfig) -> float:
@@ -111,12 +112,13 @@ class TrainState:
         cfg = self.render_config()
         r = rays.origins.reshape(-1, 3).shape[0]
         lp = self.learnable_params
+        prop = self.config.proposal
         if noise is None:
             render_key, self.prng_key = self.prng_key.split()
-            noise = render.draw_noise(render_key, r, cfg, lp.scene_contraction)
-        sched = render._schedule_for(cfg, lp.scene_contraction, None)
+            noise = render.draw_noise(render_key, r, cfg, lp.scene_contraction, prop)
+        sched = render._schedule_for(cfg, lp.scene_contraction, None, prop)
         desc = render.make_render_desc(cfg, self.aabb, noise, r, lp.scene_contraction, sched,
-                                       self.config.density_shift)
+                                       self.config.density_shift, proposal=prop)
         md = lp.model_desc()
         key = (r, cfg)
         if self._ws_key != key:

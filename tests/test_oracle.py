@@ -203,3 +203,63 @@ def test_camera_rays_center_pixel_looks_forward():
     o, d = O.camera_pixel_rays(K, np.eye(3), np.zeros(3), 800, 800)
     mid = 399 * 800 + 399
     assert d[mid][2] > 0.999999
+
+
+def test_proposal_loss_gradient_matches_finite_differences():
+    # Resampling carries no gradient, so the check freezes the resampled intervals and
+    # bins and differentiates the bound loss wrt the proposal parameters alone.
+    gen = torch.Generator().manual_seed(0)
+    G, Gp, R, Np, N, k = 8, 6, 6, 12, 8, 4
+    prop = {"vector": torch.randn((3, 4, Gp), generator=gen, dtype=torch.float64) * 0.1,
+            "matrix": torch.randn((3, 4, Gp, Gp), generator=gen, dtype=torch.float64) * 0.1,
+            "w1": torch.randn((16, 16), generator=gen, dtype=torch.float64) * 0.3,
+            "b1": torch.zeros(16, dtype=torch.float64),
+            "w2": torch.randn((16, 1), generator=gen, dtype=torch.float64) * 0.3,
+            "b2": torch.zeros(1, dtype=torch.float64)}
+    params = {"density": O.vm_init(G, 8, gen), "appearance": O.vm_init(G, 8, gen), "mlp": O.mlp_init(24, 2, 2, gen)}
+    rng = np.random.default_rng(0)
+    o = rng.normal(size=(R, 3))
+    o = o / np.linalg.norm(o, axis=1, keepdims=True) * 4
+    d = -o + rng.normal(scale=0.05, size=(R, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o, d = torch.tensor(o), torch.tensor(d)
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3], dtype=torch.float64)
+    pj = torch.tensor(rng.uniform(size=(R, Np)))
+    jt = torch.tensor(rng.uniform(size=(R, N)))
+    gum = torch.tensor(-np.log(-np.log(rng.uniform(size=N))))
+    e, wp, _, _ = O.proposal_forward(prop, o, d, aabb, Np, pj, 0.5)
+    t, delta, bins = O.resample(e, wp, N, jt)
+    assert torch.all(delta >= 0) and torch.all(t[:, 1:] >= t[:, :-1] - 1e-12)
+    _, aux = O.render_explicit(params, aabb, o, d, t, delta, k, gum, density_shift=-1.0, return_aux=True)
+    wm = aux["p_terminates"].detach()
+
+    def loss():
+        _, wp2, _, _ = O.proposal_forward(prop, o, d, aabb, Np, pj, 0.5)
+        return O.proposal_loss(wm, wp2, bins, 1.0)
+
+    for tt in prop.values():
+        tt.requires_grad_(True)
+    grads = torch.autograd.grad(loss(), list(prop.values()))
+    h = 1e-6
+    with torch.no_grad():
+        for tt, gg in zip(prop.values(), grads):
+            for idx in range(min(4, tt.numel())):
+                old = float(tt.view(-1)[idx])
+                tt.view(-1)[idx] = old + h
+                lp = float(loss())
+                tt.view(-1)[idx] = old - h
+                lm = float(loss())
+                tt.view(-1)[idx] = old
+                fd = (lp - lm) / (2 * h)
+                assert abs(fd - float(gg.view(-1)[idx])) <= 1e-6 * max(1.0, abs(fd)) + 1e-9
+
+
+def test_resample_quantiles_follow_the_histogram():
+    # A proposal with all its mass in one bin puts ~99% of the main edges inside it.
+    edges = torch.linspace(0.0, 1.0, 9, dtype=torch.float64)[None]
+    w = torch.zeros((1, 8), dtype=torch.float64)
+    w[0, 5] = 1.0
+    t, delta, bins = O.resample(edges, w, 100, torch.full((1, 100), 0.5, dtype=torch.float64))
+    inside = ((t > 0.625) & (t < 0.75)).double().mean()
+    assert inside > 0.95
+    assert float(delta.sum()) == pytest.approx(1.0)
