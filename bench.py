@@ -1,15 +1,24 @@
-"""Benchmark of the TensoRF-VM train step on one GB300 (and N replicas under torchrun).
+"""Benchmark of the TensoRF-VM train step and full-frame render on one GB300.
 
-Default workload (--workload train_fp32): the single-GPU training step of a 300^3 VM
-field with 16 / 48 components per mode, a 4096-ray batch with 512 uniform density
-samples per ray and per-ray top-64 weighted selection of appearance samples, the
-FeatureMlp with 2-frequency encodings, MSE loss, full backward and Adam (lr 0.02 grids
-/ 1e-3 MLP), all FP32. Targets: an analytic scene of 32 random spheres (radius
-U[0.1, 0.4], density 50, RGB U[0, 1]) seen by seeded 800x800 cameras with focal length
-1111, rendered by FP64 quadrature with 4096 samples per ray. Synthetic, seeded.
+Headline (`value`): the single-GPU training step of a 300^3 VM field with 16 / 48
+components per mode, a 4096-ray batch with 512 uniform density samples per ray and
+per-ray top-64 weighted selection of appearance samples, the FeatureMlp with
+2-frequency encodings, MSE loss, full backward and Adam (lr 0.02 grids / 1e-3 MLP), all
+FP32 ("plain FP32"). Beside it, in the same line:
 
-One JSON line on stdout (rank 0). ``--impl reference`` times the CPU restatement of
-the reference's algorithm (the oracle) on the host cores instead.
+* the same step with planes, lines and MLP in BF16 ("bf16"),
+* the proposal-guided BF16 step: a 64^3 rank-4 proposal VM + 16-64-1 MLP, 64 proposal
+  samples resampled to 48 field samples ("proposal_bf16"),
+* held-out PSNR of each after the same number of training steps, the PSNR gap of the
+  proposal path against plain FP32,
+* full-frame render: 16 seeded 800x800 views (10.24M rays) in chunks of 65536 rays,
+  rays/s for plain FP32 (512 samples) and proposal BF16, their PSNR against each
+  other and the median-depth difference.
+
+Targets come from an analytic scene of 32 random spheres (radius U[0.1, 0.4], density
+50, RGB U[0, 1]) seen by seeded 800x800 cameras with focal length 1111, rendered by
+FP64 quadrature with 4096 samples per ray. ``--impl reference`` times the CPU
+restatement of the reference's algorithm (the oracle) on the host cores instead.
 """
 from __future__ import annotations
 
@@ -32,16 +41,19 @@ import numpy as np  # noqa: E402
 import torch  # noqa: E402
 
 METRIC = "train & render rays/s on 1 GB300: proposal+BF16 vs plain FP32 at ≤0.1 dB PSNR gap"
-PHASES = ["density_fwd", "composite_select", "appearance_fwd", "mlp_fwd", "color_loss", "mlp_bwd",
-          "appearance_bwd", "composite_bwd", "density_bwd", "adam"]
+PHASES = ["proposal_fwd", "density_fwd", "composite_select", "appearance_fwd", "mlp_fwd", "color_loss",
+          "mlp_bwd", "appearance_bwd", "composite_bwd", "density_bwd", "proposal_bwd", "adam"]
 
 
-def workload_cfg(name: str, small: bool = False):
-    w = dict(grid=300, Cd=16, Ca=48, R=4096, N=512, k=64, precision="fp32", pool_batches=8)
-    if name == "train_bf16":
+def variant_cfg(name: str, small: bool = False, prop_k: int = 16):
+    w = dict(name=name, grid=300, Cd=16, Ca=48, R=4096, N=512, k=64, precision="fp32", proposal=None,
+             prop_grid=0)
+    if name == "bf16":
         w["precision"] = "bf16"
-    if small:  # a case for ncu captures: same kernels, 1/4 of the rays
-        w.update(R=1024, pool_batches=2)
+    if name == "proposal_bf16":
+        w.update(precision="bf16", N=48, k=prop_k, proposal=64, prop_grid=64)
+    if small:  # the same kernels on 1/4 of the rays, for profiler captures
+        w["R"] = 1024
     return w
 
 
@@ -110,33 +122,150 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_problem(w, device, seed=0):
-    from tensorf_gb300 import render, scene, training
+# ---------------------------------------------------------------------------------
+# Data and models.
+# ---------------------------------------------------------------------------------
+class Data:
+    def __init__(self, R, seed=0, pool_batches=16, test_rays=8192):
+        from tensorf_gb300 import scene
+
+        self.sc = scene.SphereScene.random(seed, count=32)
+        cams = self.sc.cameras(116, seed=seed + 1)
+        self.train_cams, self.test_cams = cams[:100], cams[100:]
+        self.R = R
+        self.rays, self.colors = self.sc.training_rays(self.train_cams, R * pool_batches, seed=seed + 2,
+                                                       n_samples=4096)
+        self.test_rays, self.test_colors = self.sc.training_rays(self.test_cams, test_rays, seed=seed + 3,
+                                                                 n_samples=4096)
+
+    def batch(self, i):
+        from tensorf_gb300 import cameras
+
+        n = self.rays.origins.shape[0] // self.R
+        j = i % n
+        sl = slice(j * self.R, (j + 1) * self.R)
+        return cameras.Rays3D(self.rays.origins[sl], self.rays.directions[sl]), self.colors[sl]
+
+
+DENSITY_SHIFT = -3.0  # training from scratch starts from a nearly empty field
+
+
+def make_state(w, data):
+    from tensorf_gb300 import render, training
 
     spec = render.ModelSpec(grid_dim=w["grid"], density_feat_dim=w["Cd"], appearance_feat_dim=w["Ca"],
-                            precision=w["precision"])
-    sc = scene.SphereScene.random(seed, count=32)
-    cams = sc.cameras(100, seed=seed + 1)
-    total = w["R"] * w["pool_batches"]
-    rays, colors = sc.training_rays(cams, total, seed=seed + 2, n_samples=4096)
-    cfg = training.TrainConfig(initial_aabb_min=sc.aabb[0], initial_aabb_max=sc.aabb[1],
-                               density_samples_per_ray=w["N"], appearance_samples_per_ray=w["k"],
-                               n_iters=30000, upsamp_iters=())
-    state = training.TrainState.initialize(cfg, spec, seed=94709)
-    return spec, sc, state, rays, colors
+                            precision=w["precision"], proposal_grid=w["prop_grid"])
+    prop = render.ProposalConfig(samples=w["proposal"]) if w["proposal"] else None
+    cfg = training.TrainConfig(initial_aabb_min=data.sc.aabb[0], initial_aabb_max=data.sc.aabb[1],
+                               density_samples_per_ray=w["N"], appearance_samples_per_ray=w["k"], n_iters=30000,
+                               upsamp_iters=(), density_shift=DENSITY_SHIFT, proposal=prop)
+    return training.TrainState.initialize(cfg, spec, seed=94709)
 
 
-def batch(rays, colors, i, R):
-    from tensorf_gb300 import cameras
+def render_cfg(w, mode=None):
+    from tensorf_gb300 import render
 
-    n = rays.origins.shape[0] // R
-    j = i % n
-    return (cameras.Rays3D(rays.origins[j * R:(j + 1) * R], rays.directions[j * R:(j + 1) * R]),
-            colors[j * R:(j + 1) * R])
+    return render.RenderConfig(0.05, 200.0, mode or render.RenderMode.RGB, w["N"], w["k"])
+
+
+def proposal_of(w):
+    from tensorf_gb300 import render
+
+    return render.ProposalConfig(samples=w["proposal"]) if w["proposal"] else None
+
+
+def time_train(state, data, steps, warmup, phases=True, start_step=0):
+    """Warm-up, then `steps` timed steps on device-resident batches. Returns (ms total,
+    per-phase mean ms, kernel launches)."""
+    import ctypes
+
+    from tensorf_gb300 import _lib
+
+    lib = _lib.load()
+    for i in range(warmup):
+        r, c = data.batch(start_step + i)
+        state.training_step(r, c, log=False)
+    torch.cuda.synchronize()
+    n_ev = len(PHASES) + 1
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ev)] for _ in range(steps)] if phases else []
+    for row in evs:  # torch creates events lazily: record once so the handles exist
+        for e in row:
+            e.record()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = lib.tvm_kernel_launches()
+    start.record()
+    for i in range(steps):
+        if phases:
+            h = (ctypes.c_void_p * n_ev)(*[e.cuda_event for e in evs[i]])
+            _lib.call("tvm_set_phase_events", h, n_ev)
+        r, c = data.batch(start_step + warmup + i)
+        state.training_step(r, c, log=False)
+    _lib.call("tvm_set_phase_events", None, 0)
+    end.record()
+    torch.cuda.synchronize()
+    launches = int(lib.tvm_kernel_launches() - l0)
+    phase_ms = {}
+    if phases:
+        phase_ms = {p: statistics.mean(evs[i][j].elapsed_time(evs[i][j + 1]) for i in range(steps))
+                    for j, p in enumerate(PHASES)}
+    return start.elapsed_time(end), phase_ms, launches
+
+
+def train_more(state, data, steps, start_step):
+    for i in range(steps):
+        r, c = data.batch(start_step + i)
+        state.training_step(r, c, log=False)
+    torch.cuda.synchronize()
+
+
+def psnr(a, b):
+    return -10.0 * math.log10(max(float(((a - b) ** 2).mean()), 1e-10))
+
+
+def eval_rays(state, w, rays, mode=None, chunk=65536):
+    from tensorf_gb300 import render
+
+    return render.render_rays_batched(state.appearance_mlp, state.learnable_params, state.aabb, rays,
+                                      render.NoiseKey(12345), render_cfg(w, mode), batch_size=chunk,
+                                      density_shift=DENSITY_SHIFT, to_host=False, proposal=proposal_of(w))
+
+
+def time_render(state, w, data, views, chunk=65536):
+    """Full-frame render of `views` 800x800 views in chunks; device time of ray
+    generation + render, rays/s."""
+    from tensorf_gb300 import cameras, render
+
+    cams = (data.test_cams * (1 + views // len(data.test_cams)))[:views]
+    rc = render_cfg(w)
+    prop = proposal_of(w)
+    key = render.NoiseKey(777)
+    rays = cams[0].pixel_rays_wrt_world()  # warm-up chunk
+    render.render_rays(state.appearance_mlp, state.learnable_params, state.aabb,
+                       cameras.Rays3D(rays.origins[:chunk], rays.directions[:chunk]), key, rc,
+                       density_shift=DENSITY_SHIFT, proposal=prop)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total = 0
+    img = None
+    e0.record()
+    for cam in cams:
+        rays = cam.pixel_rays_wrt_world()
+        n = rays.origins.shape[0]
+        out = torch.empty((n, 3), device="cuda")
+        for s in range(0, n, chunk):
+            sub = cameras.Rays3D(rays.origins[s:s + chunk], rays.directions[s:s + chunk])
+            out[s:s + chunk] = render.render_rays(state.appearance_mlp, state.learnable_params, state.aabb, sub, key,
+                                                  rc, density_shift=DENSITY_SHIFT, proposal=prop)
+        total += n
+        img = out
+    e1.record()
+    torch.cuda.synchronize()
+    return total / (e0.elapsed_time(e1) / 1e3), img
 
 
 def algorithmic_bytes(w, phase):
-    """Algorithmic bytes of one launch of each phase (documented in the design doc)."""
+    """Algorithmic bytes of one launch of each gather/scatter phase."""
     R, N, k = w["R"], w["N"], w["k"]
     s = 2 if w["precision"] == "bf16" else 4
     dens_el, app_el = 18 * w["Cd"], 18 * w["Ca"]
@@ -151,10 +280,49 @@ def algorithmic_bytes(w, phase):
     }.get(phase)
 
 
-def run_ours(args):
-    import ctypes
+def mlp_flops(w, phase):
+    """Dense-layer FLOPs of the FeatureMlp per step: forward 2 * rows * 39856 (one
+    multiply-add per weight per row at 2-frequency encodings), backward twice that."""
+    rows = w["R"] * w["k"]
+    per_row = 144 * 27 + 150 * 128 + 128 * 128 + 128 * 3
+    return {"mlp_fwd": 2 * rows * per_row, "mlp_bwd": 4 * rows * per_row}.get(phase)
 
-    from tensorf_gb300 import _lib, cameras, render, training
+
+def roofline_for(w, phase_ms):
+    hbm, bf16, src = measured_peaks()
+    dom = max(phase_ms, key=lambda p: phase_ms[p])
+    if dom in ("mlp_fwd", "mlp_bwd"):
+        tflops = mlp_flops(w, dom) / (phase_ms[dom] / 1e3) / 1e12
+        if w["precision"] == "bf16":
+            peak, note = bf16, "bf16 tcgen05 against the measured bf16 peak"
+        else:
+            # FP32-accurate path: 3 tf32 MMAs per product at half the bf16 rate, so the
+            # algorithmic FLOP peak is the measured bf16 peak / 6.
+            peak, note = bf16 / 6.0, "split-tf32 (3 tf32 MMAs per product): peak = measured bf16 / 6"
+        return {"bound": "tensor", "kernel": dom, "achieved": round(tflops, 2), "peak": round(peak, 1),
+                "unit": "TFLOP/s", "frac": round(tflops / peak, 4), "traffic": None, "peak_source": src,
+                "note": note}
+    gb = algorithmic_bytes(w, dom) / (phase_ms[dom] / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": dom, "achieved": round(gb, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(gb / hbm, 4), "traffic": None, "peak_source": src,
+            "note": "gathers/scatters are L2-resident: algorithmic bytes over the measured HBM copy peak"}
+
+
+def run_profile_variant(args):
+    """Only one variant's warm-up and timed steps (for profiler launch lists)."""
+    from tensorf_gb300 import _lib
+
+    _lib.load()
+    w = variant_cfg(args.profile_variant, args.small, args.prop_k)
+    data = Data(w["R"], pool_batches=4, test_rays=256)
+    st = make_state(w, data)
+    ms, ph, launches = time_train(st, data, args.steps, args.warmup)
+    print(json.dumps({"variant": w["name"], "ms_per_step": round(ms / args.steps, 4), "launches": launches,
+                      "phase_ms": {p: round(v, 4) for p, v in ph.items()}}), flush=True)
+
+
+def run_ours(args):
+    from tensorf_gb300 import _lib, cameras, render
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -164,120 +332,121 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    lib = _lib.load()
-    w = workload_cfg(args.workload, args.small)
-    spec, sc, state, rays, colors = build_problem(w, "cuda", seed=rank)
+    _lib.load()
+    plain = variant_cfg("plain_fp32", args.small)
+    data = Data(plain["R"], seed=rank)
     torch.cuda.synchronize()
 
-    # Warm-up.
-    for i in range(args.warmup):
-        b_r, b_c = batch(rays, colors, i, w["R"])
-        state.training_step(b_r, b_c, log=False)
-    torch.cuda.synchronize()
-
-    # Timed region: device-resident inputs, phase events on the launching stream.
-    n_ev = len(PHASES) + 1
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(n_ev)] for _ in range(args.steps)]
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for row in evs:  # torch creates events lazily: record once so the handles exist
-        for e in row:
-            e.record()
-    torch.cuda.synchronize()
-    launches0 = lib.tvm_kernel_launches()
+    # Headline: plain FP32 train step, device-resident batches.
+    st_plain = make_state(plain, data)
     if dist:
         dist.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        start.record()
-        for i in range(args.steps):
-            handles = (ctypes.c_void_p * n_ev)(*[e.cuda_event for e in evs[i]])
-            _lib.call("tvm_set_phase_events", handles, n_ev)
-            b_r, b_c = batch(rays, colors, args.warmup + i, w["R"])
-            state.training_step(b_r, b_c, log=False)
-        _lib.call("tvm_set_phase_events", None, 0)
-        end.record()
-        torch.cuda.synchronize()
+        ms, phase_ms, launches = time_train(st_plain, data, args.steps, args.warmup)
     if dist:
         dist.barrier()
-    launches = int(lib.tvm_kernel_launches() - launches0)
-    ms = start.elapsed_time(end)
-    phase_ms = {p: statistics.mean(evs[i][j].elapsed_time(evs[i][j + 1]) for i in range(args.steps))
-                for j, p in enumerate(PHASES)}
-    if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = w["R"] * args.steps * world / (ms / 1e3)
-    final_loss = float(state.loss.item())
+    value = plain["R"] * args.steps * world / (ms / 1e3)
+    done_plain = args.warmup + args.steps
 
-    # End to end through the public API: host (pinned) rays and colours copied in every
+    # End to end through the public API: pinned host rays and colours copied in every
     # step, the loss read back every step.
-    host_o = rays.origins.cpu().pin_memory()
-    host_d = rays.directions.cpu().pin_memory()
-    host_c = colors.cpu().pin_memory()
-    dev_o = torch.empty((w["R"], 3), device="cuda")
-    dev_d = torch.empty((w["R"], 3), device="cuda")
-    dev_c = torch.empty((w["R"], 3), device="cuda")
+    R = plain["R"]
+    host_o = data.rays.origins.cpu().pin_memory()
+    host_d = data.rays.directions.cpu().pin_memory()
+    host_c = data.colors.cpu().pin_memory()
+    dev_o, dev_d, dev_c = (torch.empty((R, 3), device="cuda") for _ in range(3))
     loss_host = torch.empty(1).pin_memory()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    npool = host_o.shape[0] // w["R"]
+    npool = host_o.shape[0] // R
     for i in range(args.steps):
-        j = i % npool
-        sl = slice(j * w["R"], (j + 1) * w["R"])
+        sl = slice((i % npool) * R, (i % npool + 1) * R)
         dev_o.copy_(host_o[sl], non_blocking=True)
         dev_d.copy_(host_d[sl], non_blocking=True)
         dev_c.copy_(host_c[sl], non_blocking=True)
-        state.training_step(cameras.Rays3D(dev_o, dev_d), dev_c, log=False)
-        loss_host.copy_(state.loss, non_blocking=True)
+        st_plain.training_step(cameras.Rays3D(dev_o, dev_d), dev_c, log=False)
+        loss_host.copy_(st_plain.loss, non_blocking=True)
     e1.record()
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
+    done_plain += args.steps
     if dist:
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e_value = w["R"] * args.steps * world / (e2e_ms / 1e3)
-
-    # Roofline of the dominant phase.
-    hbm, bf16, peak_src = measured_peaks()
-    dom = max((p for p in phase_ms if algorithmic_bytes(w, p) is not None), key=lambda p: phase_ms[p])
-    achieved = algorithmic_bytes(w, dom) / (phase_ms[dom] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": None, "peak_source": peak_src,
-                "note": "gathers/scatters are L2-resident: algorithmic bytes over the measured HBM copy peak"}
-    prof = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            tr = json.load(f).get(args.workload, {}).get(dom)
-        if tr:
-            roofline["traffic"] = tr
+    e2e_value = R * args.steps * world / (e2e_ms / 1e3)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if w["precision"] == "fp32" else "bf16",
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (32-sphere analytic scene, FP64 quadrature targets, seeded cameras)",
-        "config": {"workload": f"train step {w['precision']}: grid {w['grid']}^3, VM {w['Cd']}/{w['Ca']}, "
-                               f"{w['R']} rays x {w['N']} samples, top-{w['k']} appearance, Adam",
-                   "rays_per_step": w["R"], "density_samples": w["N"], "appearance_samples": w["k"],
-                   "grid": w["grid"], "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "no flush: each step streams params+grads+Adam moments (277 MB) and 2.1 GB of "
-                         "per-sample work, both larger than the 126 MB L2"},
+        "config": {"workload": f"train step fp32: grid {plain['grid']}^3, VM {plain['Cd']}/{plain['Ca']}, "
+                               f"{plain['R']} rays x {plain['N']} uniform samples, top-{plain['k']} appearance, Adam",
+                   "rays_per_step": plain["R"], "density_samples": plain["N"], "appearance_samples": plain["k"],
+                   "grid": plain["grid"], "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "no flush: each step streams params+grads+Adam moments (277 MB) and >2 GB of per-sample "
+                         "work, both larger than the 126 MB L2"},
         "phase_ms": {p: round(v, 4) for p, v in phase_ms.items()},
-        "final_loss": final_loss,
-        "e2e": {"value": round(e2e_value, 1), "unit": "rays/s", "h2d_bytes_per_step": w["R"] * 9 * 4,
+        "e2e": {"value": round(e2e_value, 1), "unit": "rays/s", "h2d_bytes_per_step": R * 9 * 4,
                 "d2h_bytes_per_step": 4},
         "gpu_launches": launches,
-        "roofline": roofline,
+        "roofline": roofline_for(plain, phase_ms),
         "clocks": clk.summary(),
     }
+
+    if not args.headline_only and world == 1:
+        variants = {"plain_fp32": {"train_rays_per_s": round(value, 1), "ms_per_step": round(ms / args.steps, 4)}}
+        states = {"plain_fp32": (plain, st_plain, done_plain)}
+        for name in ("bf16", "proposal_bf16"):
+            w = variant_cfg(name, args.small, args.prop_k)
+            st = make_state(w, data)
+            vms, vph, _ = time_train(st, data, args.steps, args.warmup)
+            variants[name] = {"train_rays_per_s": round(w["R"] * args.steps / (vms / 1e3), 1),
+                              "ms_per_step": round(vms / args.steps, 4),
+                              "phase_ms": {p: round(v, 4) for p, v in vph.items()},
+                              "density_samples": w["N"], "appearance_samples": w["k"],
+                              "proposal_samples": w["proposal"]}
+            states[name] = (w, st, args.warmup + args.steps)
+        # The same number of training steps for every variant, then held-out PSNR.
+        for name, (w, st, done) in states.items():
+            train_more(st, data, max(0, args.train_steps - done), done)
+            img = eval_rays(st, w, data.test_rays)
+            variants[name]["psnr_db"] = round(psnr(img, data.test_colors), 3)
+            variants[name]["train_steps"] = max(args.train_steps, done)
+        # Full-frame render: plain FP32 (512 samples) vs proposal BF16.
+        imgs = {}
+        for name in ("plain_fp32", "proposal_bf16"):
+            w, st, _ = states[name]
+            rps, img = time_render(st, w, data, args.render_views)
+            variants[name]["render_rays_per_s"] = round(rps, 1)
+            imgs[name] = img
+        rp, rq = variants["plain_fp32"]["render_rays_per_s"], variants["proposal_bf16"]["render_rays_per_s"]
+        # Median depth of the held-out rays under both paths.
+        w0, s0, _ = states["plain_fp32"]
+        w1, s1, _ = states["proposal_bf16"]
+        d0 = eval_rays(s0, w0, data.test_rays, render.RenderMode.DIST_MEDIAN)
+        d1 = eval_rays(s1, w1, data.test_rays, render.RenderMode.DIST_MEDIAN)
+        both = torch.isfinite(d0) & torch.isfinite(d1)
+        line["variants"] = variants
+        line["comparison"] = {
+            "train_speedup_proposal_bf16_vs_plain_fp32": round(variants["proposal_bf16"]["train_rays_per_s"] / value, 3),
+            "render_speedup_proposal_bf16_vs_plain_fp32": round(rq / rp, 3),
+            "psnr_gap_db_plain_minus_proposal_bf16": round(variants["plain_fp32"]["psnr_db"] -
+                                                          variants["proposal_bf16"]["psnr_db"], 3),
+            "render_psnr_proposal_vs_plain_db": round(psnr(imgs["proposal_bf16"], imgs["plain_fp32"]), 3),
+            "median_depth_abs_diff_mean": round(float((d0[both] - d1[both]).abs().mean()), 5) if both.any() else None,
+            "median_depth_terminated_agree": round(float((torch.isfinite(d0) == torch.isfinite(d1)).float().mean()), 4),
+            "render_views": args.render_views, "render_chunk": 65536,
+        }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args)
+        line["cpu_baseline"] = cpu_baseline(plain, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -337,15 +506,16 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    w = workload_cfg(args.workload, args.small)
+    w = variant_cfg("plain_fp32", args.small)
     threads = os.cpu_count() or 1
     torch.set_num_threads(threads)
     sample = args.cpu_sample_rays
     for _ in range(max(0, min(args.warmup, 1))):
         _cpu_step_time(w, max(8, sample // 8))
+    steps = min(args.steps, args.reference_steps)
     times = []
     t_start = time.perf_counter()
-    for i in range(args.steps):
+    for i in range(steps):
         fb, adam = _cpu_step_time(w, sample, seed=i)
         times.append(fb * (w["R"] / sample) + adam)
     wall = time.perf_counter() - t_start
@@ -353,12 +523,11 @@ def run_reference(args):
     value = w["R"] / step_s
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "rays/s", "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32" if w["precision"] == "fp32" else "bf16",
+        "steps": steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded rays, N(0, 0.1^2) parameters)",
-        "config": {"workload": f"train step {w['precision']}: grid {w['grid']}^3, VM {w['Cd']}/{w['Ca']}, "
-                               f"{w['R']} rays x {w['N']} samples, top-{w['k']} appearance, Adam",
+        "config": {"workload": f"train step fp32: grid {w['grid']}^3, VM {w['Cd']}/{w['Ca']}, "
+                               f"{w['R']} rays x {w['N']} uniform samples, top-{w['k']} appearance, Adam",
                    "rays_per_step": w["R"]},
         "cpu_baseline": {"value": round(value, 2), "unit": "rays/s", "cores": threads, "kind": "port",
                          "sample": f"each step: oracle forward+backward of {sample} rays scaled to {w['R']}, "
@@ -375,15 +544,22 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["train_fp32", "train_bf16"], default="train_fp32")
     ap.add_argument("--small", action="store_true", help="1024-ray case for profiler captures")
+    ap.add_argument("--headline-only", action="store_true", help="only the plain FP32 train step")
+    ap.add_argument("--train-steps", type=int, default=1500, help="training steps before the PSNR comparison")
+    ap.add_argument("--render-views", type=int, default=16)
+    ap.add_argument("--prop-k", type=int, default=16, help="appearance samples of the proposal path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rays", type=int, default=256)
+    ap.add_argument("--reference-steps", type=int, default=10)
+    ap.add_argument("--profile-variant", choices=["plain_fp32", "bf16", "proposal_bf16"], default=None)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile_variant:
+        run_profile_variant(args)
     else:
         run_ours(args)
 

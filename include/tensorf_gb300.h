@@ -178,9 +178,10 @@ TVM_API uint64_t tvm_kernel_launches(void);
 /* Measurement hook: when `events` (n cudaEvent_t created by the caller) is set for the
  * calling thread, tvm_train_step / tvm_loss_and_grad / tvm_render_fwd record
  * events[i] on their stream at the boundary before phase i and events[n_phases] after
- * the last one (phases: 0 density fwd, 1 composite+select, 2 appearance gather,
- * 3 MLP fwd, 4 colour+loss, 5 MLP bwd, 6 appearance scatter, 7 composite bwd,
- * 8 density scatter, 9 Adam). Unused trailing phases record nothing. NULL disables. */
+ * the last one (phases: 0 proposal network forward + resampling, 1 density fwd,
+ * 2 composite+select, 3 appearance gather, 4 MLP fwd, 5 colour+loss, 6 MLP bwd,
+ * 7 appearance scatter, 8 composite bwd, 9 density scatter, 10 proposal loss +
+ * backward, 11 Adam). Unused trailing phases record nothing. NULL disables. */
 TVM_API int tvm_set_phase_events(void* const* events, int32_t n);
 
 /* ---- parameter layout ---------------------------------------------------------- */

@@ -68,7 +68,7 @@ static int validate_model(const tvm_model_desc* m) {
     TVM_REQUIRE(m->proposal_grid >= 2 && m->proposal_grid <= 1024, TVM_ERR_SHAPE, "proposal_grid=%d outside [2, 1024]",
                 m->proposal_grid);
     TVM_REQUIRE(m->proposal_rank == 4, TVM_ERR_UNSUPPORTED, "proposal_rank must be 4");
-    TVM_REQUIRE(m->proposal_units >= 1 && m->proposal_units <= 256, TVM_ERR_SHAPE, "proposal_units outside [1, 256]");
+    TVM_REQUIRE(m->proposal_units >= 1 && m->proposal_units <= 128, TVM_ERR_SHAPE, "proposal_units outside [1, 128]");
   }
   return TVM_OK;
 }
@@ -221,7 +221,7 @@ struct PassBufs {
   int32_t* sel;
   float *w_sel, *p_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
   // proposal-guided sampling
-  float *Xp, *Hp, *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *dHp, *dXp, *loss_p;
+  float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p;
   int32_t* bins;
 };
 
@@ -248,9 +248,6 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
   }
   if (c.sampler == TVM_SAMPLER_PROPOSAL) {
     const int64_t S = R * c.proposal_samples;
-    const int64_t U = m.proposal_units;
-    b.Xp = ws.take<float>(S * 16);
-    b.Hp = ws.take<float>(S * U);
     b.sig_p = ws.take<float>(S);
     b.delta_p = ws.take<float>(S);
     b.w_p = ws.take<float>(S);
@@ -261,8 +258,6 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
       b.w_dense = ws.take<float>(R * N);
       b.g_wp = ws.take<float>(S);
       b.dz_p = ws.take<float>(S);
-      b.dHp = ws.take<float>(S * U);
-      b.dXp = ws.take<float>(S * 16);
       b.loss_p = ws.take<float>(1);
     }
   }
@@ -315,13 +310,15 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   const SamplerArgs sp = proposal ? proposal_sampler(c) : SamplerArgs{};
   const float* edges = (proposal && c.contract) ? c.schedule : nullptr;
   const int64_t S = R * c.proposal_samples;
+  phase_mark(0, st);
   if (proposal) {
     // Proposal network forward, then resampling into explicit main samples.
+    // Features and the 16-U-1 MLP in one kernel; X and h are kept only for the backward.
     const FieldView fp = proposal_field(m, L, params, shadow);
-    TVM_TRY(launch_prop_features(fp, rays.origins, rays.directions, R, sp, edges, c.proposal_jitter, b.Xp,
-                                 b.delta_p, st));
-    TVM_TRY(prop_mlp_forward(d.math, b.Xp, S, m.proposal_units, params + L.proposal_w1, params + L.proposal_b1,
-                             params + L.proposal_w2, params + L.proposal_b2, c.proposal_shift, b.Hp, b.sig_p, st));
+    const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
+                     params + L.proposal_b2, c.proposal_shift, nullptr, b.sig_p};
+    TVM_TRY(launch_prop_features(fp, rays.origins, rays.directions, R, sp, edges, c.proposal_jitter, nullptr,
+                                 b.delta_p, &pm, st));
     TVM_TRY(launch_segment_fwd(b.sig_p, b.delta_p, R, c.proposal_samples, nullptr, b.w_p, st));
     TVM_TRY(launch_resample(b.w_p, rays.origins, rays.directions, R, sp, edges, c.density_samples, c.jitter,
                             b.t_main, b.d_main, b.bins, st));
@@ -337,46 +334,46 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   const FieldView fa = appearance_field(m, L, params, shadow);
   const int k = c.appearance_samples;
 
-  phase_mark(0, st);
-  TVM_TRY(launch_density_fwd(fd, c.density_shift, rays.origins, rays.directions, R, s, b.sigma, st));
   phase_mark(1, st);
+  TVM_TRY(launch_density_fwd(fd, c.density_shift, rays.origins, rays.directions, R, s, b.sigma, st));
+  phase_mark(2, st);
   if (c.mode != TVM_MODE_RGB) {
     TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, 0, nullptr, 0,
                                     nullptr, nullptr, nullptr, nullptr, out, nullptr, st));
-    phase_mark(2, st);
+    phase_mark(3, st);
     return TVM_OK;
   }
   TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
                                   c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.wsum, nullptr,
                                   (proposal && backward) ? b.w_dense : nullptr, st));
-  phase_mark(2, st);
-  TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(3, st);
+  TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
+  phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
   TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, backward, st));
-  phase_mark(4, st);
+  phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
                               nullptr, nullptr, st));
-    phase_mark(5, st);
+    phase_mark(6, st);
     return TVM_OK;
   }
   TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, colors, out, loss, b.dZ3, b.gw,
                             b.gP, st));
-  phase_mark(5, st);
+  phase_mark(6, st);
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
   TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, R * k, b.dZ3, b.dX0, ws2, st));
-  phase_mark(6, st);
+  phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
-  phase_mark(7, st);
+  phase_mark(8, st);
   TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
                                b.gsum, st));
-  phase_mark(8, st);
+  phase_mark(9, st);
   TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
                              rays.directions, R, s, b.gsum, st));
-  phase_mark(9, st);
+  phase_mark(10, st);
   if (proposal) {
     // Proposal bound loss on the main weights, then the proposal network backward.
     cudaError_t e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), st);
@@ -384,13 +381,14 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
     TVM_TRY(launch_prop_loss(b.w_dense, b.w_p, b.bins, R, c.proposal_samples, c.density_samples,
                              c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, st));
     TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, st));
-    TVM_TRY(prop_mlp_backward(d.math, b.Xp, S, m.proposal_units, params + L.proposal_w1, params + L.proposal_w2,
-                              b.Hp, b.dz_p, b.dHp, b.dXp, grads + L.proposal_w1, grads + L.proposal_b1,
-                              grads + L.proposal_w2, grads + L.proposal_b2, st));
     const FieldView fp = proposal_field(m, L, params, shadow);
-    TVM_TRY(launch_prop_vm_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins,
-                               rays.directions, R, sp, edges, c.proposal_jitter, b.dXp, st));
+    const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
+                     params + L.proposal_b2, c.proposal_shift, nullptr, nullptr};
+    TVM_TRY(launch_prop_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins, rays.directions,
+                            R, sp, edges, c.proposal_jitter, b.dz_p, pm, grads + L.proposal_w1,
+                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, st));
   }
+  phase_mark(11, st);
   return TVM_OK;
 }
 
@@ -661,7 +659,7 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
   TVM_TRY(tvm_loss_and_grad(model, params, shadow, grads, rays, colors, cfg, loss_out, workspace,
                             workspace_bytes, stream));
   TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
-  phase_mark(10, as_stream(stream));
+  phase_mark(12, as_stream(stream));
   return TVM_OK;
 }
 

@@ -80,28 +80,42 @@ size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);
 // rgb = FeatureMlp(X0, viewdir). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...].
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st);
-// Needs the buffers kept by the preceding mlp_forward on the same workspace.
+// Needs the buffers kept by the preceding mlp_forward on the same workspace (stored
+// feature-major when mlp_fused_supported(d), row-major otherwise).
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0,
                  int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
 int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
+int fused_status(int32_t* out, cudaStream_t st);   // same for the fused MLP kernel
+bool mlp_fused_supported(const MlpDims& d);
+// Writes X1 [enc][M], H1 [units][M], H2 [units][M] feature-major when non-null.
+// wpack: mlp_fused_pack_bytes() of scratch (16-byte aligned) for the packed weights.
+size_t mlp_fused_pack_bytes();
+int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
+                         int64_t M, float* rgb, float* X1, float* H1, float* H2, uint8_t* wpack, cudaStream_t st);
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
 
-int prop_mlp_forward(int math, const float* X, int64_t M, int units, const float* w1, const float* b1,
-                     const float* w2, const float* b2, float shift, float* H, float* sigma, cudaStream_t st);
-int prop_mlp_backward(int math, const float* X, int64_t M, int units, const float* w1, const float* w2,
-                      const float* H, const float* dz, float* dH, float* dX, float* gw1, float* gb1, float* gw2,
-                      float* gb2, cudaStream_t st);
 
 // ---- proposal network (tvm_proposal.cu) ----
+// The proposal MLP evaluated inside the feature kernel (H may be null: inference).
+struct PropMlp {
+  int units;
+  const float *w1, *b1, *w2, *b2;
+  float shift;
+  float* H;
+  float* sigma;
+};
 int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
-                         const float* edges, const float* jitter, float* X, float* delta, cudaStream_t st);
-int launch_prop_vm_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
-                       int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dX,
-                       cudaStream_t st);
+                         const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
+                         cudaStream_t st);
+// Fused proposal backward from dz = dL/d(pre-softplus): field scatter and MLP weight
+// gradients (all accumulate).
+int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
+                    int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
+                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st);
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                     const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
                     cudaStream_t st);

@@ -92,6 +92,27 @@ struct EpiSoftplus {
   __device__ void operator()(int64_t m, int n, float v) const { out[m] = softplus_f(v + __ldg(bias) + shift); }
   __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const { vec4_scalar(*this, m, n, v, N); }
 };
+// C = v * (H > 0) with H stored feature-major: H[n * ldh + m].
+struct EpiReluMaskT {
+  float* C;
+  int ldc;
+  const float* H;
+  int64_t ldh;
+  __device__ void operator()(int64_t m, int n, float v) const {
+    C[m * ldc + n] = (__ldg(H + (int64_t)n * ldh + m) > 0.0f) ? v : 0.0f;
+  }
+  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
+    float* p = C + m * ldc + n;
+    if (vec_ok(p, n, N)) {
+      float o[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) o[j] = (__ldg(H + (int64_t)(n + j) * ldh + m) > 0.0f) ? v[j] : 0.0f;
+      *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+    } else {
+      vec4_scalar(*this, m, n, v, N);
+    }
+  }
+};
 struct EpiAtomic {
   float* C;
   int ldc;
@@ -239,15 +260,16 @@ __global__ void __launch_bounds__(256) pe_fwd_kernel(float* __restrict__ X1, int
 }
 
 // dH0[m][j] = dX1[m][j] + sum_f dX1[m][PE(j,f)] * d PE / d h (one thread per (m, j)).
+// h = X1[m][j] row-major (x1_fm = false) or X1[j][m] feature-major.
 __global__ void __launch_bounds__(256) pe_bwd_kernel(const float* __restrict__ dX1, int ld,
                                                     const float* __restrict__ X1, int64_t M, int sq, int nf,
-                                                    float* __restrict__ dH0) {
+                                                    float* __restrict__ dH0, bool x1_fm) {
   const int64_t m0 = (int64_t)blockIdx.x * PE_ROWS;
   const int nrows = (int)(M - m0 < PE_ROWS ? M - m0 : PE_ROWS);
   for (int e = threadIdx.x; e < nrows * sq; e += blockDim.x) {
     const int r = e / sq, j = e - r * sq;
     const int64_t m = m0 + r;
-    const float hv = __ldg(X1 + m * ld + j);
+    const float hv = x1_fm ? __ldg(X1 + (int64_t)j * M + m) : __ldg(X1 + m * ld + j);
     float g = __ldg(dX1 + m * ld + j);
     const float* pe = dX1 + m * ld + sq + 3 + j * 2 * nf;
     for (int f = 0; f < nf; ++f) {
@@ -285,6 +307,7 @@ static int ld_x1(const MlpDims& d) { return (int)round_up(d.enc, 4); }
 // Workspace carve-out shared by forward and backward (same order).
 struct MlpBufs {
   float *X1, *H1, *H2, *dH2, *dH1, *dX1, *dH0;
+  uint8_t* wpack;
 };
 static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   MlpBufs b;
@@ -295,6 +318,7 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   b.dH1 = ws.take<float>(M * d.units);
   b.dX1 = ws.take<float>(M * ld_x1(d));
   b.dH0 = ws.take<float>(M * d.squash);
+  b.wpack = ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes());
   return b;
 }
 
@@ -307,13 +331,17 @@ size_t mlp_workspace_bytes(const MlpDims& d, int64_t M) {
 
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st) {
-  (void)keep;
   MlpBufs b = carve(d, M, ws);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
     return TVM_ERR_WORKSPACE;
   }
   const int l1 = ld_x1(d);
+  if (mlp_fused_supported(d)) {
+    // BF16: all four layers in one tcgen05 kernel; X1 / H1 / H2 only when a backward follows.
+    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, keep ? b.X1 : nullptr, keep ? b.H1 : nullptr,
+                                keep ? b.H2 : nullptr, b.wpack, st);
+  }
   TVM_TRY((mm<false, false>(d.math, M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, l1}, st)));
   pe_fwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.X1, l1, M, d.squash, d.enc, d.nf, d.nv, dirs,
                                                                  rows_per_dir);
@@ -335,16 +363,27 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
   }
   const int l1 = ld_x1(d);
   const int64_t kc = -1;  // weight gradients: split-K over the rows, sized per GEMM
-  // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
-  TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
-  TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
-  // Layer 2.
-  TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
+  if (mlp_fused_supported(d)) {
+    // Activations stored feature-major by the fused forward: X1 [enc][M], H1/H2 [units][M].
+    TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMaskT{b.dH2, d.units, b.H2, M}, st)));
+    TVM_TRY((mm<false, false>(d.math, d.units, 3, M, b.H2, M, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+    TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
+                             EpiReluMaskT{b.dH1, d.units, b.H1, M}, st)));
+    TVM_TRY((mm<false, false>(d.math, d.units, d.units, M, b.H1, M, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
+    TVM_TRY((mm<false, true>(d.math, M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
+    TVM_TRY((mm<false, false>(d.math, d.enc, d.units, M, b.X1, M, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
+  } else {
+    // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
+    TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
+    TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+    // Layer 2.
+    TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
                              EpiReluMask{b.dH1, d.units, b.H1, d.units}, st)));
-  TVM_TRY((mm<true, false>(d.math, d.units, d.units, M, b.H1, d.units, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
-  // Layer 1.
-  TVM_TRY((mm<false, true>(d.math, M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
-  TVM_TRY((mm<true, false>(d.math, d.enc, d.units, M, b.X1, l1, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
+    TVM_TRY((mm<true, false>(d.math, d.units, d.units, M, b.H1, d.units, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
+    // Layer 1.
+    TVM_TRY((mm<false, true>(d.math, M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
+    TVM_TRY((mm<true, false>(d.math, d.enc, d.units, M, b.X1, l1, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
+  }
   // Bias gradients.
   {
     const int64_t cs = 128;  // rows per colsum block: M/128 blocks keep every SM busy
@@ -358,7 +397,8 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     TVM_TRY(check_launch("colsum"));
   }
   // Fourier encoding backward, then layer 0.
-  pe_bwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0);
+  pe_bwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0,
+                                                                 mlp_fused_supported(d));
   TVM_TRY(check_launch("pe_bwd"));
   TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, d.squash, EpiAtomic{g.w0, d.squash}, st, kc)));
   if (dX0) {
@@ -392,7 +432,9 @@ int device_status(int32_t* out, cudaStream_t st) {
     set_error("device_status: %s", cudaGetErrorString(e));
     return TVM_ERR_LAUNCH;
   }
-  *out = v;
+  int32_t f = 0;
+  TVM_TRY(fused_status(&f, st));
+  *out = v | f;
   return TVM_OK;
 }
 
@@ -416,29 +458,5 @@ int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const floa
 }  // namespace tvm
 
 namespace tvm {
-
-// Proposal MLP 16 -> units -> 1 (see tvm_proposal.cu): H = relu(X W1 + b1),
-// sigma = softplus(H W2 + b2 + shift).
-int prop_mlp_forward(int math, const float* X, int64_t M, int units, const float* w1, const float* b1,
-                     const float* w2, const float* b2, float shift, float* H, float* sigma, cudaStream_t st) {
-  TVM_TRY((mm<false, false>(math, M, units, 16, X, 16, w1, units, EpiBiasAct{H, units, b1, 1}, st)));
-  return mm<false, false>(math, M, 1, units, H, units, w2, 1, EpiSoftplus{sigma, b2, shift}, st);
-}
-
-// Backward from dz = dL/d(pre-softplus): weight gradients ACCUMULATE, dX overwritten.
-int prop_mlp_backward(int math, const float* X, int64_t M, int units, const float* w1, const float* w2,
-                      const float* H, const float* dz, float* dH, float* dX, float* gw1, float* gb1, float* gw2,
-                      float* gb2, cudaStream_t st) {
-  TVM_TRY((mm<false, true>(math, M, units, 1, dz, 1, w2, 1, EpiReluMask{dH, units, H, units}, st)));
-  TVM_TRY((mm<true, false>(math, units, 1, M, H, units, dz, 1, EpiAtomic{gw2, 1}, st, -1)));
-  TVM_TRY((mm<false, true>(math, M, 16, units, dH, units, w1, units, EpiStore{dX, 16}, st)));
-  TVM_TRY((mm<true, false>(math, 16, units, M, X, 16, dH, units, EpiAtomic{gw1, units}, st, -1)));
-  const int64_t cs = 128;
-  colsum_kernel<<<dim3(1, (unsigned)ceil_div(M, cs)), 32, 0, st>>>(dz, 1, M, 1, cs, gb2);
-  TVM_TRY(check_launch("colsum"));
-  colsum_kernel<<<dim3((unsigned)ceil_div(units, 128), (unsigned)ceil_div(M, cs)), 128, 0, st>>>(dH, units, M, units,
-                                                                                                  cs, gb1);
-  return check_launch("colsum");
-}
 
 }  // namespace tvm

@@ -84,12 +84,28 @@ __device__ __forceinline__ void prop_sample(const RayGeom& g, const SamplerArgs&
   sample_point(g, s, t, x);
 }
 
-// Features X[s] = [12 VM features (pair-major), x, y, z, |x|_inf] and bin length.
+// Features X[s] = [12 VM features (pair-major), x, y, z, |x|_inf], bin length, and
+// (with weights) the whole MLP in registers: h = relu(X W1 + b1), sigma = softplus(h W2
+// + b2 + shift). The weights sit in shared memory and every thread reads the same
+// element at the same time (broadcast). X and h are written only when the backward
+// needs them.
+constexpr int PROP_MAXU = 256;
+
 template <typename T>
-__global__ void prop_features_kernel(const T* __restrict__ lines, const T* __restrict__ planes, int G,
-                                     const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
-                                     SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter,
-                                     float* __restrict__ X, float* __restrict__ delta) {
+__global__ void __launch_bounds__(128) prop_features_kernel(
+    const T* __restrict__ lines, const T* __restrict__ planes, int G, const float* __restrict__ origins,
+    const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
+    const float* __restrict__ jitter, float* __restrict__ X, float* __restrict__ delta, int units,
+    const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
+    const float* __restrict__ b2, float shift, float* __restrict__ H, float* __restrict__ sigma) {
+  extern __shared__ float sw[];  // w1 [16][units], b1 [units], w2 [units]
+  const bool mlp = w1 != nullptr;
+  if (mlp) {
+    for (int e = threadIdx.x; e < 18 * units; e += blockDim.x) {
+      sw[e] = e < 16 * units ? __ldg(w1 + e) : (e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units));
+    }
+    __syncthreads();
+  }
   const int Np = s.N;
   const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (smp >= R * Np) return;
@@ -115,65 +131,154 @@ __global__ void prop_features_kernel(const T* __restrict__ lines, const T* __res
   out[13] = x[1];
   out[14] = x[2];
   out[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
-  float4* dst = reinterpret_cast<float4*>(X + smp * PROP_IN);
+  if (X) {
+    float4* dst = reinterpret_cast<float4*>(X + smp * PROP_IN);
 #pragma unroll
-  for (int q = 0; q < 4; ++q) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+    for (int q = 0; q < 4; ++q) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+  }
   delta[smp] = len;
+  if (mlp) {
+    const float* sw1 = sw;
+    const float* sb1 = sw + 16 * units;
+    const float* sw2 = sw + 17 * units;
+    float z = __ldg(b2);
+    for (int u = 0; u < units; ++u) {
+      float h = sb1[u];
+#pragma unroll
+      for (int i = 0; i < PROP_IN; ++i) h = fmaf(out[i], sw1[i * units + u], h);
+      h = fmaxf(h, 0.0f);
+      if (H) H[smp * units + u] = h;
+      z = fmaf(h, sw2[u], z);
+    }
+    sigma[smp] = softplus_f(z + shift);
+  }
 }
 
-// Scatter dL/dX[:, 0:12] into the proposal field gradients (FP32).
+// Fused proposal backward, one thread per sample, 128 samples per block: recompute the
+// features X (16) and hidden units h (U) in registers, dz -> dh = dz * w2 * [h > 0] ->
+// dX = dh W1^T -> scatter dX[0:12) into the proposal field gradients. The weight
+// gradients dW1 = sum_s X_s dh_s^T, db1 = sum dh, dW2 = sum h dz, db2 = sum dz are
+// reduced over the block in shared memory, then added to global memory with one atomic
+// per weight per block.
+constexpr int PBWD_THREADS = 128;
+
 template <typename T>
-__global__ void prop_vm_bwd_kernel(const T* __restrict__ lines, const T* __restrict__ planes, int G,
-                                   float* __restrict__ glines, float* __restrict__ gplanes,
-                                   const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
-                                   SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter,
-                                   const float* __restrict__ dX) {
+__global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
+    const T* __restrict__ lines, const T* __restrict__ planes, int G, float* __restrict__ glines,
+    float* __restrict__ gplanes, const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
+    SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter, const float* __restrict__ dz_in,
+    int units, const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
+    float* __restrict__ gw1, float* __restrict__ gb1, float* __restrict__ gw2, float* __restrict__ gb2) {
+  extern __shared__ float sm[];
+  float* sw1 = sm;                          // [16][U]
+  float* sb1 = sw1 + 16 * units;            // [U]
+  float* sw2 = sb1 + units;                 // [U]
+  float* sX = sw2 + units;                  // [128][17]
+  float* sdh = sX + PBWD_THREADS * 17;      // [128][U+1]
+  float* sh = sdh + PBWD_THREADS * (units + 1);  // [128][U+1]
+  float* sdz = sh + PBWD_THREADS * (units + 1);  // [128]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 18 * units; e += PBWD_THREADS)
+    sm[e] = e < 16 * units ? __ldg(w1 + e) : (e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units));
+  __syncthreads();
   const int Np = s.N;
-  const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (smp >= R * Np) return;
-  const float4* g4 = reinterpret_cast<const float4*>(dX + smp * PROP_IN);
-  float gf[12];
+  const int64_t smp = (int64_t)blockIdx.x * PBWD_THREADS + tid;
+  const bool valid = smp < R * Np;
+  float dz = valid ? __ldg(dz_in + smp) : 0.f;
+  float X[PROP_IN];
 #pragma unroll
-  for (int q = 0; q < 3; ++q) {
-    const float4 v = __ldg(g4 + q);
-    gf[4 * q] = v.x; gf[4 * q + 1] = v.y; gf[4 * q + 2] = v.z; gf[4 * q + 3] = v.w;
+  for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
+  PropPair e3[3];
+  if (valid) {
+    const int64_t r = smp / Np;
+    const int j = (int)(smp - r * Np);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, len, x[3];
+    prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
+    float u3[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u3[a] = grid_coord(x[a], G);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      int a, b, c;
+      mode_perm(m, a, b, c);
+      prop_pair<T>(lines, planes, G, m, u3[a], u3[b], u3[c], e3[m]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) X[m * 4 + q] = e3[m].L[q] * e3[m].P[q];
+    }
+    X[12] = x[0];
+    X[13] = x[1];
+    X[14] = x[2];
+    X[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
   }
+  // Recompute h, form dh and dX.
+  float dX[PROP_IN];
+#pragma unroll
+  for (int i = 0; i < PROP_IN; ++i) dX[i] = 0.f;
+  for (int u = 0; u < units; ++u) {
+    float h = sb1[u];
+#pragma unroll
+    for (int i = 0; i < PROP_IN; ++i) h = fmaf(X[i], sw1[i * units + u], h);
+    h = fmaxf(h, 0.f);
+    const float dh = (h > 0.f) ? dz * sw2[u] : 0.f;
+#pragma unroll
+    for (int i = 0; i < PROP_IN; ++i) dX[i] = fmaf(dh, sw1[i * units + u], dX[i]);
+    sdh[tid * (units + 1) + u] = dh;
+    sh[tid * (units + 1) + u] = h;
+  }
+#pragma unroll
+  for (int i = 0; i < PROP_IN; ++i) sX[tid * 17 + i] = X[i];
+  sdz[tid] = dz;
+  // Field gradient scatter.
   bool any = false;
 #pragma unroll
-  for (int q = 0; q < 12; ++q) any |= (gf[q] != 0.0f);
-  if (!any) return;
-  const int64_t r = smp / Np;
-  const int j = (int)(smp - r * Np);
-  RayGeom g = load_ray(origins, dirs, r, s);
-  float t, len, x[3];
-  prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
-  float u[3];
+  for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
+  if (valid && any) {
 #pragma unroll
-  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+    for (int m = 0; m < 3; ++m) {
+      const PropPair& e = e3[m];
+      float* lb = glines + (int64_t)m * G * PROP_C;
+      float* pb = gplanes + (int64_t)m * G * G * PROP_C;
+      float v[4];
 #pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    int a, b, c;
-    mode_perm(m, a, b, c);
-    PropPair e;
-    prop_pair<T>(lines, planes, G, m, u[a], u[b], u[c], e);
-    float* lb = glines + (int64_t)m * G * PROP_C;
-    float* pb = gplanes + (int64_t)m * G * G * PROP_C;
-    float v[4];
+      for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w0;
+      atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i0 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.P[q] * e.tl.w0;
-    atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i0 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+      for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w1;
+      atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i1 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+      const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
+      const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
+      const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.P[q] * e.tl.w1;
-    atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i1 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
-    const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
-    const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
-    const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
+      for (int k = 0; k < 4; ++k) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = gf[m * 4 + q] * e.L[q] * w[k];
-      atomicAdd(reinterpret_cast<float4*>(pb + ((int64_t)rows[k] * G + cols[k]) * PROP_C),
-                make_float4(v[0], v[1], v[2], v[3]));
+        for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.L[q] * w[k];
+        atomicAdd(reinterpret_cast<float4*>(pb + ((int64_t)rows[k] * G + cols[k]) * PROP_C),
+                  make_float4(v[0], v[1], v[2], v[3]));
+      }
+    }
+  }
+  __syncthreads();
+  // Block reduction of the weight gradients: thread t owns entries t, t+128, ... of
+  // [dW1 (16*U) | db1 (U) | dW2 (U) | db2 (1)].
+  const int total = 18 * units + 1;
+  for (int e = tid; e < total; e += PBWD_THREADS) {
+    float acc = 0.f;
+    if (e < 16 * units) {
+      const int i = e / units, u = e - i * units;
+      for (int q = 0; q < PBWD_THREADS; ++q) acc = fmaf(sX[q * 17 + i], sdh[q * (units + 1) + u], acc);
+      if (acc != 0.f) atomicAdd(gw1 + e, acc);
+    } else if (e < 17 * units) {
+      const int u = e - 16 * units;
+      for (int q = 0; q < PBWD_THREADS; ++q) acc += sdh[q * (units + 1) + u];
+      if (acc != 0.f) atomicAdd(gb1 + u, acc);
+    } else if (e < 18 * units) {
+      const int u = e - 17 * units;
+      for (int q = 0; q < PBWD_THREADS; ++q) acc = fmaf(sh[q * (units + 1) + u], sdz[q], acc);
+      if (acc != 0.f) atomicAdd(gw2 + u, acc);
+    } else {
+      for (int q = 0; q < PBWD_THREADS; ++q) acc += sdz[q];
+      if (acc != 0.f) atomicAdd(gb2, acc);
     }
   }
 }
@@ -294,33 +399,51 @@ __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* _
 
 // ---------------------------------------------------------------------------------
 int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
-                         const float* edges, const float* jitter, float* X, float* delta, cudaStream_t st) {
+                         const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
+                         cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
   const unsigned blocks = (unsigned)ceil_div(n, 128);
+  const int units = mlp ? mlp->units : 0;
+  const size_t smem = mlp ? (size_t)18 * units * sizeof(float) : 0;
+  const float *w1 = mlp ? mlp->w1 : nullptr, *b1 = mlp ? mlp->b1 : nullptr, *w2 = mlp ? mlp->w2 : nullptr,
+              *b2 = mlp ? mlp->b2 : nullptr;
+  float* H = mlp ? mlp->H : nullptr;
+  float* sig = mlp ? mlp->sigma : nullptr;
+  const float shift = mlp ? mlp->shift : 0.f;
   if (f.dtype == TVM_BF16)
-    prop_features_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>(
-        (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, origins, dirs, R, s, edges, jitter, X, delta);
+    prop_features_kernel<__nv_bfloat16><<<blocks, 128, smem, st>>>(
+        (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, origins, dirs, R, s, edges, jitter, X,
+        delta, units, w1, b1, w2, b2, shift, H, sig);
   else
-    prop_features_kernel<float><<<blocks, 128, 0, st>>>((const float*)f.lines, (const float*)f.planes, f.G, origins,
-                                                        dirs, R, s, edges, jitter, X, delta);
+    prop_features_kernel<float><<<blocks, 128, smem, st>>>((const float*)f.lines, (const float*)f.planes, f.G, origins,
+                                                           dirs, R, s, edges, jitter, X, delta, units, w1, b1, w2, b2,
+                                                           shift, H, sig);
   return check_launch("prop_features");
 }
 
-int launch_prop_vm_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
-                       int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dX,
-                       cudaStream_t st) {
+int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
+                    int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
+                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
-  const unsigned blocks = (unsigned)ceil_div(n, 128);
-  if (f.dtype == TVM_BF16)
-    prop_vm_bwd_kernel<__nv_bfloat16><<<blocks, 128, 0, st>>>((const __nv_bfloat16*)f.lines,
-                                                              (const __nv_bfloat16*)f.planes, f.G, glines, gplanes,
-                                                              origins, dirs, R, s, edges, jitter, dX);
-  else
-    prop_vm_bwd_kernel<float><<<blocks, 128, 0, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines,
-                                                      gplanes, origins, dirs, R, s, edges, jitter, dX);
-  return check_launch("prop_vm_bwd");
+  const int U = mlp.units;
+  const size_t smem = ((size_t)18 * U + PBWD_THREADS * 17 + 2 * PBWD_THREADS * (U + 1) + PBWD_THREADS) * sizeof(float);
+  const unsigned blocks = (unsigned)ceil_div(n, PBWD_THREADS);
+  if (f.dtype == TVM_BF16) {
+    auto fn = prop_bwd_kernel<__nv_bfloat16>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<blocks, PBWD_THREADS, smem, st>>>((const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines,
+                                           gplanes, origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2,
+                                           gw1, gb1, gw2, gb2);
+  } else {
+    auto fn = prop_bwd_kernel<float>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    fn<<<blocks, PBWD_THREADS, smem, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines, gplanes,
+                                           origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2, gw1, gb1,
+                                           gw2, gb2);
+  }
+  return check_launch("prop_bwd");
 }
 
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
