@@ -68,7 +68,8 @@ static int validate_model(const tvm_model_desc* m) {
     TVM_REQUIRE(m->proposal_grid >= 2 && m->proposal_grid <= 1024, TVM_ERR_SHAPE, "proposal_grid=%d outside [2, 1024]",
                 m->proposal_grid);
     TVM_REQUIRE(m->proposal_rank == 4, TVM_ERR_UNSUPPORTED, "proposal_rank must be 4");
-    TVM_REQUIRE(m->proposal_units >= 1 && m->proposal_units <= 128, TVM_ERR_SHAPE, "proposal_units outside [1, 128]");
+    TVM_REQUIRE(m->proposal_units >= 4 && m->proposal_units <= 128 && m->proposal_units % 4 == 0, TVM_ERR_SHAPE,
+                "proposal_units must be a multiple of 4 in [4, 128]");
   }
   return TVM_OK;
 }

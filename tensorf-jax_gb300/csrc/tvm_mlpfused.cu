@@ -169,58 +169,63 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
     }
     if (!layer(D0, OFF_A0, OFF_W0, F / 16, SBO_F, SBO_F, SQP)) { ok = 0; break; }
 
-    // Fourier encoding: row r = 32*sub + lane; warp half 0 writes chunks 0..9, half 1
-    // chunks 10..19 of X1 (each chunk = 8 encoded values).
+    // Fourier encoding (networks.py:13-35, 68-76), row r = 32*sub + lane. X1 columns:
+    // [h (27) | d (3) | PE(h): 4 per feature | PE(d): 4 per axis | zero pad to 160], PE(v)
+    // = [sin v, sin 2v, sin(v + pi/2), sin(2v + pi/2)] computed as [s, 2sc, c, c^2 - s^2]
+    // from one sincos. Warp half 0 encodes features 0..13, half 1 features 14..26, the
+    // direction and the padding. Each value is one 2-byte store at its canonical position.
     {
       const int r = sub * 32 + lane;
       const int64_t row = m0 + r;
-      float h[SQP];
-      {
-        float v[16];
-        tc::tmem_ld16(D0 + lane_off, v);
+      uint8_t* xrow = smem + OFF_A1 + (r >> 3) * SBO_E + (r & 7) * 16;
+      auto put = [&](int col, float v) {
+        *reinterpret_cast<__nv_bfloat16*>(xrow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
+        if (a.X1 && row < a.M) a.X1[(int64_t)col * a.M + row] = v;
+      };
+      auto pe4 = [&](int col, float v) {
+        float sn, cs;
+        __sincosf(v, &sn, &cs);
+        put(col, sn);
+        put(col + 1, 2.0f * sn * cs);
+        put(col + 2, cs);
+        put(col + 3, cs * cs - sn * sn);
+      };
+      float v16[16];
+      if (half == 0) {
+        tc::tmem_ld16(D0 + lane_off, v16);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) h[j] = v[j];
-        tc::tmem_ld16(D0 + lane_off + 16, v);
-#pragma unroll
-        for (int j = 0; j < 16; ++j) h[16 + j] = v[j];
-      }
-      float d[3] = {0.f, 0.f, 0.f};
-      if (row < a.M) {
-        const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
-        d[0] = __ldg(dp);
-        d[1] = __ldg(dp + 1);
-        d[2] = __ldg(dp + 2);
-      }
-      for (int kc = half * 10; kc < half * 10 + 10; ++kc) {
-        float v[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const int c = kc * 8 + e;
-          float x;
-          if (c < SQ) {
-            x = h[c];
-          } else if (c < SQ + 3) {
-            x = d[c - SQ];
-          } else if (c < SQ + 3 + SQ * 4) {
-            const int q = c - (SQ + 3), j = q >> 2, f = q & 3;
-            const float arg = h[j] * (float)(1 << (f & 1));
-            x = sinf(f < 2 ? arg : arg + kHalfPi);
-          } else if (c < ENC) {
-            const int q = c - (SQ + 3 + SQ * 4), j = q >> 2, f = q & 3;
-            const float arg = d[j] * (float)(1 << (f & 1));
-            x = sinf(f < 2 ? arg : arg + kHalfPi);
-          } else {
-            x = 0.f;
-          }
-          v[e] = x;
+        for (int j = 0; j < 14; ++j) {
+          put(j, v16[j]);
+          pe4(SQ + 3 + 4 * j, v16[j]);
         }
-        *reinterpret_cast<uint4*>(smem + OFF_A1 + coff(r, kc, SBO_E)) =
-            make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
-        if (a.X1 && row < a.M) {
+      } else {
+        tc::tmem_ld16(D0 + lane_off, v16);  // columns 0..15: 14 and 15 are this half's
+        const float h14 = v16[14], h15 = v16[15];
+        tc::tmem_ld16(D0 + lane_off + 16, v16);
+        put(14, h14);
+        pe4(SQ + 3 + 4 * 14, h14);
+        put(15, h15);
+        pe4(SQ + 3 + 4 * 15, h15);
 #pragma unroll
-          for (int e = 0; e < 8; ++e)
-            if (kc * 8 + e < ENC) a.X1[(int64_t)(kc * 8 + e) * a.M + row] = v[e];
+        for (int j = 16; j < SQ; ++j) {
+          put(j, v16[j - 16]);
+          pe4(SQ + 3 + 4 * j, v16[j - 16]);
         }
+        float d[3] = {0.f, 0.f, 0.f};
+        if (row < a.M) {
+          const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
+          d[0] = __ldg(dp);
+          d[1] = __ldg(dp + 1);
+          d[2] = __ldg(dp + 2);
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          put(SQ + q, d[q]);
+          pe4(SQ + 3 + 4 * SQ + 4 * q, d[q]);
+        }
+#pragma unroll
+        for (int c = ENC; c < ENCP; ++c)
+          *reinterpret_cast<__nv_bfloat16*>(xrow + (c >> 3) * 128 + (c & 7) * 2) = __float2bfloat16_rn(0.f);
       }
     }
     if (!layer(D1, OFF_A1, OFF_W1, ENCP / 16, SBO_E, SBO_E, U)) { ok = 0; break; }

@@ -98,11 +98,18 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
     const float* __restrict__ jitter, float* __restrict__ X, float* __restrict__ delta, int units,
     const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
     const float* __restrict__ b2, float shift, float* __restrict__ H, float* __restrict__ sigma) {
-  extern __shared__ float sw[];  // w1 [16][units], b1 [units], w2 [units]
+  extern __shared__ __align__(16) float sw[];  // w1 transposed [units][16], b1 [units], w2 [units]
   const bool mlp = w1 != nullptr;
   if (mlp) {
     for (int e = threadIdx.x; e < 18 * units; e += blockDim.x) {
-      sw[e] = e < 16 * units ? __ldg(w1 + e) : (e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units));
+      float v;
+      if (e < 16 * units) {
+        const int u = e / 16, i = e % 16;
+        v = __ldg(w1 + i * units + u);
+      } else {
+        v = e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units);
+      }
+      sw[e] = v;
     }
     __syncthreads();
   }
@@ -138,14 +145,20 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
   }
   delta[smp] = len;
   if (mlp) {
-    const float* sw1 = sw;
+    const float4* sw1 = reinterpret_cast<const float4*>(sw);  // row u: 16 weights
     const float* sb1 = sw + 16 * units;
     const float* sw2 = sw + 17 * units;
     float z = __ldg(b2);
     for (int u = 0; u < units; ++u) {
       float h = sb1[u];
 #pragma unroll
-      for (int i = 0; i < PROP_IN; ++i) h = fmaf(out[i], sw1[i * units + u], h);
+      for (int q = 0; q < 4; ++q) {
+        const float4 w = sw1[u * 4 + q];
+        h = fmaf(out[4 * q], w.x, h);
+        h = fmaf(out[4 * q + 1], w.y, h);
+        h = fmaf(out[4 * q + 2], w.z, h);
+        h = fmaf(out[4 * q + 3], w.w, h);
+      }
       h = fmaxf(h, 0.0f);
       if (H) H[smp * units + u] = h;
       z = fmaf(h, sw2[u], z);
@@ -169,17 +182,26 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
     SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter, const float* __restrict__ dz_in,
     int units, const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
     float* __restrict__ gw1, float* __restrict__ gb1, float* __restrict__ gw2, float* __restrict__ gb2) {
-  extern __shared__ float sm[];
-  float* sw1 = sm;                          // [16][U]
+  extern __shared__ __align__(16) float sm[];
+  float* sw1 = sm;                          // transposed [U][16]
   float* sb1 = sw1 + 16 * units;            // [U]
   float* sw2 = sb1 + units;                 // [U]
-  float* sX = sw2 + units;                  // [128][17]
-  float* sdh = sX + PBWD_THREADS * 17;      // [128][U+1]
-  float* sh = sdh + PBWD_THREADS * (units + 1);  // [128][U+1]
-  float* sdz = sh + PBWD_THREADS * (units + 1);  // [128]
+  const int ld = units + 4;                 // row pitch: float4-aligned, 4-way store conflicts at most
+  float* sX = sw2 + units;                  // [128][16]
+  float* sdh = sX + PBWD_THREADS * 16;      // [128][U+4]
+  float* sh = sdh + PBWD_THREADS * ld;      // [128][U+4]
+  float* sdz = sh + PBWD_THREADS * ld;      // [128]
   const int tid = threadIdx.x;
-  for (int e = tid; e < 18 * units; e += PBWD_THREADS)
-    sm[e] = e < 16 * units ? __ldg(w1 + e) : (e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units));
+  for (int e = tid; e < 18 * units; e += PBWD_THREADS) {
+    float v;
+    if (e < 16 * units) {
+      const int u = e / 16, i = e % 16;
+      v = __ldg(w1 + i * units + u);
+    } else {
+      v = e < 17 * units ? __ldg(b1 + e - 16 * units) : __ldg(w2 + e - 17 * units);
+    }
+    sm[e] = v;
+  }
   __syncthreads();
   const int Np = s.N;
   const int64_t smp = (int64_t)blockIdx.x * PBWD_THREADS + tid;
@@ -215,19 +237,33 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
   float dX[PROP_IN];
 #pragma unroll
   for (int i = 0; i < PROP_IN; ++i) dX[i] = 0.f;
+  const float4* sw1v = reinterpret_cast<const float4*>(sw1);
   for (int u = 0; u < units; ++u) {
+    float4 w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = sw1v[u * 4 + q];
     float h = sb1[u];
 #pragma unroll
-    for (int i = 0; i < PROP_IN; ++i) h = fmaf(X[i], sw1[i * units + u], h);
+    for (int q = 0; q < 4; ++q) {
+      h = fmaf(X[4 * q], w[q].x, h);
+      h = fmaf(X[4 * q + 1], w[q].y, h);
+      h = fmaf(X[4 * q + 2], w[q].z, h);
+      h = fmaf(X[4 * q + 3], w[q].w, h);
+    }
     h = fmaxf(h, 0.f);
     const float dh = (h > 0.f) ? dz * sw2[u] : 0.f;
 #pragma unroll
-    for (int i = 0; i < PROP_IN; ++i) dX[i] = fmaf(dh, sw1[i * units + u], dX[i]);
-    sdh[tid * (units + 1) + u] = dh;
-    sh[tid * (units + 1) + u] = h;
+    for (int q = 0; q < 4; ++q) {
+      dX[4 * q] = fmaf(dh, w[q].x, dX[4 * q]);
+      dX[4 * q + 1] = fmaf(dh, w[q].y, dX[4 * q + 1]);
+      dX[4 * q + 2] = fmaf(dh, w[q].z, dX[4 * q + 2]);
+      dX[4 * q + 3] = fmaf(dh, w[q].w, dX[4 * q + 3]);
+    }
+    sdh[tid * ld + u] = dh;
+    sh[tid * ld + u] = h;
   }
 #pragma unroll
-  for (int i = 0; i < PROP_IN; ++i) sX[tid * 17 + i] = X[i];
+  for (int i = 0; i < PROP_IN; ++i) sX[tid * 16 + i] = X[i];
   sdz[tid] = dz;
   // Field gradient scatter.
   bool any = false;
@@ -259,23 +295,41 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
     }
   }
   __syncthreads();
-  // Block reduction of the weight gradients: thread t owns entries t, t+128, ... of
-  // [dW1 (16*U) | db1 (U) | dW2 (U) | db2 (1)].
-  const int total = 18 * units + 1;
-  for (int e = tid; e < total; e += PBWD_THREADS) {
+  // Block reduction of the weight gradients. dW1 (16 x U): thread t owns feature
+  // i = t % 16 and units [8*(t/16), +8) (+ 64 per extra pass when U > 64), 8 FMAs per
+  // sample from one X load and two 16-byte dh loads. Then dW2, db1 and db2.
+  for (int u0 = (tid / 16) * 8; u0 < units; u0 += (PBWD_THREADS / 16) * 8) {
+    const int i = tid % 16;
+    float acc[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) acc[e] = 0.f;
+    if (u0 + 8 <= units) {
+      for (int q = 0; q < PBWD_THREADS; ++q) {
+        const float xv = sX[q * 16 + i];
+        const float4 d0 = *reinterpret_cast<const float4*>(sdh + q * ld + u0);
+        const float4 d1 = *reinterpret_cast<const float4*>(sdh + q * ld + u0 + 4);
+        acc[0] = fmaf(xv, d0.x, acc[0]); acc[1] = fmaf(xv, d0.y, acc[1]);
+        acc[2] = fmaf(xv, d0.z, acc[2]); acc[3] = fmaf(xv, d0.w, acc[3]);
+        acc[4] = fmaf(xv, d1.x, acc[4]); acc[5] = fmaf(xv, d1.y, acc[5]);
+        acc[6] = fmaf(xv, d1.z, acc[6]); acc[7] = fmaf(xv, d1.w, acc[7]);
+      }
+    } else {
+      for (int q = 0; q < PBWD_THREADS; ++q) {
+        const float xv = sX[q * 16 + i];
+        for (int e = 0; e < 8 && u0 + e < units; ++e) acc[e] = fmaf(xv, sdh[q * ld + u0 + e], acc[e]);
+      }
+    }
+    for (int e = 0; e < 8 && u0 + e < units; ++e)
+      if (acc[e] != 0.f) atomicAdd(gw1 + i * units + u0 + e, acc[e]);
+  }
+  for (int e = tid; e < 2 * units + 1; e += PBWD_THREADS) {
     float acc = 0.f;
-    if (e < 16 * units) {
-      const int i = e / units, u = e - i * units;
-      for (int q = 0; q < PBWD_THREADS; ++q) acc = fmaf(sX[q * 17 + i], sdh[q * (units + 1) + u], acc);
-      if (acc != 0.f) atomicAdd(gw1 + e, acc);
-    } else if (e < 17 * units) {
-      const int u = e - 16 * units;
-      for (int q = 0; q < PBWD_THREADS; ++q) acc += sdh[q * (units + 1) + u];
-      if (acc != 0.f) atomicAdd(gb1 + u, acc);
-    } else if (e < 18 * units) {
-      const int u = e - 17 * units;
-      for (int q = 0; q < PBWD_THREADS; ++q) acc = fmaf(sh[q * (units + 1) + u], sdz[q], acc);
-      if (acc != 0.f) atomicAdd(gw2 + u, acc);
+    if (e < units) {
+      for (int q = 0; q < PBWD_THREADS; ++q) acc = fmaf(sh[q * ld + e], sdz[q], acc);
+      if (acc != 0.f) atomicAdd(gw2 + e, acc);
+    } else if (e < 2 * units) {
+      for (int q = 0; q < PBWD_THREADS; ++q) acc += sdh[q * ld + e - units];
+      if (acc != 0.f) atomicAdd(gb1 + e - units, acc);
     } else {
       for (int q = 0; q < PBWD_THREADS; ++q) acc += sdz[q];
       if (acc != 0.f) atomicAdd(gb2, acc);
@@ -428,7 +482,7 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
   const int U = mlp.units;
-  const size_t smem = ((size_t)18 * U + PBWD_THREADS * 17 + 2 * PBWD_THREADS * (U + 1) + PBWD_THREADS) * sizeof(float);
+  const size_t smem = ((size_t)18 * U + PBWD_THREADS * 16 + 2 * PBWD_THREADS * (U + 4) + PBWD_THREADS) * sizeof(float);
   const unsigned blocks = (unsigned)ceil_div(n, PBWD_THREADS);
   if (f.dtype == TVM_BF16) {
     auto fn = prop_bwd_kernel<__nv_bfloat16>;
