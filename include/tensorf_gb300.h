@@ -249,6 +249,36 @@ TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const f
                 const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
                 void* grads, void* workspace, size_t workspace_bytes, void* stream);
 
+/* FeatureMlp forward without a caller workspace. This function has no counterpart in
+ * the reference. It computes the same rgb as tvm_mlp_fwd, with the same kernels, but
+ * it allocates nothing and takes no workspace. Its scratch is one static device array
+ * of TVM_MLP_STATIC_SCRATCH_BYTES inside the library, shared by every call on a
+ * device.
+ *
+ * It is for callers that can neither allocate nor pass scratch:
+ *   - a handler run by another framework's executor, such as an XLA FFI custom call.
+ *     XLA reserves most of device memory up front, and a handler only receives the
+ *     buffers its call declares.
+ *   - code that must not stall other streams, because cudaFree synchronises the
+ *     device.
+ *
+ * Limit: n is at most the number of rows whose tvm_mlp_fwd workspace fits the array.
+ * That is 9,924 rows for the default model (144 features, 27 squash, 2/2
+ * frequencies, 128 units). Larger n returns TVM_ERR_SHAPE before any launch, and the
+ * message gives the maximum for the model.
+ *
+ * Set-up: the first call with a device current looks up the array's device address
+ * for that device. That lookup may load the library's module and reserve the array.
+ * Make that first call before any stream capture.
+ *
+ * Calls whose GPU work overlaps race on the shared array: different streams, or
+ * different threads, with no ordering between them. Order them on one stream or with
+ * events. Nothing in the array has to start at zero. */
+#define TVM_MLP_STATIC_SCRATCH_BYTES (32u << 20)
+TVM_API int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params,
+                                       const float* features, const float* viewdirs, int64_t n,
+                                       float* rgb, void* stream);
+
 /* Plain GEMM on the tensor-core path used by the MLP (exposed for testing):
  * D[M x N] (+)= A(m,k) * B(k,n), A(m,k) = a_trans ? A[k*lda + m] : A[m*lda + k],
  * B(k,n) = b_trans ? B[n*ldb + k] : B[k*ldb + n]; all float32 in memory. math: 0 =

@@ -4,6 +4,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "tvm_internal.h"
 
@@ -662,6 +663,98 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
   TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
   phase_mark(12, as_stream(stream));
   return TVM_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// FeatureMlp forward on library-owned scratch (tvm_mlp_fwd_static_scratch).
+//
+// Some callers cannot hand this library a workspace or let it allocate one:
+//   - a handler run by another framework's executor, e.g. an XLA FFI custom call:
+//     XLA's allocator reserves most of device memory up front (so a cudaMalloc of
+//     our own can fail), and a handler only receives the buffers its call declares;
+//   - code that must not stall other streams: cudaFree synchronises the device.
+// For them the MLP forward's scratch (activation buffers X1/H1/H2 and the packed
+// bf16 weights, laid out exactly as for tvm_mlp_fwd) lives in one static device
+// array owned by this file.
+//
+// The array holds TVM_MLP_STATIC_SCRATCH_BYTES (32 MiB). Its device address is
+// looked up once per device, by the first call made with that device current
+// (cudaGetSymbolAddress, which may load this module and so reserve the array); that
+// first call should come before any stream capture. Later calls only launch kernels.
+//
+// Every call on a device shares the one array, so calls whose GPU work overlaps
+// (different streams, or different host threads, without an ordering between them)
+// race on it and give wrong results; order them on one stream or with events.
+// Nothing in the array has to start at zero: each call writes every scratch byte it
+// reads before reading it, so the array is never cleared.
+// ---------------------------------------------------------------------------------
+namespace tvm {
+
+constexpr size_t kMlpStaticScratchBytes = size_t(32) << 20;
+constexpr int kMaxStaticScratchDevices = 64;
+
+static __device__ __align__(256) unsigned char g_mlp_static_scratch[kMlpStaticScratchBytes];
+
+static std::mutex g_static_scratch_mu;
+static void* g_static_scratch_ptr[kMaxStaticScratchDevices] = {};
+
+// Device address of g_mlp_static_scratch for the current device (set-up on first use).
+static int static_scratch_address(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "cudaGetDevice: %s", cudaGetErrorString(e));
+  TVM_REQUIRE(dev >= 0 && dev < kMaxStaticScratchDevices, TVM_ERR_UNSUPPORTED,
+              "device %d: static scratch supports devices 0..%d", dev, kMaxStaticScratchDevices - 1);
+  std::lock_guard<std::mutex> lock(g_static_scratch_mu);
+  if (g_static_scratch_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_mlp_static_scratch);
+    TVM_REQUIRE(e == cudaSuccess && p != nullptr, TVM_ERR_LAUNCH, "cudaGetSymbolAddress(static scratch): %s",
+                cudaGetErrorString(e));
+    g_static_scratch_ptr[dev] = p;
+  }
+  *out = g_static_scratch_ptr[dev];
+  return TVM_OK;
+}
+
+// Largest row count whose forward scratch fits the static array (monotone in n).
+static int64_t static_scratch_max_rows(const MlpDims& d) {
+  int64_t lo = 0, hi = int64_t(1) << 32;
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo + 1) / 2;
+    if (mlp_workspace_bytes(d, mid) <= kMlpStaticScratchBytes) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+}  // namespace tvm
+
+extern "C" {
+
+int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params, const float* features,
+                               const float* viewdirs, int64_t n, float* rgb, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  const MlpDims d = mlp_dims(*model);
+  const size_t need = mlp_workspace_bytes(d, n);
+  TVM_REQUIRE(need <= kMlpStaticScratchBytes, TVM_ERR_SHAPE,
+              "n=%lld rows need %zu bytes of MLP scratch; the static scratch holds %zu bytes, "
+              "at most %lld rows for this model",
+              (long long)n, need, kMlpStaticScratchBytes, (long long)static_scratch_max_rows(d));
+  if (n == 0) return TVM_OK;
+  TVM_REQUIRE(params && features && viewdirs && rgb, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(params, 16) && aligned(features, 16), TVM_ERR_ALIGN,
+              "params and features must be 16-byte aligned");
+  void* scratch = nullptr;
+  TVM_TRY(static_scratch_address(&scratch));
+  tvm_param_layout L;
+  make_layout(*model, L);
+  Workspace ws{static_cast<char*>(scratch), kMlpStaticScratchBytes, 0, false};
+  return mlp_forward(d, mlp_weights(L, static_cast<const float*>(params)), features, viewdirs, 1, n, rgb, ws,
+                     false, as_stream(stream));
 }
 
 }  // extern "C"

@@ -92,6 +92,8 @@ _SIGNATURES = {
                               c_size_t, c_void_p]),
     "tvm_mlp_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                               c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tvm_mlp_fwd_static_scratch": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                                            c_void_p]),
     "tvm_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int64, c_int32, c_int64, c_void_p, c_int64, c_void_p,
                            c_int64, c_void_p, c_int64, c_int32, c_void_p]),
     "tvm_device_status": (c_int32, [POINTER(c_int32), c_void_p]),
