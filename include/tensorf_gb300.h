@@ -9,9 +9,11 @@
  *     a negative TVM_ERR_* code before launching anything when they are wrong, with
  *     a message readable through tvm_last_error_message() (per calling thread);
  *   - allocates nothing: scratch comes from a caller buffer sized by the matching
- *     *_workspace_size() call;
- *   - keeps no global mutable state besides the per-thread error message, so calls
- *     on distinct streams from distinct threads are independent.
+ *     *_workspace_size() call (tvm_mlp_fwd_static_scratch instead uses a static array
+ *     inside the library);
+ *   - keeps no global mutable state besides the per-thread error message, the device
+ *     status words and that static array, so calls on distinct streams from distinct
+ *     threads are independent, except overlapping tvm_mlp_fwd_static_scratch calls.
  *
  * Layouts (device memory). Field tensors are CHANNEL-LAST:
  *   lines  [3][G][C]     element (m, x, c)        at (m*G + x)*C + c
