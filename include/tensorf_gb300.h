@@ -265,9 +265,11 @@ TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const f
  *     device.
  *
  * Limit: n is at most the number of rows whose tvm_mlp_fwd workspace fits the array.
- * That is 9,924 rows for the default model (144 features, 27 squash, 2/2
- * frequencies, 128 units). Larger n returns TVM_ERR_SHAPE before any launch, and the
- * message gives the maximum for the model.
+ * For the default TVM_F32 model (144 features, 27 squash, 2/2 frequencies, 128
+ * units) that is 9,950 rows. A TVM_BF16 model with those dimensions runs the fused
+ * kernel: it needs only the 87,040-byte packed weights, so n is not limited. Larger n
+ * returns TVM_ERR_SHAPE before any launch, and the message gives the maximum for the
+ * model.
  *
  * Set-up: the first call with a device current looks up the array's device address
  * for that device. That lookup may load the library's module and reserve the array.

@@ -353,7 +353,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
-  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, backward, st));
+  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, st));
   phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
@@ -365,7 +365,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
                             b.gP, st));
   phase_mark(6, st);
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
-  TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, R * k, b.dZ3, b.dX0, ws2, st));
+  TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, k, R * k, b.dZ3, b.dX0, ws2, st));
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
@@ -525,7 +525,7 @@ int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* fe
   make_layout(*model, L);
   Workspace ws{static_cast<char*>(workspace), workspace_bytes, 0, false};
   return mlp_forward(mlp_dims(*model), mlp_weights(L, static_cast<const float*>(params)), features,
-                     viewdirs, 1, n, rgb, ws, false, as_stream(stream));
+                     viewdirs, 1, n, rgb, ws, as_stream(stream));
 }
 
 int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
@@ -547,10 +547,10 @@ int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* fe
   float* dz = ws.take<float>(n * 3);
   const size_t off = ws.used;
   TVM_REQUIRE(ws.ok(), TVM_ERR_WORKSPACE, "workspace too small");
-  TVM_TRY(mlp_forward(d, w, features, viewdirs, 1, n, rgb, ws, true, st));
+  TVM_TRY(mlp_forward(d, w, features, viewdirs, 1, n, rgb, ws, st));
   TVM_TRY(launch_sigmoid_bwd(rgb, grad_rgb, n, dz, st));
   Workspace ws2{static_cast<char*>(workspace), workspace_bytes, off, false};
-  return mlp_backward(d, w, mlp_grads(L, static_cast<float*>(grads)), features, n, dz, grad_features,
+  return mlp_backward(d, w, mlp_grads(L, static_cast<float*>(grads)), features, viewdirs, 1, n, dz, grad_features,
                       ws2, st);
 }
 
@@ -675,9 +675,9 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
 //     XLA's allocator reserves most of device memory up front (so a cudaMalloc of
 //     our own can fail), and a handler only receives the buffers its call declares;
 //   - code that must not stall other streams: cudaFree synchronises the device.
-// For them the MLP forward's scratch (activation buffers X1/H1/H2 and the packed
-// bf16 weights, laid out exactly as for tvm_mlp_fwd) lives in one static device
-// array owned by this file.
+// For them the MLP forward's scratch (the layered path's activation buffers, or the
+// fused path's packed bf16 weights, laid out exactly as for tvm_mlp_fwd) lives in one
+// static device array owned by this file.
 //
 // The array holds TVM_MLP_STATIC_SCRATCH_BYTES (32 MiB). Its device address is
 // looked up once per device, by the first call made with that device current
@@ -754,7 +754,7 @@ int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params, 
   make_layout(*model, L);
   Workspace ws{static_cast<char*>(scratch), kMlpStaticScratchBytes, 0, false};
   return mlp_forward(d, mlp_weights(L, static_cast<const float*>(params)), features, viewdirs, 1, n, rgb, ws,
-                     false, as_stream(stream));
+                     as_stream(stream));
 }
 
 }  // extern "C"

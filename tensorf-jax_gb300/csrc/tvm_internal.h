@@ -79,22 +79,28 @@ struct MlpGrads {
 size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);
 // rgb = FeatureMlp(X0, viewdir). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...].
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
-                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st);
-// Needs the buffers kept by the preceding mlp_forward on the same workspace (stored
-// feature-major when mlp_fused_supported(d), row-major otherwise).
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st);
+// Needs the preceding mlp_forward on the same workspace: its kept row-major activations
+// (layered path), or its packed bf16 weights (fused path, which recomputes the forward
+// from X0 and the view directions).
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
-int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0,
-                 int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
+int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
+                 int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
 int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
 int fused_status(int32_t* out, cudaStream_t st);   // same for the fused MLP kernel
 bool mlp_fused_supported(const MlpDims& d);
-// Writes X1 [enc][M], H1 [units][M], H2 [units][M] feature-major when non-null.
 // wpack: mlp_fused_pack_bytes() of scratch (16-byte aligned) for the packed weights.
 size_t mlp_fused_pack_bytes();
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, float* X1, float* H1, float* H2, uint8_t* wpack, cudaStream_t st);
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st);
+// Fused BF16 backward: recomputes the forward per tile, accumulates all weight and
+// bias gradients into g, writes dX0 (M, 144) when non-null. wpack: the images packed by
+// launch_mlp_fwd_fused.
+int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
+                         int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
+                         cudaStream_t st);
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
 

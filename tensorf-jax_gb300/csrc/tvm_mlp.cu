@@ -92,27 +92,6 @@ struct EpiSoftplus {
   __device__ void operator()(int64_t m, int n, float v) const { out[m] = softplus_f(v + __ldg(bias) + shift); }
   __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const { vec4_scalar(*this, m, n, v, N); }
 };
-// C = v * (H > 0) with H stored feature-major: H[n * ldh + m].
-struct EpiReluMaskT {
-  float* C;
-  int ldc;
-  const float* H;
-  int64_t ldh;
-  __device__ void operator()(int64_t m, int n, float v) const {
-    C[m * ldc + n] = (__ldg(H + (int64_t)n * ldh + m) > 0.0f) ? v : 0.0f;
-  }
-  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const {
-    float* p = C + m * ldc + n;
-    if (vec_ok(p, n, N)) {
-      float o[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) o[j] = (__ldg(H + (int64_t)(n + j) * ldh + m) > 0.0f) ? v[j] : 0.0f;
-      *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
-    } else {
-      vec4_scalar(*this, m, n, v, N);
-    }
-  }
-};
 struct EpiAtomic {
   float* C;
   int ldc;
@@ -259,17 +238,17 @@ __global__ void __launch_bounds__(256) pe_fwd_kernel(float* __restrict__ X1, int
   }
 }
 
-// dH0[m][j] = dX1[m][j] + sum_f dX1[m][PE(j,f)] * d PE / d h (one thread per (m, j)).
-// h = X1[m][j] row-major (x1_fm = false) or X1[j][m] feature-major.
+// dH0[m][j] = dX1[m][j] + sum_f dX1[m][PE(j,f)] * d PE / d h (one thread per (m, j)),
+// h = X1[m][j].
 __global__ void __launch_bounds__(256) pe_bwd_kernel(const float* __restrict__ dX1, int ld,
                                                     const float* __restrict__ X1, int64_t M, int sq, int nf,
-                                                    float* __restrict__ dH0, bool x1_fm) {
+                                                    float* __restrict__ dH0) {
   const int64_t m0 = (int64_t)blockIdx.x * PE_ROWS;
   const int nrows = (int)(M - m0 < PE_ROWS ? M - m0 : PE_ROWS);
   for (int e = threadIdx.x; e < nrows * sq; e += blockDim.x) {
     const int r = e / sq, j = e - r * sq;
     const int64_t m = m0 + r;
-    const float hv = x1_fm ? __ldg(X1 + (int64_t)j * M + m) : __ldg(X1 + m * ld + j);
+    const float hv = __ldg(X1 + m * ld + j);
     float g = __ldg(dX1 + m * ld + j);
     const float* pe = dX1 + m * ld + sq + 3 + j * 2 * nf;
     for (int f = 0; f < nf; ++f) {
@@ -310,7 +289,11 @@ struct MlpBufs {
   uint8_t* wpack;
 };
 static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
-  MlpBufs b;
+  MlpBufs b{};
+  if (mlp_fused_supported(d)) {  // the fused kernels keep every activation on chip
+    b.wpack = ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes());
+    return b;
+  }
   b.X1 = ws.take<float>(M * ld_x1(d));
   b.H1 = ws.take<float>(M * d.units);
   b.H2 = ws.take<float>(M * d.units);
@@ -318,7 +301,6 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   b.dH1 = ws.take<float>(M * d.units);
   b.dX1 = ws.take<float>(M * ld_x1(d));
   b.dH0 = ws.take<float>(M * d.squash);
-  b.wpack = ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes());
   return b;
 }
 
@@ -330,7 +312,7 @@ size_t mlp_workspace_bytes(const MlpDims& d, int64_t M) {
 
 
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
-                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, bool keep, cudaStream_t st) {
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st) {
   MlpBufs b = carve(d, M, ws);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
@@ -338,9 +320,9 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
   }
   const int l1 = ld_x1(d);
   if (mlp_fused_supported(d)) {
-    // BF16: all four layers in one tcgen05 kernel; X1 / H1 / H2 only when a backward follows.
-    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, keep ? b.X1 : nullptr, keep ? b.H1 : nullptr,
-                                keep ? b.H2 : nullptr, b.wpack, st);
+    // BF16: all four layers in one tcgen05 kernel. Nothing is kept for the backward,
+    // which recomputes the activations from X0 (only the packed weights are reused).
+    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st);
   }
   TVM_TRY((mm<false, false>(d.math, M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, l1}, st)));
   pe_fwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.X1, l1, M, d.squash, d.enc, d.nf, d.nv, dirs,
@@ -354,25 +336,19 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
   return TVM_OK;
 }
 
-int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0,
-                 int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st) {
+int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
+                 int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st) {
   MlpBufs b = carve(d, M, ws);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
     return TVM_ERR_WORKSPACE;
   }
+  if (mlp_fused_supported(d)) {
+    return launch_mlp_bwd_fused(w, g, X0, dirs, rows_per_dir, M, dZ3, dX0, b.wpack, st);
+  }
   const int l1 = ld_x1(d);
   const int64_t kc = -1;  // weight gradients: split-K over the rows, sized per GEMM
-  if (mlp_fused_supported(d)) {
-    // Activations stored feature-major by the fused forward: X1 [enc][M], H1/H2 [units][M].
-    TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMaskT{b.dH2, d.units, b.H2, M}, st)));
-    TVM_TRY((mm<false, false>(d.math, d.units, 3, M, b.H2, M, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
-    TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
-                             EpiReluMaskT{b.dH1, d.units, b.H1, M}, st)));
-    TVM_TRY((mm<false, false>(d.math, d.units, d.units, M, b.H1, M, b.dH2, d.units, EpiAtomic{g.w2, d.units}, st, kc)));
-    TVM_TRY((mm<false, true>(d.math, M, d.enc, d.units, b.dH1, d.units, w.w1, d.units, EpiStore{b.dX1, l1}, st)));
-    TVM_TRY((mm<false, false>(d.math, d.enc, d.units, M, b.X1, M, b.dH1, d.units, EpiAtomic{g.w1, d.units}, st, kc)));
-  } else {
+  {
     // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
     TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
     TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
@@ -397,8 +373,7 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     TVM_TRY(check_launch("colsum"));
   }
   // Fourier encoding backward, then layer 0.
-  pe_bwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0,
-                                                                 mlp_fused_supported(d));
+  pe_bwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.dX1, l1, b.X1, M, d.squash, d.nf, b.dH0);
   TVM_TRY(check_launch("pe_bwd"));
   TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, d.squash, EpiAtomic{g.w0, d.squash}, st, kc)));
   if (dX0) {

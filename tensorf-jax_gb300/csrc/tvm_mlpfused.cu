@@ -9,8 +9,7 @@
 //   MMA L1 (N=128, K=160) -> D1 -> +b1, ReLU -> bf16 H1 tile (reuses the X0 tile)
 //   MMA L2 (N=128, K=128) -> D2 -> +b2, ReLU -> bf16 H2 tile (reuses the X1 tile)
 //   MMA L3 (N=16,  K=128) -> D3 -> +b3, sigmoid -> rgb (global)
-// Activations never leave the SM, except X1 / H1 / H2 in fp32 when a backward follows
-// (the layered backward reads them). One elected thread issues the MMAs and commits to an
+// Activations never leave the SM (the fused backward recomputes them). One elected thread issues the MMAs and commits to an
 // mbarrier; every wait is bounded and reports through the device status word.
 #include "tvm_internal.h"
 #include "tvm_tc.cuh"
@@ -100,9 +99,6 @@ struct Args {
   int rows_per_dir;
   const float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
   float* rgb;          // (M, 3)
-  float* X1;           // optional feature-major fp32 copies for the backward:
-  float* H1;           // X1 [ENC][M], H1 [U][M], H2 [U][M] (a warp's lanes hold
-  float* H2;           // consecutive rows, so each store is one 128-byte line)
 };
 
 __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
@@ -180,7 +176,6 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
       uint8_t* xrow = smem + OFF_A1 + (r >> 3) * SBO_E + (r & 7) * 16;
       auto put = [&](int col, float v) {
         *reinterpret_cast<__nv_bfloat16*>(xrow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
-        if (a.X1 && row < a.M) a.X1[(int64_t)col * a.M + row] = v;
       };
       auto pe4 = [&](int col, float v) {
         float sn, cs;
@@ -230,10 +225,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
     }
     if (!layer(D1, OFF_A1, OFF_W1, ENCP / 16, SBO_E, SBO_E, U)) { ok = 0; break; }
 
-    // Hidden layers: +bias, ReLU, bf16 into the next A tile (and fp32 to global).
-    auto hidden = [&](uint32_t Dsrc, const float* bias, int dst_off, float* gout) {
+    // Hidden layers: +bias, ReLU, bf16 into the next A tile.
+    auto hidden = [&](uint32_t Dsrc, const float* bias, int dst_off) {
       const int r = sub * 32 + lane;
-      const int64_t row = m0 + r;
       for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
         float v[16];
         tc::tmem_ld16(Dsrc + lane_off + ch * 16, v);
@@ -245,15 +239,11 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
               make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
                          pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
         }
-        if (gout && row < a.M) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) gout[(int64_t)(ch * 16 + j) * a.M + row] = v[j];
-        }
       }
     };
-    hidden(D1, a.b1, OFF_A0, a.H1);
+    hidden(D1, a.b1, OFF_A0);
     if (!layer(D2, OFF_A0, OFF_W2, U / 16, SBO_U, SBO_U, U)) { ok = 0; break; }
-    hidden(D2, a.b2, OFF_A1, a.H2);
+    hidden(D2, a.b2, OFF_A1);
     if (!layer(D3, OFF_A1, OFF_W3, U / 16, SBO_U, SBO_U, OUTP)) { ok = 0; break; }
     if (half == 0) {
       const int r = sub * 32 + lane;
@@ -282,6 +272,452 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   }
 }
 
+
+// ---------------------------------------------------------------------------------
+// Fused backward for BF16 models. Per 128-row tile, one persistent CTA per SM:
+//   recompute  X0 -> L0 -> h -> Fourier encoding -> X1 -> L1 -> H1 -> L2 -> H2
+//   (a) dH2 = (dZ W3^T) * [H2 > 0]          (b) dW3 += H2^T dZ
+//   (c) dH1 = (dH2 W2^T) * [H1 > 0]          (d) dW2 += H1^T dH2   (e) db2 += dH2^T 1
+//   (f) dX1 = dH1 W1^T -> encoding backward -> dH0                 (g) dW1 += X1^T dH1 (+ db1)
+//   (h) dX0 = dH0 W0^T                       (i) dW0 += X0^T dH0
+// The data-gradient products read activation tiles K-major as usual; the
+// weight-gradient products contract over the tile's rows and read the SAME tiles as
+// MN-major operands (transpose bits of the instruction descriptor), so no transposed
+// copy is ever made. The four weight gradients (and db1, db2) accumulate in TMEM across
+// all of a CTA's tiles and are added to the global gradients once at the end. Nothing
+// but dX0 and the gradients goes back to global memory.
+// ---------------------------------------------------------------------------------
+namespace bwd {
+
+// Natural tiles are [rows][width] bf16 in the K-major canonical layout with
+// SBO = (width / 8) * 128. Shared-memory map (bytes):
+constexpr int SBO_A = SBO_F;                // RA: 144 wide (X0, then H1 / dH1, then X0 again)
+constexpr int SBO_B = SBO_E;                // RB: 160 wide (X1; dX0 staging at the end of a tile)
+constexpr int SBO_C = SBO_U;                // RC: 128 wide (H2 / dH2)
+constexpr int SBO_Z = 256;                  // RD, RE3: 16 wide (dZ, the constant e3 tile)
+constexpr int SBO_H0 = 512;                 // RE: 32 wide (dH0)
+constexpr int RA = WPACK_BYTES;             // after the forward's packed weight images
+constexpr int RB = RA + BM * F * 2;
+constexpr int RC = RB + BM * ENCP * 2;
+constexpr int RD = RC + BM * U * 2;
+constexpr int RE3 = RD + BM * 16 * 2;
+constexpr int RE = RE3 + BM * 16 * 2;
+constexpr int RF = RE + BM * SQP * 2;       // h (fp32, 128 x 27) for the encoding backward
+constexpr int BAR = RF + BM * SQ * 4;
+constexpr int SMEM = BAR + 64;
+static_assert(SMEM <= 232448, "shared memory");
+
+// TMEM columns: the per-tile chain (L0..L2 outputs, dH2, dH1, dX1, dX0) reuses
+// [0, 144); the weight-gradient accumulators persist.
+constexpr uint32_t T_CH = 0, T_W3 = 144, T_W2 = 160, T_W1 = 288, T_W0A = 448, T_W0B = 480;
+
+// MN-major, no-swizzle canonical layout: LBO = byte distance between core matrices
+// adjacent along K, SBO = along M/N. A natural tile read MN-major has K = its rows.
+struct Op {
+  uint32_t addr, lbo, sbo, step;  // step: start-address advance per 16-element K step
+};
+__device__ __forceinline__ Op kmaj(uint32_t addr, uint32_t sbo) { return Op{addr, 128u, sbo, 256u}; }
+__device__ __forceinline__ Op mnmaj(uint32_t addr, uint32_t row_group_stride) {
+  return Op{addr, row_group_stride, 128u, 2u * row_group_stride};
+}
+__host__ __device__ constexpr uint32_t idesc_t(int M, int N, bool a_mn, bool b_mn) {
+  return tc::idesc(M, N, 1u) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+__device__ __forceinline__ void mma_run(uint32_t d, Op a, Op b, int ksteps, uint32_t idesc, bool accumulate) {
+#pragma unroll 1
+  for (int s = 0; s < ksteps; ++s) {
+    tc::mma_bf16(d, tc::sdesc(a.addr + s * a.step, a.lbo, a.sbo), tc::sdesc(b.addr + s * b.step, b.lbo, b.sbo),
+                 idesc, (accumulate || s > 0) ? 1u : 0u);
+  }
+}
+
+struct Args {
+  int64_t M;
+  const uint8_t* wpack;  // the forward's packed weight images (WPACK_BYTES)
+  const float* X0;       // (M, 144)
+  const float* dirs;
+  int rows_per_dir;
+  const float *b1, *b2;
+  const float* dZ3;      // (M, 3): gradient wrt the pre-sigmoid output
+  float* dX0;            // (M, 144) overwritten, or null
+  float *gw0, *gw1, *gb1, *gw2, *gb2, *gw3, *gb3;  // accumulate
+};
+
+// Encoding backward for features [J0, J0 + NJ) of row r: dh_j = dX1[j] + the
+// derivatives of [sin h, sin 2h, cos h, cos 2h] (columns 30 + 4j .. 33 + 4j).
+template <int J0, int NJ>
+__device__ __forceinline__ void encoding_bwd(uint32_t taddr, const float* hrow, float (&dh)[14]) {
+  float fc[NJ][4];
+#pragma unroll
+  for (int jj = 0; jj < NJ; ++jj) {
+    float s1, c1;
+    __sincosf(hrow[J0 + jj], &s1, &c1);
+    fc[jj][0] = c1;
+    fc[jj][1] = 2.0f * (c1 * c1 - s1 * s1);
+    fc[jj][2] = -s1;
+    fc[jj][3] = -4.0f * s1 * c1;
+    dh[jj] = 0.0f;
+  }
+  constexpr int PE_LO = SQ + 3 + 4 * J0, PE_HI = PE_LO + 4 * NJ;  // encoding columns of these features
+#pragma unroll
+  for (int ch = 0; ch < 9; ++ch) {
+    const int c0 = ch * 16;
+    const bool direct = c0 < J0 + NJ && c0 + 16 > J0;
+    const bool pe = c0 < PE_HI && c0 + 16 > PE_LO;
+    if (!direct && !pe) continue;
+    float v[16];
+    tc::tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const int col = c0 + e;
+      if (col >= J0 && col < J0 + NJ) dh[col - J0] += v[e];
+      if (col >= PE_LO && col < PE_HI) {
+        const int j = (col - PE_LO) >> 2, q = (col - PE_LO) & 3;
+        dh[j] = fmaf(fc[j][q], v[e], dh[j]);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + BAR);
+  uint64_t* wbar = mbar + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + BAR + 16);
+  float* hstash = reinterpret_cast<float*>(smem + RF);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int sub = warp & 3, half = warp >> 2;
+  const int r = sub * 32 + lane;  // tile row owned by this thread in the epilogues
+
+  if (warp == 0) tc::tmem_alloc(tslot, 512);
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_init(wbar, 1);
+  }
+  // Constant tile e3 (column 3 = 1): dH2^T e3 accumulates db2 into column 3 of dW3.
+  for (int c = tid; c < BM * 2; c += THREADS) {
+    const int row = c >> 1, kc = c & 1;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (kc == 0) v.y = pack2(0.0f, 1.0f);
+    *reinterpret_cast<uint4*>(smem + RE3 + coff(row, kc, SBO_Z)) = v;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    tc::mbar_expect_tx(wbar, WPACK_BYTES);
+    tc::bulk_g2s(smem + OFF_W0, a.wpack, WPACK_BYTES, wbar);
+  }
+  int ok = tc::mbar_wait(wbar, 0, WAIT_LIMIT) ? 1 : 0;
+  ok = __syncthreads_and(ok);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane_off = (uint32_t)(sub * 32) << 16;
+  const uint32_t sb = tc::smem_u32(smem);
+  uint32_t phase = 0;
+  float db3[3] = {0.f, 0.f, 0.f};
+  bool first = true;
+
+  // Thread 0 issues the MMAs of one step; everyone waits for them.
+  auto run = [&](auto&& issue_fn) -> bool {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      issue_fn();
+      tc::mma_commit(mbar);
+    }
+    const int done = tc::mbar_wait(mbar, phase, WAIT_LIMIT) ? 1 : 0;
+    phase ^= 1u;
+    const int all = __syncthreads_and(done);
+    tc::fence_after_sync();
+    return all != 0;
+  };
+  auto load_x0 = [&](int64_t m0) {
+    for (int c = tid; c < BM * (F / 8); c += THREADS) {
+      const int rr = c / (F / 8), kc = c % (F / 8);
+      const int64_t row = m0 + rr;
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), q = p;
+      if (row < a.M) {
+        const float4* src = reinterpret_cast<const float4*>(a.X0 + row * F + kc * 8);
+        p = __ldg(src);
+        q = __ldg(src + 1);
+      }
+      *reinterpret_cast<uint4*>(smem + RA + coff(rr, kc, SBO_A)) =
+          make_uint4(pack2(p.x, p.y), pack2(p.z, p.w), pack2(q.x, q.y), pack2(q.z, q.w));
+    }
+  };
+  // +bias, ReLU, bf16 into a natural tile.
+  auto hidden = [&](const float* bias, int dst, int sbo) {
+    for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
+      float v[16];
+      tc::tmem_ld16(tmem + T_CH + lane_off + ch * 16, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        *reinterpret_cast<uint4*>(smem + dst + coff(r, ch * 2 + q, sbo)) =
+            make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                       pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+      }
+    }
+  };
+  // dH = D * [H > 0], written over H in place (H's tile is no longer read by any MMA).
+  auto relu_bwd = [&](int reg, int sbo) {
+    for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
+      float v[16];
+      tc::tmem_ld16(tmem + T_CH + lane_off + ch * 16, v);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        uint4* p = reinterpret_cast<uint4*>(smem + reg + coff(r, ch * 2 + q, sbo));
+        uint4 hv = *p;
+        const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&hv);
+        uint32_t o[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float2 f = __bfloat1622float2(hb[e]);
+          o[e] = pack2(f.x > 0.f ? v[8 * q + 2 * e] : 0.f, f.y > 0.f ? v[8 * q + 2 * e + 1] : 0.f);
+        }
+        *p = make_uint4(o[0], o[1], o[2], o[3]);
+      }
+    }
+  };
+
+  const int64_t ntiles = (a.M + BM - 1) / BM;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int64_t m0 = tile * BM;
+    load_x0(m0);
+    if (tid < BM) {  // dZ tile: columns 0..2, zero to 16
+      const int64_t row = m0 + tid;
+      float z0 = 0.f, z1 = 0.f, z2 = 0.f;
+      if (row < a.M) {
+        z0 = __ldg(a.dZ3 + row * 3);
+        z1 = __ldg(a.dZ3 + row * 3 + 1);
+        z2 = __ldg(a.dZ3 + row * 3 + 2);
+        db3[0] += z0;
+        db3[1] += z1;
+        db3[2] += z2;
+      }
+      *reinterpret_cast<uint4*>(smem + RD + coff(tid, 0, SBO_Z)) = make_uint4(pack2(z0, z1), pack2(z2, 0.f), 0u, 0u);
+      *reinterpret_cast<uint4*>(smem + RD + coff(tid, 1, SBO_Z)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    // L0: h = X0 W0.
+    if (!run([&] { mma_run(tmem + T_CH, kmaj(sb + RA, SBO_A), kmaj(sb + OFF_W0, SBO_F), F / 16,
+                           idesc_t(BM, SQP, false, false), false); })) { ok = 0; break; }
+    // Fourier encoding into X1 (as in the forward; column 150 = 1 makes dW1's product
+    // also deliver db1), and h kept in fp32 for the encoding backward.
+    {
+      const int64_t row = m0 + r;
+      uint8_t* xrow = smem + RB + (r >> 3) * SBO_B + (r & 7) * 16;
+      auto put = [&](int col, float v) {
+        *reinterpret_cast<__nv_bfloat16*>(xrow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
+      };
+      auto pe4 = [&](int col, float v) {
+        float sn, cs;
+        __sincosf(v, &sn, &cs);
+        put(col, sn);
+        put(col + 1, 2.0f * sn * cs);
+        put(col + 2, cs);
+        put(col + 3, cs * cs - sn * sn);
+      };
+      float v16[16];
+      if (half == 0) {
+        tc::tmem_ld16(tmem + T_CH + lane_off, v16);
+#pragma unroll
+        for (int j = 0; j < 14; ++j) {
+          put(j, v16[j]);
+          pe4(SQ + 3 + 4 * j, v16[j]);
+          hstash[r * SQ + j] = v16[j];
+        }
+      } else {
+        tc::tmem_ld16(tmem + T_CH + lane_off, v16);
+        const float h14 = v16[14], h15 = v16[15];
+        tc::tmem_ld16(tmem + T_CH + lane_off + 16, v16);
+        put(14, h14);
+        pe4(SQ + 3 + 4 * 14, h14);
+        hstash[r * SQ + 14] = h14;
+        put(15, h15);
+        pe4(SQ + 3 + 4 * 15, h15);
+        hstash[r * SQ + 15] = h15;
+#pragma unroll
+        for (int j = 16; j < SQ; ++j) {
+          put(j, v16[j - 16]);
+          pe4(SQ + 3 + 4 * j, v16[j - 16]);
+          hstash[r * SQ + j] = v16[j - 16];
+        }
+        float d[3] = {0.f, 0.f, 0.f};
+        if (row < a.M) {
+          const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
+          d[0] = __ldg(dp);
+          d[1] = __ldg(dp + 1);
+          d[2] = __ldg(dp + 2);
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          put(SQ + q, d[q]);
+          pe4(SQ + 3 + 4 * SQ + 4 * q, d[q]);
+        }
+#pragma unroll
+        for (int c = ENC; c < ENCP; ++c) put(c, c == ENC ? 1.0f : 0.0f);
+      }
+    }
+    // L1, L2 (the L1 product ignores column 150: W1's image is zero there).
+    if (!run([&] { mma_run(tmem + T_CH, kmaj(sb + RB, SBO_B), kmaj(sb + OFF_W1, SBO_E), ENCP / 16,
+                           idesc_t(BM, U, false, false), false); })) { ok = 0; break; }
+    hidden(a.b1, RA, SBO_A);
+    if (!run([&] { mma_run(tmem + T_CH, kmaj(sb + RA, SBO_A), kmaj(sb + OFF_W2, SBO_U), U / 16,
+                           idesc_t(BM, U, false, false), false); })) { ok = 0; break; }
+    hidden(a.b2, RC, SBO_C);
+    // (a) dH2 pre-mask = dZ W3^T; (b) dW3 += H2^T dZ.
+    if (!run([&] {
+          mma_run(tmem + T_CH, kmaj(sb + RD, SBO_Z), mnmaj(sb + OFF_W3, SBO_U), 1, idesc_t(BM, U, false, true), false);
+          mma_run(tmem + T_W3, mnmaj(sb + RC, SBO_C), mnmaj(sb + RD, SBO_Z), BM / 16, idesc_t(BM, 16, true, true),
+                  !first);
+        })) { ok = 0; break; }
+    relu_bwd(RC, SBO_C);
+    // (c) dH1 pre-mask = dH2 W2^T; (d) dW2^T += dH2^T H1; (e) db2 via dH2^T e3.
+    if (!run([&] {
+          mma_run(tmem + T_CH, kmaj(sb + RC, SBO_C), mnmaj(sb + OFF_W2, SBO_U), U / 16, idesc_t(BM, U, false, true),
+                  false);
+          mma_run(tmem + T_W2, mnmaj(sb + RC, SBO_C), mnmaj(sb + RA, SBO_A), BM / 16, idesc_t(BM, U, true, true),
+                  !first);
+          mma_run(tmem + T_W3, mnmaj(sb + RC, SBO_C), mnmaj(sb + RE3, SBO_Z), BM / 16, idesc_t(BM, 16, true, true),
+                  true);
+        })) { ok = 0; break; }
+    relu_bwd(RA, SBO_A);
+    // (f) dX1 = dH1 W1^T (144 columns: everything before the view-direction encoding);
+    // (g) dW1^T += dH1^T X1 (column 150 of X1 is 1: db1).
+    if (!run([&] {
+          mma_run(tmem + T_CH, kmaj(sb + RA, SBO_A), mnmaj(sb + OFF_W1, SBO_E), U / 16, idesc_t(BM, F, false, true),
+                  false);
+          mma_run(tmem + T_W1, mnmaj(sb + RA, SBO_A), mnmaj(sb + RB, SBO_B), BM / 16, idesc_t(BM, ENCP, true, true),
+                  !first);
+        })) { ok = 0; break; }
+    {
+      float dh[14];
+      const float* hrow = hstash + r * SQ;
+      uint8_t* drow = smem + RE + (r >> 3) * SBO_H0 + (r & 7) * 16;
+      auto put = [&](int col, float v) {
+        *reinterpret_cast<__nv_bfloat16*>(drow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
+      };
+      if (half == 0) {
+        encoding_bwd<0, 14>(tmem + T_CH + lane_off, hrow, dh);
+#pragma unroll
+        for (int j = 0; j < 14; ++j) put(j, dh[j]);
+      } else {
+        encoding_bwd<14, 13>(tmem + T_CH + lane_off, hrow, dh);
+#pragma unroll
+        for (int j = 0; j < 13; ++j) put(14 + j, dh[j]);
+#pragma unroll
+        for (int c = SQ; c < SQP; ++c) put(c, 0.0f);
+      }
+    }
+    load_x0(m0);  // dW0 contracts X0 again; RA is free now
+    // (h) dX0 = dH0 W0^T; (i) dW0 += X0^T dH0 as two M = 128 products (features 0..127
+    // and 16..143).
+    if (!run([&] {
+          if (a.dX0)
+            mma_run(tmem + T_CH, kmaj(sb + RE, SBO_H0), mnmaj(sb + OFF_W0, SBO_F), SQP / 16,
+                    idesc_t(BM, F, false, true), false);
+          mma_run(tmem + T_W0A, mnmaj(sb + RA, SBO_A), mnmaj(sb + RE, SBO_H0), BM / 16,
+                  idesc_t(BM, SQP, true, true), !first);
+          mma_run(tmem + T_W0B, mnmaj(sb + RA + 256, SBO_A), mnmaj(sb + RE, SBO_H0), BM / 16,
+                  idesc_t(BM, SQP, true, true), !first);
+        })) { ok = 0; break; }
+    if (a.dX0) {
+      // TMEM -> per-warp 32 x 17 staging (in RB) -> 16-byte row stores.
+      float* buf = reinterpret_cast<float*>(smem + RB) + warp * (32 * 17);
+      const int ch_begin = half ? 5 : 0, ch_end = half ? 9 : 5;
+      for (int ch = ch_begin; ch < ch_end; ++ch) {
+        float v[16];
+        tc::tmem_ld16(tmem + T_CH + lane_off + ch * 16, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) buf[lane * 17 + j] = v[j];
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int idx = q * 32 + lane;
+          const int rr = idx >> 2, c4 = (idx & 3) * 4;
+          const int64_t row = m0 + sub * 32 + rr;
+          if (row < a.M) {
+            *reinterpret_cast<float4*>(a.dX0 + row * F + ch * 16 + c4) =
+                make_float4(buf[rr * 17 + c4], buf[rr * 17 + c4 + 1], buf[rr * 17 + c4 + 2], buf[rr * 17 + c4 + 3]);
+          }
+        }
+        __syncwarp();
+      }
+    }
+    first = false;
+  }
+
+  if (ok && !first) {
+    // Weight gradients: TMEM lane = output row of each accumulator.
+    float v[16];
+    if (half == 0) {  // dW3 (lane = H2 feature, columns 0..2) and db2 (column 3)
+      tc::tmem_ld16(tmem + T_W3 + lane_off, v);
+#pragma unroll
+      for (int n = 0; n < 3; ++n) atomicAdd(a.gw3 + r * 3 + n, v[n]);
+      atomicAdd(a.gb2 + r, v[3]);
+    } else {  // dW0, features 128..143 (lanes 112..127 of the second product)
+#pragma unroll
+      for (int ch = 0; ch < 2; ++ch) {
+        tc::tmem_ld16(tmem + T_W0B + lane_off + ch * 16, v);
+        if (r >= 112) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (ch * 16 + j < SQ) atomicAdd(a.gw0 + (int64_t)(r + 16) * SQ + ch * 16 + j, v[j]);
+        }
+      }
+    }
+    if (half == 0) {  // dW0, features 0..127
+#pragma unroll
+      for (int ch = 0; ch < 2; ++ch) {
+        tc::tmem_ld16(tmem + T_W0A + lane_off + ch * 16, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (ch * 16 + j < SQ) atomicAdd(a.gw0 + (int64_t)r * SQ + ch * 16 + j, v[j]);
+      }
+    }
+    for (int ch = half * 4; ch < half * 4 + 4; ++ch) {  // dW2^T: lane = output unit, column = input
+      tc::tmem_ld16(tmem + T_W2 + lane_off + ch * 16, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) atomicAdd(a.gw2 + (int64_t)(ch * 16 + j) * U + r, v[j]);
+    }
+    for (int ch = half * 5; ch < half * 5 + 5; ++ch) {  // dW1^T and db1 (input column 150)
+      tc::tmem_ld16(tmem + T_W1 + lane_off + ch * 16, v);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int in = ch * 16 + j;
+        if (in < ENC) atomicAdd(a.gw1 + (int64_t)in * U + r, v[j]);
+        else if (in == ENC) atomicAdd(a.gb1 + r, v[j]);
+      }
+    }
+    if (warp < 4) {
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        float s = db3[n];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) atomicAdd(a.gb3 + n, s);
+      }
+    }
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(&g_fused_status, 1);
+    tc::mbar_wait(wbar, 0, WAIT_LIMIT);
+    tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+}  // namespace bwd
+
 }  // namespace fmlp
 
 int fused_status(int32_t* out, cudaStream_t st) {
@@ -306,7 +742,7 @@ bool mlp_fused_supported(const MlpDims& d) {
 size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }
 
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, float* X1, float* H1, float* H2, uint8_t* wpack, cudaStream_t st) {
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st) {
   if (M == 0) return TVM_OK;
   static int sms = 0;
   static bool attr = false;
@@ -328,11 +764,41 @@ int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0,
   }
   fmlp::pack_weights_kernel<<<64, 256, 0, st>>>(wpack, w.w0, w.w1, w.w2, w.w3);
   TVM_TRY(check_launch("pack_weights"));
-  fmlp::Args a{M, wpack, X0, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb, X1, H1, H2};
+  fmlp::Args a{M, wpack, X0, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(sms, 1));
   fmlp::mlp_fwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::SMEM, st>>>(a);
   return check_launch("mlp_fwd_fused");
+}
+
+int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
+                         int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
+                         cudaStream_t st) {
+  if (M == 0) return TVM_OK;
+  static int sms = 0;
+  static bool attr = false;
+  if (!attr) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaFuncSetAttribute(fmlp::bwd::mlp_bwd_fused_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, fmlp::bwd::SMEM);
+    if (e != cudaSuccess) {
+      set_error("fused mlp backward smem attribute: %s", cudaGetErrorString(e));
+      return TVM_ERR_LAUNCH;
+    }
+    attr = true;
+  }
+  if (!aligned(wpack, 16) || !aligned(X0, 16) || (dX0 && !aligned(dX0, 16))) {
+    set_error("fused mlp backward: packed weights, features and dX0 must be 16-byte aligned");
+    return TVM_ERR_ALIGN;
+  }
+  fmlp::bwd::Args a{M, wpack, X0, dirs, rows_per_dir, w.b1, w.b2, dZ3, dX0,
+                    g.w0, g.w1, g.b1, g.w2, g.b2, g.w3, g.b3};
+  const int64_t ntiles = ceil_div(M, fmlp::BM);
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(sms, 1));
+  fmlp::bwd::mlp_bwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::bwd::SMEM, st>>>(a);
+  return check_launch("mlp_bwd_fused");
 }
 
 }  // namespace tvm

@@ -2,7 +2,8 @@
 library's static scratch array instead of a caller workspace. Through the C ABI, two
 calls in a row (different inputs and row counts, the first at the largest row count
 the scratch allows) must give the rgb of tvm_mlp_fwd within the MLP parity
-tolerance. Oversized calls must be rejected before any launch.
+tolerance. Oversized calls must be rejected before any launch; their buffers are
+sized for every requested row all the same.
 
 The file name sorts last so that pytest runs it after every other test; it must
 also pass alone in a fresh process."""
@@ -14,7 +15,19 @@ import torch
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-4  # same relative tolerance as the MLP parity tests
-MAX_ROWS_DEFAULT_MODEL = 9924
+
+
+def _max_rows(lp):
+    """The row limit the library reports for this model: a call with an impossible row
+    count and no pointers fails the size check on the host, before any launch."""
+    import re
+    from tensorf_gb300 import _lib
+    lib = _lib.load()
+    md = lp.model_desc()
+    status = lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), None, None, None, 1 << 40, None, None)
+    if status != -2:  # no scratch limit for this model (fused BF16 path)
+        return None
+    return int(re.search(r"at most (\d+) rows", lib.tvm_last_error_message().decode()).group(1))
 
 
 def _rel_err(a, b):
@@ -65,8 +78,10 @@ def _static(lp, feats, dirs, rgb):
 def test_static_scratch_mlp_matches_workspace_entry_point(precision):
     from tensorf_gb300 import _lib
     lp = _model(precision, seed=11)
-    outs = []
-    for call, n in enumerate((MAX_ROWS_DEFAULT_MODEL, 3001)):
+    limit = _max_rows(lp)
+    assert (limit is None) == (precision == "bf16")
+    first_n = limit if limit is not None else 50000
+    for call, n in enumerate((first_n, 3001)):
         feats, dirs = _inputs(n, seed=100 + call)
         want = _with_workspace(lp, feats, dirs)
         got = torch.full((n, 3), float("nan"), device="cuda")
@@ -75,7 +90,6 @@ def test_static_scratch_mlp_matches_workspace_entry_point(precision):
         assert torch.isfinite(got).all()
         err = _rel_err(got, want)
         assert err < RTOL, (precision, call, err)
-        outs.append(got)
     st = ctypes.c_int32(-1)
     _lib.call("tvm_device_status", ctypes.byref(st), None)
     assert st.value == 0
@@ -83,16 +97,20 @@ def test_static_scratch_mlp_matches_workspace_entry_point(precision):
 
 def test_static_scratch_rejects_rows_beyond_maximum():
     from tensorf_gb300 import _lib
+    from tensorf_gb300._util import ptr
     lp = _model("fp32", seed=12)
-    feats, dirs = _inputs(8, seed=3)
-    rgb = torch.zeros((8, 3), device="cuda")
+    limit = _max_rows(lp)
+    assert limit is not None and 1000 < limit < 20000
+    n = limit + 1
+    # Buffers hold all n rows, so nothing is out of bounds even if the call ran.
+    feats, dirs = _inputs(n, seed=3)
+    rgb = torch.zeros((n, 3), device="cuda")
     md = lp.model_desc()
     lib = _lib.load()
-    from tensorf_gb300._util import ptr
-    status = lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs),
-                                            MAX_ROWS_DEFAULT_MODEL + 1, ptr(rgb), None)
+    status = lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(rgb),
+                                            None)
     assert status == -2  # TVM_ERR_SHAPE, returned before any launch
     msg = lib.tvm_last_error_message().decode()
-    assert "at most 9924 rows" in msg, msg
+    assert f"at most {limit} rows" in msg, msg
     torch.cuda.synchronize()
     assert float(rgb.abs().max()) == 0.0
