@@ -52,8 +52,14 @@ def variant_cfg(name: str, small: bool = False, prop_k: int = 7):
         w["precision"] = "bf16"
     if name == "proposal_bf16":
         w.update(precision="bf16", N=48, k=prop_k, proposal=64, prop_grid=64)
+    if name.startswith("unbounded_"):
+        # Unbounded scene: L-inf contraction to [-2, 2]^3, spacing linear in disparity,
+        # 8192 rays per step, BF16; plain 512 samples vs proposal 64 -> 48.
+        w.update(precision="bf16", R=8192, contract=True)
+        if name == "unbounded_proposal_bf16":
+            w.update(N=48, k=prop_k, proposal=64, prop_grid=64)
     if small:  # the same kernels on 1/4 of the rays, for profiler captures
-        w["R"] = 1024
+        w["R"] //= 4
     return w
 
 
@@ -151,6 +157,35 @@ class Data:
 # half-transparent: softplus(0) = 0.69. With the reference's +10 the 300^3 field starts
 # opaque and neither path recovers within the run; with -3 the uniform path starves.
 DENSITY_SHIFT = 0.0
+# Unbounded scene: step sizes are world distances that grow to hundreds of units at the
+# far end, so the field starts more transparent (softplus(-3) = 0.05); 0 and -6 both
+# train worse on both paths.
+DENSITY_SHIFT_UNBOUNDED = -3.0
+UNBOUNDED_NEAR, UNBOUNDED_FAR = 0.5, 1000.0
+
+
+def shift_of(w):
+    return DENSITY_SHIFT_UNBOUNDED if w.get("contract") else DENSITY_SHIFT
+
+
+class UnboundedData:
+    """Rays from inside radius 1 in uniform directions on the unbounded sphere scene."""
+
+    def __init__(self, R, seed=0, pool_batches=32, test_rays=8192):
+        from tensorf_gb300 import scene
+
+        self.sc = scene.SphereScene.unbounded(seed + 5)
+        self.R = R
+        self.rays, self.colors = self.sc.unbounded_training_rays(R * pool_batches, seed=seed + 6)
+        self.test_rays, self.test_colors = self.sc.unbounded_training_rays(test_rays, seed=seed + 7)
+
+    def batch(self, i):
+        from tensorf_gb300 import cameras
+
+        n = self.rays.origins.shape[0] // self.R
+        j = i % n
+        sl = slice(j * self.R, (j + 1) * self.R)
+        return cameras.Rays3D(self.rays.origins[sl], self.rays.directions[sl]), self.colors[sl]
 
 
 def make_state(w, data):
@@ -159,9 +194,16 @@ def make_state(w, data):
     spec = render.ModelSpec(grid_dim=w["grid"], density_feat_dim=w["Cd"], appearance_feat_dim=w["Ca"],
                             precision=w["precision"], proposal_grid=w["prop_grid"])
     prop = render.ProposalConfig(samples=w["proposal"]) if w["proposal"] else None
-    cfg = training.TrainConfig(initial_aabb_min=data.sc.aabb[0], initial_aabb_max=data.sc.aabb[1],
-                               density_samples_per_ray=w["N"], appearance_samples_per_ray=w["k"], n_iters=30000,
-                               upsamp_iters=(), density_shift=DENSITY_SHIFT, proposal=prop)
+    if w.get("contract"):
+        cfg = training.TrainConfig(initial_aabb_min=(-2.0,) * 3, initial_aabb_max=(2.0,) * 3, scene_contraction=True,
+                                   contracted_spacing="disparity", render_near=UNBOUNDED_NEAR,
+                                   render_far=UNBOUNDED_FAR, density_samples_per_ray=w["N"],
+                                   appearance_samples_per_ray=w["k"], n_iters=30000, upsamp_iters=(),
+                                   density_shift=DENSITY_SHIFT_UNBOUNDED, proposal=prop)
+    else:
+        cfg = training.TrainConfig(initial_aabb_min=data.sc.aabb[0], initial_aabb_max=data.sc.aabb[1],
+                                   density_samples_per_ray=w["N"], appearance_samples_per_ray=w["k"],
+                                   n_iters=30000, upsamp_iters=(), density_shift=DENSITY_SHIFT, proposal=prop)
     return training.TrainState.initialize(cfg, spec, seed=94709)
 
 
@@ -175,6 +217,21 @@ def proposal_of(w):
     from tensorf_gb300 import render
 
     return render.ProposalConfig(samples=w["proposal"]) if w["proposal"] else None
+
+
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time (ms); every rank gets it. dist is None on one process."""
+    if dist is None:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rays_per_s(rays_per_step, steps, world, ms_max):
+    """Whole-job throughput of replicas: every rank processes its own rays_per_step
+    each step, the job ends with the slowest rank."""
+    return rays_per_step * steps * world / (ms_max / 1e3)
 
 
 def time_train(state, data, steps, warmup, phases=True, start_step=0):
@@ -229,9 +286,13 @@ def psnr(a, b):
 def eval_rays(state, w, rays, mode=None, chunk=65536):
     from tensorf_gb300 import render
 
+    rc = render_cfg(w, mode)
+    if w.get("contract"):
+        rc = render.RenderConfig(UNBOUNDED_NEAR, UNBOUNDED_FAR, rc.mode, w["N"], w["k"])
     return render.render_rays_batched(state.appearance_mlp, state.learnable_params, state.aabb, rays,
-                                      render.NoiseKey(12345), render_cfg(w, mode), batch_size=chunk,
-                                      density_shift=DENSITY_SHIFT, to_host=False, proposal=proposal_of(w))
+                                      render.NoiseKey(12345), rc, batch_size=chunk,
+                                      density_shift=shift_of(w), to_host=False, proposal=proposal_of(w),
+                                      schedule=state.schedule())
 
 
 def time_render(state, w, data, views, chunk=65536):
@@ -317,7 +378,8 @@ def run_profile_variant(args):
 
     _lib.load()
     w = variant_cfg(args.profile_variant, args.small, args.prop_k)
-    data = Data(w["R"], pool_batches=8, test_rays=256)
+    data = UnboundedData(w["R"], pool_batches=8, test_rays=256) if w.get("contract") else \
+        Data(w["R"], pool_batches=8, test_rays=256)
     st = make_state(w, data)
     ms, ph, launches = time_train(st, data, args.steps, args.warmup)
     print(json.dumps({"variant": w["name"], "ms_per_step": round(ms / args.steps, 4), "launches": launches,
@@ -348,10 +410,8 @@ def run_ours(args):
         ms, phase_ms, launches = time_train(st_plain, data, args.steps, args.warmup)
     if dist:
         dist.barrier()
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = plain["R"] * args.steps * world / (ms / 1e3)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = job_rays_per_s(plain["R"], args.steps, world, ms)
     done_plain = args.warmup + args.steps
 
     # End to end through the public API: pinned host rays and colours copied in every
@@ -379,11 +439,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1)
     done_plain += args.steps
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = R * args.steps * world / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
+    e2e_value = job_rays_per_s(R, args.steps, world, e2e_ms)
 
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -448,12 +505,43 @@ def run_ours(args):
             "median_depth_terminated_agree": round(float((torch.isfinite(d0) == torch.isfinite(d1)).float().mean()), 4),
             "render_views": args.render_views, "render_chunk": 65536,
         }
+    if not args.headline_only and world == 1:
+        line["unbounded"] = run_unbounded(args)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(plain, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def run_unbounded(args):
+    """Unbounded scene (contraction to [-2, 2]^3, 8192 rays, BF16): proposal 64 -> 48
+    vs plain 512 samples, both spaced linearly in disparity. Train rays/s over the timed
+    steps, then held-out PSNR after the same number of steps."""
+    out = {}
+    data = None
+    for name in ("unbounded_plain_bf16", "unbounded_proposal_bf16"):
+        w = variant_cfg(name, args.small, args.prop_k)
+        if data is None:
+            data = UnboundedData(w["R"])
+        st = make_state(w, data)
+        ms, ph, _ = time_train(st, data, args.steps, args.warmup)
+        done = args.warmup + args.steps
+        train_more(st, data, max(0, args.train_steps - done), done)
+        img = eval_rays(st, w, data.test_rays)
+        out[name] = {"train_rays_per_s": round(w["R"] * args.steps / (ms / 1e3), 1),
+                     "ms_per_step": round(ms / args.steps, 4), "phase_ms": {p: round(v, 4) for p, v in ph.items()},
+                     "rays_per_step": w["R"], "density_samples": w["N"], "appearance_samples": w["k"],
+                     "proposal_samples": w["proposal"], "psnr_db": round(psnr(img, data.test_colors), 3),
+                     "train_steps": max(args.train_steps, done)}
+    p, q = out["unbounded_plain_bf16"], out["unbounded_proposal_bf16"]
+    out["train_speedup_proposal_vs_plain"] = round(q["train_rays_per_s"] / p["train_rays_per_s"], 3)
+    out["psnr_gap_db_plain_minus_proposal"] = round(p["psnr_db"] - q["psnr_db"], 3)
+    out["scene"] = ("128 spheres at distances 2..12 around the origin, rays from inside radius 1 in uniform "
+                    "directions, FP64 quadrature targets (8192 samples per ray)")
+    out["density_shift"] = DENSITY_SHIFT_UNBOUNDED
+    return out
 
 
 # ---------------------------------------------------------------------------------
@@ -556,7 +644,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-rays", type=int, default=256)
     ap.add_argument("--reference-steps", type=int, default=10)
-    ap.add_argument("--profile-variant", choices=["plain_fp32", "bf16", "proposal_bf16"], default=None)
+    ap.add_argument("--profile-variant", choices=["plain_fp32", "bf16", "proposal_bf16", "unbounded_plain_bf16",
+                                                  "unbounded_proposal_bf16"], default=None)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

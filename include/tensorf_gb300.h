@@ -322,6 +322,20 @@ TVM_API int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, c
                       const tvm_render_desc* cfg, float* loss_out, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* FP64 evaluation of the training loss for finite-difference checks of the FP32
+ * gradients, done on the device. It follows render_rays (render.py:105-279, RGB mode)
+ * and the MSE of training_step (training.py:121-134) in double precision. Optionally
+ * params[perturb_index] + perturb_delta replaces one parameter (-1: none). It supports
+ * TVM_F32 models, the bounded sampler, and k == N <= 1024: every sample reaches the
+ * appearance path, so the loss has no selection discontinuity. *loss_out (device
+ * double) is overwritten. This is a check path, not tuned for speed. */
+TVM_API size_t tvm_loss_f64_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg,
+                                           int64_t rays);
+TVM_API int tvm_loss_f64(const tvm_model_desc* model, const void* params, const tvm_rays* rays,
+                         const float* colors, const tvm_render_desc* cfg, int64_t perturb_index,
+                         double perturb_delta, double* loss_out, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
 /* Fused Adam over the flat buffers (training.py:184-203, 213-243). n = layout.total.
  * Elements [0, mlp_begin) use lr_tensor, the rest lr_mlp. Zeroes grads. If shadow is
  * non-NULL (TVM_BF16) the field segments are rounded into it. */

@@ -649,6 +649,42 @@ int tvm_gemm(int32_t math, int32_t a_trans, int32_t b_trans, int64_t M, int32_t 
                   as_stream(stream));
 }
 
+static int validate_loss_f64(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t R) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(model->dtype == TVM_F32, TVM_ERR_DTYPE, "the FP64 loss checks TVM_F32 models");
+  TVM_TRY(validate_render(cfg, R, false, model));
+  TVM_REQUIRE(cfg->sampler == TVM_SAMPLER_BBOX && cfg->mode == TVM_MODE_RGB, TVM_ERR_UNSUPPORTED,
+              "the FP64 loss supports the bounded sampler in RGB mode");
+  TVM_REQUIRE(cfg->appearance_samples == cfg->density_samples && cfg->density_samples <= 1024, TVM_ERR_UNSUPPORTED,
+              "the FP64 loss needs k == N <= 1024 (every sample reaches the appearance path)");
+  return TVM_OK;
+}
+
+size_t tvm_loss_f64_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
+  if (validate_loss_f64(model, cfg, rays) != TVM_OK) return 0;
+  tvm_param_layout L;
+  make_layout(*model, L);
+  return loss_f64_scratch_bytes(*model, L.encoded_dim, rays, cfg->density_samples) + 256;
+}
+
+int tvm_loss_f64(const tvm_model_desc* model, const void* params, const tvm_rays* rays, const float* colors,
+                 const tvm_render_desc* cfg, int64_t perturb_index, double perturb_delta, double* loss_out,
+                 void* workspace, size_t workspace_bytes, void* stream) {
+  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_loss_f64(model, cfg, rays->count));
+  TVM_REQUIRE(params && loss_out && (rays->count == 0 || colors), TVM_ERR_INVALID, "NULL pointer");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  TVM_REQUIRE(perturb_index >= -1 && perturb_index < L.total, TVM_ERR_INVALID, "perturb_index %lld out of range",
+              (long long)perturb_index);
+  const size_t need = loss_f64_scratch_bytes(*model, L.encoded_dim, rays->count, cfg->density_samples);
+  TVM_REQUIRE(workspace_bytes >= need && (need == 0 || workspace), TVM_ERR_WORKSPACE,
+              "workspace too small (%zu < %zu bytes)", workspace_bytes, need);
+  TVM_REQUIRE(aligned(workspace, 8) && aligned(loss_out, 8), TVM_ERR_ALIGN, "workspace and loss_out: 8-byte aligned");
+  return launch_loss_f64(L, *model, static_cast<const float*>(params), perturb_index, perturb_delta, *rays, colors,
+                         *cfg, static_cast<double*>(workspace), loss_out, as_stream(stream));
+}
+
 int tvm_device_status(int32_t* out, void* stream) {
   TVM_REQUIRE(out != nullptr, TVM_ERR_INVALID, "out is NULL");
   return device_status(out, as_stream(stream));

@@ -128,6 +128,12 @@ int launch_resample(const float* wprop, const float* origins, const float* dirs,
 int launch_prop_loss(const float* wmain, const float* wprop, const int32_t* bins, int64_t R, int Np, int Nm,
                      float scale, float* loss, float* gprop, cudaStream_t st);
 
+// ---- FP64 loss for finite-difference checks (tvm_fdcheck.cu) ----
+size_t loss_f64_scratch_bytes(const tvm_model_desc& m, int encoded_dim, int64_t R, int N);
+int launch_loss_f64(const tvm_param_layout& L, const tvm_model_desc& m, const float* params, int64_t pidx,
+                    double delta, const tvm_rays& rays, const float* colors, const tvm_render_desc& c,
+                    double* scratch, double* loss, cudaStream_t st);
+
 // ---- Adam (tvm_adam.cu) ----
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
                 const tvm_adam_desc& a, cudaStream_t st);

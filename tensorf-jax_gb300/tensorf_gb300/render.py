@@ -414,7 +414,7 @@ def render_rays(appearance_mlp: networks.FeatureMlp, learnable_params: Learnable
 def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: LearnableParams, aabb,
                         rays_wrt_world: "cameras.Rays3D", prng_key, config: RenderConfig, *,
                         batch_size: int = 4096, use_tqdm: bool = False, density_shift: float = 10.0,
-                        to_host: bool = True, proposal: Optional[ProposalConfig] = None):
+                        to_host: bool = True, proposal: Optional[ProposalConfig] = None, schedule=None):
     """render.py:49-102: chunks of ``batch_size`` rays, concatenated. Rays stay on the
     device; ``to_host`` returns a NumPy array like the reference."""
     batch_axes = rays_wrt_world.origins.shape[:-1]
@@ -425,7 +425,7 @@ def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: L
     for start in range(0, total, batch_size):
         chunk = cameras.Rays3D(origins=o[start:start + batch_size], directions=d[start:start + batch_size])
         outs.append(render_rays(appearance_mlp, learnable_params, aabb, chunk, prng_key, config,
-                                density_shift=density_shift, proposal=proposal))
+                                density_shift=density_shift, schedule=schedule, proposal=proposal))
     out = torch.cat(outs, dim=0)
     out = out.reshape(tuple(batch_axes) + tuple(out.shape[1:]))
     return out.cpu().numpy() if to_host else out
@@ -453,6 +453,29 @@ def loss_and_grad(learnable_params: LearnableParams, grads: torch.Tensor, aabb, 
               ptr(grads), ctypes.byref(rs), ptr(colors.contiguous()), ctypes.byref(desc), ptr(loss), ptr(ws),
               ws.numel(), stream_handle())
     return loss
+
+
+def loss_f64(learnable_params: LearnableParams, aabb, rays_wrt_world, colors: torch.Tensor, noise: RenderNoise,
+             config: RenderConfig, *, density_shift: float = 10.0, perturb_index: int = -1,
+             perturb_delta: float = 0.0) -> float:
+    """The training loss evaluated in FP64 on the device, optionally with one flat
+    parameter moved by ``perturb_delta``: central finite differences of the FP32
+    gradients (bounded sampler, k == N, FP32 models)."""
+    o = rays_wrt_world.origins.reshape(-1, 3)
+    r = o.shape[0]
+    desc = make_render_desc(config, aabb, noise, r, False, None, density_shift)
+    md = learnable_params.model_desc()
+    rs = rays_struct(rays_wrt_world)
+    lib = _lib.load()
+    nbytes = lib.tvm_loss_f64_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
+    if nbytes == 0:
+        raise ValueError("invalid FP64 loss configuration: " + lib.tvm_last_error_message().decode())
+    ws = workspace(nbytes, o.device)
+    out = torch.zeros(1, dtype=torch.float64, device=o.device)
+    _lib.call("tvm_loss_f64", ctypes.byref(md), ptr(learnable_params.params), ctypes.byref(rs),
+              ptr(colors.contiguous()), ctypes.byref(desc), int(perturb_index), float(perturb_delta), ptr(out),
+              ptr(ws), ws.numel(), stream_handle())
+    return float(out.item())
 
 
 # ---------------------------------------------------------------------------------

@@ -9,6 +9,9 @@
   quadrature (4096 midpoint samples per ray over the aabb segment) on the device. It
   stands in for the Blender lego scene, which is not available here.
 * ``unbounded_rays`` -- origins within radius 1, directions uniform on the sphere.
+* ``SphereScene.unbounded`` -- spheres at distances 2..12 from the origin in every
+  direction, radius proportional to distance, seen from inside by ``unbounded_rays``:
+  the unbounded-scene workload (scene contraction to [-2, 2]^3).
 """
 from __future__ import annotations
 
@@ -57,6 +60,26 @@ class SphereScene:
         return SphereScene(centers=rng.uniform(-extent, extent, size=(count, 3)),
                            radii=rng.uniform(0.1, 0.4, size=count),
                            colors=rng.uniform(0.0, 1.0, size=(count, 3)))
+
+    @staticmethod
+    def unbounded(seed: int, count: int = 128) -> "SphereScene":
+        """Spheres around the origin at distances U[2, 12], radius U[0.1, 0.25] times the
+        distance, so that rays starting within radius 1 see content in every direction
+        and most of it beyond the contraction radius."""
+        rng = onp.random.default_rng(seed)
+        v = rng.normal(size=(count, 3))
+        v /= onp.linalg.norm(v, axis=1, keepdims=True)
+        dist = rng.uniform(2.0, 12.0, size=count)
+        return SphereScene(centers=v * dist[:, None], radii=rng.uniform(0.1, 0.25, size=count) * dist,
+                           colors=rng.uniform(0.0, 1.0, size=(count, 3)),
+                           aabb=((-16.0, -16.0, -16.0), (16.0, 16.0, 16.0)))
+
+    def unbounded_training_rays(self, total: int, seed: int, n_samples: int = 8192):
+        """``total`` rays from inside radius 1 in uniform directions with their FP64 target
+        colours."""
+        o, d = unbounded_rays(total, seed)
+        rays = cameras.Rays3D(origins=torch.as_tensor(o, device="cuda"), directions=torch.as_tensor(d, device="cuda"))
+        return rays, self.render(rays, n_samples)
 
     def cameras(self, count: int, seed: int, width: int = 800, height: int = 800, focal: float = 1111.0,
                 radius: float = 4.0) -> List[cameras.Camera]:

@@ -39,6 +39,9 @@ class TrainConfig:
     initial_aabb_max: Tuple[float, float, float] = (1.0, 1.0, 1.0)
     upsamp_iters: Tuple[int, ...] = (2000, 3000, 4000, 5500, 7000)
     scene_contraction: bool = False
+    # Plain contracted sampler: "reference" keeps render.py's heuristic schedule
+    # (render.py:127-151), "disparity" spaces the samples linearly in disparity.
+    contracted_spacing: str = "reference"
     render_near: float = 0.05
     render_far: float = 200.0
     train_ray_sample_multiplier: float = 1.0
@@ -101,6 +104,17 @@ class TrainState:
                                    mode=render.RenderMode.RGB, density_samples_per_ray=n,
                                    appearance_samples_per_ray=k)
 
+    def schedule(self) -> Optional[onp.ndarray]:
+        """The contracted sampler's fixed schedule when it is not the reference one."""
+        if not self.learnable_params.scene_contraction or self.config.proposal is not None:
+            return None
+        if self.config.contracted_spacing == "disparity":
+            cfg = self.render_config()
+            return render.disparity_schedule(cfg.near, cfg.far, cfg.density_samples_per_ray)
+        if self.config.contracted_spacing != "reference":
+            raise ValueError(f"unknown contracted_spacing {self.config.contracted_spacing!r}")
+        return None
+
     def adam_desc(self, count: int) -> _lib.AdamDesc:
         o = self.config.optimizer
         return _lib.AdamDesc(lr_tensor=o.lr_init_tensor, lr_mlp=o.lr_init_mlp, b1=0.9, b2=0.99, eps=1e-8,
@@ -116,7 +130,7 @@ class TrainState:
         if noise is None:
             render_key, self.prng_key = self.prng_key.split()
             noise = render.draw_noise(render_key, r, cfg, lp.scene_contraction, prop)
-        sched = render._schedule_for(cfg, lp.scene_contraction, None, prop)
+        sched = render._schedule_for(cfg, lp.scene_contraction, self.schedule(), prop)
         desc = render.make_render_desc(cfg, self.aabb, noise, r, lp.scene_contraction, sched,
                                        self.config.density_shift, proposal=prop)
         md = lp.model_desc()
