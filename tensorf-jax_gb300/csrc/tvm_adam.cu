@@ -4,8 +4,8 @@
 // optax.chain(scale_by_adam(b1=0.9, b2=0.99, eps=1e-8, eps_root=0),
 // masked(scale(-lr_mlp)), masked(scale(-lr_tensor))) followed by the learning-rate
 // decay multiplier and apply_updates. One pass streams param, grad, mu, nu (4 reads,
-// 3 writes + the zeroed grad): 32 B per parameter, HBM-bound. float4 lanes, grid sized
-// to the 152 SMs.
+// 3 writes + the zeroed grad): 32 B per parameter, HBM-bound, plus 2 B for the bf16
+// shadow of the field segments in BF16 mode. float4 lanes, grid sized to the 152 SMs.
 #include <algorithm>
 
 #include "tvm_internal.h"
@@ -13,37 +13,48 @@
 namespace tvm {
 
 struct AdamScalars {
-  float b1, b2, omb1, omb2, bc1, bc2, eps, lr_t, lr_m, decay;
+  float b1, b2, omb1, omb2, rbc1, rbc2, eps, lr_t, lr_m, decay;
 };
 
+// mu_hat = mu / (1 - b1^t) and nu_hat = nu / (1 - b2^t) as products with the
+// host-side reciprocals (at most one rounding apart from the quotients).
 __device__ __forceinline__ float adam_one(float p, float g, float& m, float& v, float lr,
                                           const AdamScalars& a) {
   m = a.omb1 * g + a.b1 * m;
   v = a.omb2 * (g * g) + a.b2 * v;
-  const float mh = m / a.bc1;
-  const float vh = v / a.bc2;
+  const float mh = m * a.rbc1;
+  const float vh = v * a.rbc2;
   const float u = mh / (sqrtf(vh + 0.0f) + a.eps);
   return p + a.decay * (-lr * u);
 }
 
-__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float* __restrict__ m,
-                            float* __restrict__ v, int64_t n, int64_t mlp_begin, AdamScalars a) {
+// shadow (may be null): bf16 copy of the updated elements [0, shadow_n).
+__global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float* __restrict__ g,
+                                                   float* __restrict__ m, float* __restrict__ v, int64_t n,
+                                                   int64_t mlp_begin, __nv_bfloat16* __restrict__ shadow,
+                                                   int64_t shadow_n, AdamScalars a) {
   const int64_t n4 = n / 4;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
     float4 pp = reinterpret_cast<float4*>(p)[q];
-    float4 gg = reinterpret_cast<float4*>(g)[q];
+    const float4 gg = reinterpret_cast<float4*>(g)[q];
     float4 mm = reinterpret_cast<float4*>(m)[q];
     float4 vv = reinterpret_cast<float4*>(v)[q];
     const int64_t e = q * 4;
-    pp.x = adam_one(pp.x, gg.x, mm.x, vv.x, (e + 0 < mlp_begin) ? a.lr_t : a.lr_m, a);
-    pp.y = adam_one(pp.y, gg.y, mm.y, vv.y, (e + 1 < mlp_begin) ? a.lr_t : a.lr_m, a);
-    pp.z = adam_one(pp.z, gg.z, mm.z, vv.z, (e + 2 < mlp_begin) ? a.lr_t : a.lr_m, a);
-    pp.w = adam_one(pp.w, gg.w, mm.w, vv.w, (e + 3 < mlp_begin) ? a.lr_t : a.lr_m, a);
+    const float lr = (e < mlp_begin) ? a.lr_t : a.lr_m;  // mlp_begin is a multiple of 64
+    pp.x = adam_one(pp.x, gg.x, mm.x, vv.x, lr, a);
+    pp.y = adam_one(pp.y, gg.y, mm.y, vv.y, lr, a);
+    pp.z = adam_one(pp.z, gg.z, mm.z, vv.z, lr, a);
+    pp.w = adam_one(pp.w, gg.w, mm.w, vv.w, lr, a);
     reinterpret_cast<float4*>(p)[q] = pp;
     reinterpret_cast<float4*>(m)[q] = mm;
     reinterpret_cast<float4*>(v)[q] = vv;
     reinterpret_cast<float4*>(g)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (shadow != nullptr && e < shadow_n) {
+      __nv_bfloat162 lo = __floats2bfloat162_rn(pp.x, pp.y), hi = __floats2bfloat162_rn(pp.z, pp.w);
+      reinterpret_cast<uint2*>(shadow)[q] =
+          make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi));
+    }
   }
   for (int64_t e = n4 * 4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     float mm = m[e], vv = v[e];
@@ -51,6 +62,7 @@ __global__ void adam_kernel(float* __restrict__ p, float* __restrict__ g, float*
     m[e] = mm;
     v[e] = vv;
     g[e] = 0.f;
+    if (shadow != nullptr && e < shadow_n) shadow[e] = __float2bfloat16_rn(p[e]);
   }
 }
 
@@ -62,7 +74,7 @@ __global__ void shadow_kernel(const float* __restrict__ src, __nv_bfloat16* __re
 }
 
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
-                const tvm_adam_desc& d, cudaStream_t st) {
+                const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st) {
   if (n == 0) return TVM_OK;
   AdamScalars a;
   a.b1 = d.b1;
@@ -70,14 +82,14 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
   a.omb1 = (float)(1.0 - (double)d.b1);
   a.omb2 = (float)(1.0 - (double)d.b2);
   // optax.bias_correction: 1 - decay**count in float32.
-  a.bc1 = 1.0f - powf(d.b1, (float)d.count);
-  a.bc2 = 1.0f - powf(d.b2, (float)d.count);
+  a.rbc1 = 1.0f / (1.0f - powf(d.b1, (float)d.count));
+  a.rbc2 = 1.0f / (1.0f - powf(d.b2, (float)d.count));
   a.eps = d.eps;
   a.lr_t = d.lr_tensor;
   a.lr_m = d.lr_mlp;
   a.decay = d.lr_decay;
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n / 4 + 1, 256), 152 * 8);
-  adam_kernel<<<blocks, 256, 0, st>>>(params, grads, mu, nu, n, mlp_begin, a);
+  adam_kernel<<<blocks, 256, 0, st>>>(params, grads, mu, nu, n, mlp_begin, shadow, shadow_n, a);
   return check_launch("adam");
 }
 

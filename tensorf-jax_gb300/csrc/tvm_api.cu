@@ -615,12 +615,11 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
   tvm_param_layout L;
   make_layout(*model, L);
   cudaStream_t st = as_stream(stream);
-  TVM_TRY(launch_adam(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
-                      static_cast<float*>(nu), L.total, L.mlp_begin, *adam, st));
-  if (shadow && model->dtype == TVM_BF16)
-    TVM_TRY(launch_shadow(static_cast<const float*>(params), static_cast<__nv_bfloat16*>(shadow),
-                          L.shadow_total, st));
-  return TVM_OK;
+  const bool bf16 = shadow && model->dtype == TVM_BF16;
+  TVM_REQUIRE(!bf16 || aligned(shadow, 8), TVM_ERR_ALIGN, "shadow must be 8-byte aligned");
+  return launch_adam(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
+                     static_cast<float*>(nu), L.total, L.mlp_begin, *adam,
+                     bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0, st);
 }
 
 int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow, void* stream) {

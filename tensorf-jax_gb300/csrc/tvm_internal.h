@@ -136,7 +136,7 @@ int launch_loss_f64(const tvm_param_layout& L, const tvm_model_desc& m, const fl
 
 // ---- Adam (tvm_adam.cu) ----
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
-                const tvm_adam_desc& a, cudaStream_t st);
+                const tvm_adam_desc& a, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st);
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
 
 }  // namespace tvm

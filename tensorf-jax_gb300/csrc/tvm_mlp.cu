@@ -215,26 +215,40 @@ __global__ void __launch_bounds__(256) pe_fwd_kernel(float* __restrict__ X1, int
     dv[r][a] = __ldg(dirs + ((m0 + r) / rows_per_dir) * 3 + a);
   }
   __syncthreads();
-  const int width = enc - sq;
+  // One thread per (row, encoded coordinate): one sincosf, the higher frequencies by
+  // the double-angle identities (sin 2x = 2 s c, cos 2x = c^2 - s^2) for up to 4
+  // frequencies, direct sincosf beyond. sin(x + pi/2) is written as cos(x).
   const int f_end = sq + 3 + sq * 2 * nf;
-  for (int e = threadIdx.x; e < nrows * width; e += blockDim.x) {
-    const int r = e / width;
-    const int c = sq + (e - r * width);
-    float v;
-    if (c < sq + 3) {
-      v = dv[r][c - sq];
-    } else if (c < f_end) {
-      const int q = c - (sq + 3);
-      const int j = q / (2 * nf), f = q - j * 2 * nf;
-      const float x = h[r][j] * (float)(1 << (f % nf));
-      v = sinf(f < nf ? x : x + kHalfPi);
+  for (int e = threadIdx.x; e < nrows * (sq + 3); e += blockDim.x) {
+    const int r = e / (sq + 3), j = e - r * (sq + 3);
+    float* row = X1 + (m0 + r) * ld;
+    float x;
+    int n, col;
+    if (j < sq) {
+      x = h[r][j];
+      n = nf;
+      col = sq + 3 + j * 2 * nf;
     } else {
-      const int q = c - f_end;
-      const int j = q / (2 * nv), f = q - j * 2 * nv;
-      const float x = dv[r][j] * (float)(1 << (f % nv));
-      v = sinf(f < nv ? x : x + kHalfPi);
+      x = dv[r][j - sq];
+      row[j] = x;
+      n = nv;
+      col = f_end + (j - sq) * 2 * nv;
     }
-    X1[(m0 + r) * ld + c] = v;
+    float sn, cs;
+    sincosf(x, &sn, &cs);
+    for (int f = 0; f < n; ++f) {
+      if (f > 0) {
+        if (n <= 4) {
+          const float s2 = 2.0f * sn * cs, c2 = cs * cs - sn * sn;
+          sn = s2;
+          cs = c2;
+        } else {
+          sincosf(x * (float)(1 << f), &sn, &cs);
+        }
+      }
+      row[col + f] = sn;
+      row[col + n + f] = cs;
+    }
   }
 }
 
