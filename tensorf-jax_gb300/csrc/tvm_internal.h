@@ -90,6 +90,7 @@ int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const floa
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
 int fused_status(int32_t* out, cudaStream_t st);   // same for the fused MLP kernel
+int prop_status(int32_t* out, cudaStream_t st);    // same for the tensor-core proposal backward
 bool mlp_fused_supported(const MlpDims& d);
 // wpack: mlp_fused_pack_bytes() of scratch (16-byte aligned) for the packed weights.
 size_t mlp_fused_pack_bytes();

@@ -421,9 +421,10 @@ int device_status(int32_t* out, cudaStream_t st) {
     set_error("device_status: %s", cudaGetErrorString(e));
     return TVM_ERR_LAUNCH;
   }
-  int32_t f = 0;
+  int32_t f = 0, q = 0;
   TVM_TRY(fused_status(&f, st));
-  *out = v | f;
+  TVM_TRY(prop_status(&q, st));
+  *out = v | f | q;
   return TVM_OK;
 }
 

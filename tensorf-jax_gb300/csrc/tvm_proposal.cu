@@ -17,6 +17,7 @@
 // The MLP layers run on the shared tensor-core GEMM (tvm_mlp.cu); these kernels are
 // the per-sample VM features and their scatter, the resampler and the loss.
 #include "tvm_internal.h"
+#include "tvm_tc.cuh"
 
 namespace tvm {
 
@@ -476,12 +477,306 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
   return check_launch("prop_features");
 }
 
+// ---------------------------------------------------------------------------------
+// Tensor-core proposal backward for BF16 models with 64 hidden units. Persistent CTAs
+// of 128 threads, one 128-sample tile at a time (thread = sample = TMEM lane):
+//   gather X (16, bf16 A tile)            -> MMA  H = X W1              (TMEM, 64 cols)
+//   h = relu(H + b1), dh = dz w2 [h > 0]  -> bf16 tiles H, dH (units padded to 128)
+//   MMA dX = dH W1^T (16 cols) | dW1^T += dH^T X | [dW2, db1] += H^T [dz, 0] + dH^T [0, 1]
+//   dX[0:12) -> float4 scatter into the proposal field gradients.
+// The weight-gradient products contract over the tile's samples and read the H / dH /
+// X / Z tiles as MN-major operands. They accumulate in TMEM across the CTA's tiles and
+// reach global memory once per CTA. bf16 operands, fp32 accumulation: the BF16 mode's
+// arithmetic.
+// ---------------------------------------------------------------------------------
+static __device__ int g_prop_status;  // sticky: bit 0 = a bounded tensor-core wait gave up
+
+namespace ptc {
+
+constexpr int THREADS = 128;
+constexpr int U = 64;
+constexpr uint32_t WAIT_LIMIT = 1u << 24;
+// Shared-memory map (bytes). Tiles are [rows][width] bf16, K-major canonical, SBO =
+// (width / 8) * 128.
+constexpr int SBO_16 = 256, SBO_128 = 2048;
+constexpr int OFF_W1 = 0;                       // [64 units][16 inputs]: 2 KB
+constexpr int OFF_X = OFF_W1 + U * 16 * 2;      // [128][16]
+constexpr int OFF_Z1 = OFF_X + 128 * 16 * 2;    // [128][16], column 0 = dz
+constexpr int OFF_Z2 = OFF_Z1 + 128 * 16 * 2;   // [128][16], column 1 = 1
+constexpr int OFF_H = OFF_Z2 + 128 * 16 * 2;    // [128][128], columns 64.. stay 0
+constexpr int OFF_DH = OFF_H + 128 * 128 * 2;   // [128][128], columns 64.. stay 0
+constexpr int OFF_BAR = OFF_DH + 128 * 128 * 2;
+constexpr int SMEM = OFF_BAR + 64;              // ~78 KB: at most 2 CTAs per SM, 2 x 128 TMEM columns
+// TMEM columns.
+constexpr uint32_t T_H = 0, T_DX = 64, T_W1 = 80, T_W2 = 96, NCOLS = 128;
+
+__device__ __forceinline__ int coff(int row, int kchunk, int sbo) { return (row >> 3) * sbo + kchunk * 128 + (row & 7) * 16; }
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+struct Op {
+  uint32_t addr, lbo, sbo, step;
+};
+__device__ __forceinline__ Op kmaj(uint32_t addr, uint32_t sbo) { return Op{addr, 128u, sbo, 256u}; }
+// MN-major view of a natural tile whose rows are the K index (LBO = K-direction core
+// stride, SBO = MN-direction core stride, no swizzle).
+__device__ __forceinline__ Op mnmaj(uint32_t addr, uint32_t row_group_stride) {
+  return Op{addr, row_group_stride, 128u, 2u * row_group_stride};
+}
+__host__ __device__ constexpr uint32_t idesc_t(int M, int N, bool a_mn, bool b_mn) {
+  return tc::idesc(M, N, 1u) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+__device__ __forceinline__ void mma_run(uint32_t d, Op a, Op b, int ksteps, uint32_t idesc, bool accumulate) {
+#pragma unroll 1
+  for (int s = 0; s < ksteps; ++s) {
+    tc::mma_bf16(d, tc::sdesc(a.addr + s * a.step, a.lbo, a.sbo), tc::sdesc(b.addr + s * b.step, b.lbo, b.sbo),
+                 idesc, (accumulate || s > 0) ? 1u : 0u);
+  }
+}
+
+__global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
+    const __nv_bfloat16* __restrict__ lines, const __nv_bfloat16* __restrict__ planes, int G,
+    float* __restrict__ glines, float* __restrict__ gplanes, const float* __restrict__ origins,
+    const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
+    const float* __restrict__ jitter, const float* __restrict__ dz_in, const float* __restrict__ w1,
+    const float* __restrict__ b1, const float* __restrict__ w2, float* __restrict__ gw1, float* __restrict__ gb1,
+    float* __restrict__ gw2, float* __restrict__ gb2) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + OFF_BAR + 8);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  if (warp == 0) tc::tmem_alloc(tslot, NCOLS);
+  if (tid == 0) tc::mbar_init(mbar, 1);
+  // W1 image (B operand [unit][input]), constant columns of Z2, zero halves of H / dH.
+  for (int c = tid; c < U * 2; c += THREADS) {
+    const int u = c >> 1, kc = c & 1;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = __ldg(w1 + (kc * 8 + e) * U + u);
+    *reinterpret_cast<uint4*>(smem + OFF_W1 + coff(u, kc, SBO_16)) =
+        make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+  }
+  {
+    const int r = tid;
+    *reinterpret_cast<uint4*>(smem + OFF_Z2 + coff(r, 0, SBO_16)) = make_uint4(pack2(0.f, 1.f), 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(smem + OFF_Z2 + coff(r, 1, SBO_16)) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(smem + OFF_Z1 + coff(r, 1, SBO_16)) = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (int kc = 8; kc < 16; ++kc) {
+      *reinterpret_cast<uint4*>(smem + OFF_H + coff(r, kc, SBO_128)) = make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(smem + OFF_DH + coff(r, kc, SBO_128)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t sb = tc::smem_u32(smem);
+  uint32_t phase = 0;
+  int ok = 1;
+  bool first = true;
+  float db2 = 0.f;
+  auto run = [&](auto&& issue_fn) -> bool {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      issue_fn();
+      tc::mma_commit(mbar);
+    }
+    const int done = tc::mbar_wait(mbar, phase, WAIT_LIMIT) ? 1 : 0;
+    phase ^= 1u;
+    const int all = __syncthreads_and(done);
+    tc::fence_after_sync();
+    return all != 0;
+  };
+
+  const int Np = s.N;
+  const int64_t nsmp = R * Np;
+  const int64_t ntiles = (nsmp + THREADS - 1) / THREADS;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int64_t smp = tile * THREADS + tid;
+    const bool valid = smp < nsmp;
+    const float dz = valid ? __ldg(dz_in + smp) : 0.f;
+    db2 += dz;
+    float X[PROP_IN];
+#pragma unroll
+    for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
+    PropPair e3[3];
+    if (valid) {
+      const int64_t r = smp / Np;
+      const int j = (int)(smp - r * Np);
+      RayGeom g = load_ray(origins, dirs, r, s);
+      float t, len, x[3];
+      prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
+      float u3[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) u3[a] = grid_coord(x[a], G);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        int a, b, c;
+        mode_perm(m, a, b, c);
+        prop_pair<__nv_bfloat16>(lines, planes, G, m, u3[a], u3[b], u3[c], e3[m]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) X[m * 4 + q] = e3[m].L[q] * e3[m].P[q];
+      }
+      X[12] = x[0];
+      X[13] = x[1];
+      X[14] = x[2];
+      X[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
+    }
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc) {
+      *reinterpret_cast<uint4*>(smem + OFF_X + coff(tid, kc, SBO_16)) =
+          make_uint4(pack2(X[8 * kc], X[8 * kc + 1]), pack2(X[8 * kc + 2], X[8 * kc + 3]),
+                     pack2(X[8 * kc + 4], X[8 * kc + 5]), pack2(X[8 * kc + 6], X[8 * kc + 7]));
+    }
+    *reinterpret_cast<uint4*>(smem + OFF_Z1 + coff(tid, 0, SBO_16)) = make_uint4(pack2(dz, 0.f), 0u, 0u, 0u);
+    // H = X W1.
+    if (!run([&] { mma_run(tmem + T_H, kmaj(sb + OFF_X, SBO_16), kmaj(sb + OFF_W1, SBO_16), 1,
+                           idesc_t(128, U, false, false), false); })) { ok = 0; break; }
+#pragma unroll
+    for (int ch = 0; ch < U / 16; ++ch) {
+      float v[16];
+      tc::tmem_ld16(tmem + T_H + lane_off + ch * 16, v);
+      float dh[16];
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int u = ch * 16 + e;
+        v[e] = fmaxf(v[e] + __ldg(b1 + u), 0.f);
+        dh[e] = v[e] > 0.f ? dz * __ldg(w2 + u) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        *reinterpret_cast<uint4*>(smem + OFF_H + coff(tid, ch * 2 + q, SBO_128)) =
+            make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                       pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+        *reinterpret_cast<uint4*>(smem + OFF_DH + coff(tid, ch * 2 + q, SBO_128)) =
+            make_uint4(pack2(dh[8 * q], dh[8 * q + 1]), pack2(dh[8 * q + 2], dh[8 * q + 3]),
+                       pack2(dh[8 * q + 4], dh[8 * q + 5]), pack2(dh[8 * q + 6], dh[8 * q + 7]));
+      }
+    }
+    // dX = dH W1^T; dW1^T += dH^T X; [dW2, db1] += H^T Z1 + dH^T Z2.
+    if (!run([&] {
+          mma_run(tmem + T_DX, kmaj(sb + OFF_DH, SBO_128), mnmaj(sb + OFF_W1, SBO_16), U / 16,
+                  idesc_t(128, 16, false, true), false);
+          mma_run(tmem + T_W1, mnmaj(sb + OFF_DH, SBO_128), mnmaj(sb + OFF_X, SBO_16), THREADS / 16,
+                  idesc_t(128, 16, true, true), !first);
+          mma_run(tmem + T_W2, mnmaj(sb + OFF_H, SBO_128), mnmaj(sb + OFF_Z1, SBO_16), THREADS / 16,
+                  idesc_t(128, 16, true, true), !first);
+          mma_run(tmem + T_W2, mnmaj(sb + OFF_DH, SBO_128), mnmaj(sb + OFF_Z2, SBO_16), THREADS / 16,
+                  idesc_t(128, 16, true, true), true);
+        })) { ok = 0; break; }
+    float dX[16];
+    tc::tmem_ld16(tmem + T_DX + lane_off, dX);
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
+    if (valid && any) {
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const PropPair& e = e3[m];
+        float* lb = glines + (int64_t)m * G * PROP_C;
+        float* pb = gplanes + (int64_t)m * G * G * PROP_C;
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w0;
+        atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i0 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w1;
+        atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i1 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+        const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
+        const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
+        const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.L[q] * w[k];
+          atomicAdd(reinterpret_cast<float4*>(pb + ((int64_t)rows[k] * G + cols[k]) * PROP_C),
+                    make_float4(v[0], v[1], v[2], v[3]));
+        }
+      }
+    }
+    first = false;
+  }
+  if (ok && !first) {
+    // TMEM lane u (< 64): dW1^T row u = dW1[:, u]; [dW2, db1] row u.
+    float v[16];
+    tc::tmem_ld16(tmem + T_W1 + lane_off, v);
+    if (tid < U) {
+#pragma unroll
+      for (int i = 0; i < PROP_IN; ++i) atomicAdd(gw1 + i * U + tid, v[i]);
+    }
+    tc::tmem_ld16(tmem + T_W2 + lane_off, v);
+    if (tid < U) {
+      atomicAdd(gw2 + tid, v[0]);
+      atomicAdd(gb1 + tid, v[1]);
+    }
+    float sdz = db2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sdz += __shfl_xor_sync(0xffffffffu, sdz, o);
+    if ((tid & 31) == 0) atomicAdd(gb2, sdz);
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(&g_prop_status, 1);
+    tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, NCOLS);
+  }
+}
+
+}  // namespace ptc
+
+int prop_status(int32_t* out, cudaStream_t st) {
+  int32_t v = 0;
+  const int32_t zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbolAsync(&v, g_prop_status, sizeof(int32_t), 0, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_prop_status, &zero, sizeof(int32_t), 0, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_error("prop_status: %s", cudaGetErrorString(e));
+    return TVM_ERR_LAUNCH;
+  }
+  *out = v;
+  return TVM_OK;
+}
+
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
                     const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
   const int U = mlp.units;
+  if (f.dtype == TVM_BF16 && U == ptc::U) {
+    static int sms = 0;
+    static bool attr = false;
+    if (!attr) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaError_t e = cudaFuncSetAttribute(ptc::prop_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           ptc::SMEM);
+      if (e != cudaSuccess) {
+        set_error("proposal backward smem attribute: %s", cudaGetErrorString(e));
+        return TVM_ERR_LAUNCH;
+      }
+      attr = true;
+    }
+    const int64_t tiles = ceil_div(n, ptc::THREADS);
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * std::max(sms, 1));  // 2 CTAs fit an SM
+    ptc::prop_bwd_tc_kernel<<<grid, ptc::THREADS, ptc::SMEM, st>>>(
+        (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines, gplanes, origins, dirs, R, s, edges,
+        jitter, dz, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2);
+    return check_launch("prop_bwd_tc");
+  }
   const size_t smem = ((size_t)18 * U + PBWD_THREADS * 16 + 2 * PBWD_THREADS * (U + 4) + PBWD_THREADS) * sizeof(float);
   const unsigned blocks = (unsigned)ceil_div(n, PBWD_THREADS);
   if (f.dtype == TVM_BF16) {

@@ -162,3 +162,26 @@ def test_trained_proposal_beats_uniform_sampling_at_equal_samples():
         results[name] = _psnr(img, test_colors)
     print(results)
     assert results["proposal"] > results["uniform"] + 0.5, results
+
+
+def test_bf16_proposal_gradients_align_with_fp32():
+    """The BF16 model's proposal backward (tcgen05, bf16 operands) against the FP32
+    model's (FP32 SIMT) on identical parameters: cosine of every proposal segment."""
+    from tensorf_gb300 import cameras, render
+    Np, N, k = 32, 24, 8
+    spec32, ref, o, d, c, aabb, noise = _setup(seed=6, R=4096, Np=Np, N=N, k=k)  # 1024 tiles: several per CTA
+    rn = render.RenderNoise(noise["jitter"].cuda(), noise["gumbel"].cuda(), noise["pj"].cuda())
+    cfg = render.RenderConfig(0.05, 50.0, render.RenderMode.RGB, N, k)
+    prop = render.ProposalConfig(samples=Np, shift=0.5, loss_weight=3.0)
+    out = {}
+    for prec in ("fp32", "bf16"):
+        spec = render.ModelSpec(grid_dim=24, proposal_grid=16, proposal_units=64, precision=prec)
+        lp = render.LearnableParams.from_reference(spec, ref)
+        g = torch.zeros_like(lp.params)
+        render.loss_and_grad(lp, g, aabb, cameras.Rays3D(o.cuda(), d.cuda()), c.cuda(), rn, cfg, density_shift=-1.0,
+                             proposal=prop)
+        out[prec] = lp.to_reference(g)["proposal"]
+    for nm in ("vector", "matrix", "w1", "b1", "w2", "b2"):
+        a, b = out["fp32"][nm].double().flatten(), out["bf16"][nm].double().flatten()
+        cos = float(torch.dot(a, b) / (a.norm() * b.norm() + 1e-30))
+        assert cos > 0.99, (nm, cos)
