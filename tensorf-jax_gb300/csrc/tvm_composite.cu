@@ -23,8 +23,9 @@ __device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) 
 
 // Exact top-k of N uint32 keys held in shared memory by one warp. Writes k packed
 // entries (key << 32 | ~index) to list[0..k), sorted by key descending then index
-// ascending; list has P >= k slots (P a power of two).
-__device__ void warp_topk(const uint32_t* keys, int N, int k, uint64_t* list, int P, int lane) {
+// ascending (by_key), or in increasing index order (!by_key, no sort); list has P >= k
+// slots (P a power of two).
+__device__ void warp_topk(const uint32_t* keys, int N, int k, uint64_t* list, int P, int lane, bool by_key = true) {
   uint32_t T = 0;
   for (int b = 31; b >= 0; --b) {
     const uint32_t cand = T | (1u << b);
@@ -54,6 +55,8 @@ __device__ void warp_topk(const uint32_t* keys, int N, int k, uint64_t* list, in
     sel_base += __popc(selm);
     eq_base += __popc(eqm);
   }
+  __syncwarp();
+  if (!by_key) return;  // list[0, k) is already in increasing sample order
   for (int j = k + lane; j < P; j += 32) list[j] = 0ull;
   __syncwarp();
   for (int size = 2; size <= P; size <<= 1) {
@@ -278,7 +281,10 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
     return;
   }
   __syncwarp();
-  warp_topk(keys, N, k, list, P, lane);
+  // Selected samples in increasing sample order (the set of jax.random.choice; the
+  // order only fixes the row order of the appearance path, and the colour is summed in
+  // sample order as the reference's scatter into (R, N) does).
+  warp_topk(keys, N, k, list, P, lane, false);
   float ws = 0.f;
   for (int j = lane; j < k; j += 32) {
     const int i = entry_index(list[j]);

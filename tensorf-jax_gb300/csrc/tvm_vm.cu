@@ -79,6 +79,82 @@ __device__ __forceinline__ void vm_pair_scatter(float* __restrict__ glines, floa
   }
 }
 
+// Scatter of two samples' gradients for pair m (sample b optional): b's taps that land
+// on one of a's taps are added into a's values first, so a texel shared by consecutive
+// samples of a ray gets one reduction instead of two. (Consecutive samples of a ray are
+// less than one voxel apart at the configured sample counts, so most of their taps
+// coincide.)
+template <typename T, int CPL>
+__device__ __forceinline__ void vm_pair_scatter2(float* __restrict__ glines, float* __restrict__ gplanes, int G,
+                                                 int C, int m, int ch0, const PairEval<T, CPL>& a,
+                                                 const float (&ga)[CPL], bool has_b, const PairEval<T, CPL>& b,
+                                                 const float (&gb)[CPL]) {
+  float* lb = glines + (int64_t)m * G * C + ch0;
+  float* pb = gplanes + (int64_t)m * G * G * C + ch0;
+  float l0[CPL], l1[CPL];
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) {
+    l0[j] = ga[j] * a.P[j] * a.tl.w0;
+    l1[j] = ga[j] * a.P[j] * a.tl.w1;
+  }
+  const float wa[4] = {a.tr.w0 * a.tc.w0, a.tr.w0 * a.tc.w1, a.tr.w1 * a.tc.w0, a.tr.w1 * a.tc.w1};
+  const int ra[4] = {a.tr.i0, a.tr.i0, a.tr.i1, a.tr.i1};
+  const int ca[4] = {a.tc.i0, a.tc.i1, a.tc.i0, a.tc.i1};
+  float pv[4][CPL];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) pv[q][j] = ga[j] * a.L[j] * wa[q];
+  }
+  if (has_b) {
+    const int lidx[2] = {b.tl.i0, b.tl.i1};
+    const float lw[2] = {b.tl.w0, b.tl.w1};
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      float v[CPL];
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) v[j] = gb[j] * b.P[j] * lw[t];
+      if (lidx[t] == a.tl.i0) {
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) l0[j] += v[j];
+      } else if (lidx[t] == a.tl.i1) {
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) l1[j] += v[j];
+      } else {
+        red_chunk<CPL>(lb + (int64_t)lidx[t] * C, v);
+      }
+    }
+    const float wb[4] = {b.tr.w0 * b.tc.w0, b.tr.w0 * b.tc.w1, b.tr.w1 * b.tc.w0, b.tr.w1 * b.tc.w1};
+    const int rb[4] = {b.tr.i0, b.tr.i0, b.tr.i1, b.tr.i1};
+    const int cb[4] = {b.tc.i0, b.tc.i1, b.tc.i0, b.tc.i1};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      float v[CPL];
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) v[j] = gb[j] * b.L[j] * wb[t];
+      int hit = -1;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (hit < 0 && rb[t] == ra[q] && cb[t] == ca[q]) hit = q;
+      if (hit >= 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (q == hit) {
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) pv[q][j] += v[j];
+          }
+        }
+      } else {
+        red_chunk<CPL>(pb + ((int64_t)rb[t] * G + cb[t]) * C, v);
+      }
+    }
+  }
+  red_chunk<CPL>(lb + (int64_t)a.tl.i0 * C, l0);
+  red_chunk<CPL>(lb + (int64_t)a.tl.i1 * C, l1);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) red_chunk<CPL>(pb + ((int64_t)ra[q] * G + ca[q]) * C, pv[q]);
+}
+
 __device__ __forceinline__ unsigned quad_mask() { return 0xFu << (threadIdx.x & 28); }
 
 __device__ __forceinline__ float quad_sum(float v) {
@@ -214,6 +290,64 @@ __global__ void __launch_bounds__(256) density_bwd_kernel(const T* __restrict__ 
   }
 }
 
+template <typename T, int C>
+__global__ void __launch_bounds__(256) density_bwd2_kernel(const T* __restrict__ lines,
+                                                         const T* __restrict__ planes, int G,
+                                                         float* __restrict__ glines,
+                                                         float* __restrict__ gplanes,
+                                                         const float* __restrict__ origins,
+                                                         const float* __restrict__ dirs,
+                                                         int64_t total, SamplerArgs s,
+                                                         const float* __restrict__ gsum) {
+  // A quad owns samples 2p and 2p + 1 (consecutive along a ray unless 2p + 1 starts the
+  // next ray, which is still correct, only merges less).
+  constexpr int CPL = C / 4;
+  const int64_t pair = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  const int64_t sa = 2 * pair, sbi = sa + 1;
+  if (sa >= total) return;
+  const float gsa = __ldg(gsum + sa);
+  const float gsb = sbi < total ? __ldg(gsum + sbi) : 0.0f;
+  if (gsa == 0.0f && gsb == 0.0f) return;  // the whole quad agrees: nothing to scatter
+  float ua[3], ub[3];
+  {
+    const int64_t r = sa / s.N;
+    const int i = (int)(sa - r * s.N);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ua[a] = grid_coord(x[a], G);
+  }
+  const bool has_b = gsb != 0.0f;
+  if (has_b) {
+    const int64_t r = sbi / s.N;
+    const int i = (int)(sbi - r * s.N);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ub[a] = grid_coord(x[a], G);
+  }
+  float ga[CPL], gb[CPL];
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) {
+    ga[j] = gsa;
+    gb[j] = gsb;
+  }
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> ea, eb;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, ua[a], ua[b], ua[c], sub * CPL, ea);
+    if (has_b) vm_pair_eval<T, CPL>(lines, planes, G, C, m, ub[a], ub[b], ub[c], sub * CPL, eb);
+    vm_pair_scatter2<T, CPL>(glines, gplanes, G, C, m, sub * CPL, ea, ga, has_b, eb, gb);
+  }
+}
+
 // ---------------------------------------------------------------------------------
 // Fused appearance gather for the selected samples (render.py:472-486): row
 // m = r*k + j uses sample sel_idx[m] of ray r; X0[m] = 3C features, mode-major.
@@ -283,6 +417,64 @@ __global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict
 #pragma unroll
     for (int j = 0; j < CPL; ++j) gv[j] = __ldg(src + m * C + j);
     vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
+  }
+}
+
+template <typename T, int C>
+__global__ void __launch_bounds__(256) appearance_bwd2_kernel(const T* __restrict__ lines,
+                                                            const T* __restrict__ planes, int G,
+                                                            float* __restrict__ glines,
+                                                            float* __restrict__ gplanes,
+                                                            const float* __restrict__ origins,
+                                                            const float* __restrict__ dirs,
+                                                            int64_t rows, int k, SamplerArgs s,
+                                                            const int32_t* __restrict__ sel_idx,
+                                                            const float* __restrict__ dX0) {
+  // A quad owns rows 2p and 2p + 1: the selected samples of a ray are stored in
+  // increasing sample order, so consecutive rows are neighbours along the ray.
+  constexpr int CPL = C / 4;
+  const int64_t pair = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  const int64_t ra_ = 2 * pair, rb_ = ra_ + 1;
+  if (ra_ >= rows) return;
+  const bool has_b = rb_ < rows;
+  float ua[3], ub[3];
+  {
+    const int64_t r = ra_ / k;
+    const int i = __ldg(sel_idx + ra_);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ua[a] = grid_coord(x[a], G);
+  }
+  if (has_b) {
+    const int64_t r = rb_ / k;
+    const int i = __ldg(sel_idx + rb_);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ub[a] = grid_coord(x[a], G);
+  }
+  const float* srca = dX0 + ra_ * (3 * C) + sub * CPL;
+  const float* srcb = dX0 + rb_ * (3 * C) + sub * CPL;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PairEval<T, CPL> ea, eb;
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, ua[a], ua[b], ua[c], sub * CPL, ea);
+    float ga[CPL], gb[CPL];
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) {
+      ga[j] = __ldg(srca + m * C + j);
+      gb[j] = has_b ? __ldg(srcb + m * C + j) : 0.0f;
+    }
+    if (has_b) vm_pair_eval<T, CPL>(lines, planes, G, C, m, ub[a], ub[b], ub[c], sub * CPL, eb);
+    vm_pair_scatter2<T, CPL>(glines, gplanes, G, C, m, sub * CPL, ea, ga, has_b, eb, gb);
   }
 }
 
@@ -412,13 +604,24 @@ int launch_density_fwd(const FieldView& f, float shift, const float* origins, co
   return check_launch("density_fwd");
 }
 
+// Two samples per quad with merged reductions pay off when samples are dense along the
+// rays (512 uniform samples, 64 selected); with few samples per ray the single-sample
+// kernels keep more warps resident, which matters more.
+constexpr int kPairScatterMinSamples = 128;
+constexpr int kPairScatterMinSelected = 32;
+
 int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
                        const float* dirs, int64_t R, const SamplerArgs& s, const float* gsum,
                        cudaStream_t st) {
   const int64_t total = R * s.N;
   if (total == 0) return TVM_OK;
-  TVM_DISPATCH_FIELD(f, (density_bwd_kernel<TT, CC><<<quad_blocks(total), 256, 0, st>>>(
-                             L_, P_, f.G, glines, gplanes, origins, dirs, total, s, gsum)));
+  if (s.N >= kPairScatterMinSamples) {
+    TVM_DISPATCH_FIELD(f, (density_bwd2_kernel<TT, CC><<<quad_blocks((total + 1) / 2), 256, 0, st>>>(
+                               L_, P_, f.G, glines, gplanes, origins, dirs, total, s, gsum)));
+  } else {
+    TVM_DISPATCH_FIELD(f, (density_bwd_kernel<TT, CC><<<quad_blocks(total), 256, 0, st>>>(
+                               L_, P_, f.G, glines, gplanes, origins, dirs, total, s, gsum)));
+  }
   return check_launch("density_bwd");
 }
 
@@ -437,9 +640,13 @@ int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, con
                           const int32_t* sel_idx, int k, const float* dX0, cudaStream_t st) {
   const int64_t rows = R * k;
   if (rows == 0) return TVM_OK;
-  TVM_DISPATCH_FIELD(f, (appearance_bwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
-                             L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx,
-                             dX0)));
+  if (k >= kPairScatterMinSelected) {
+    TVM_DISPATCH_FIELD(f, (appearance_bwd2_kernel<TT, CC><<<quad_blocks((rows + 1) / 2), 256, 0, st>>>(
+                               L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx, dX0)));
+  } else {
+    TVM_DISPATCH_FIELD(f, (appearance_bwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
+                               L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx, dX0)));
+  }
   return check_launch("appearance_bwd");
 }
 
