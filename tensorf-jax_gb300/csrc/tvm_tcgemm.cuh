@@ -52,10 +52,15 @@ struct Stager {
   static constexpr int PER = (CHUNKS + THREADS - 1) / THREADS;
   float v[PER][EPC];
 
+  // KCONTIG: a warp covers 8 rows x 4 chunks, so each 16-byte shared store of the warp
+  // fills whole 128-byte core matrices (no bank conflicts) while each row still reads 64
+  // contiguous bytes of global memory. Otherwise consecutive lanes take consecutive rows.
+  static_assert(!KCONTIG || (R % 8 == 0 && KCH % 4 == 0), "row / chunk grouping");
   __device__ __forceinline__ static void chunk_rc(int c, int& r, int& kc) {
     if (KCONTIG) {
-      r = c / KCH;
-      kc = c % KCH;
+      const int grp = c >> 5, lane = c & 31;
+      r = 8 * (grp % (R / 8)) + (lane & 7);
+      kc = 4 * (grp / (R / 8)) + (lane >> 3);
     } else {
       kc = c / R;
       r = c % R;
