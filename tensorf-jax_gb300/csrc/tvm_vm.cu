@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) density_bwd_kernel(const T* __restrict__ 
 }
 
 template <typename T, int C>
-__global__ void __launch_bounds__(256) density_bwd2_kernel(const T* __restrict__ lines,
+__global__ void __launch_bounds__(256, 3) density_bwd2_kernel(const T* __restrict__ lines,
                                                          const T* __restrict__ planes, int G,
                                                          float* __restrict__ glines,
                                                          float* __restrict__ gplanes,
@@ -300,7 +300,8 @@ __global__ void __launch_bounds__(256) density_bwd2_kernel(const T* __restrict__
                                                          int64_t total, SamplerArgs s,
                                                          const float* __restrict__ gsum) {
   // A quad owns samples 2p and 2p + 1 (consecutive along a ray unless 2p + 1 starts the
-  // next ray, which is still correct, only merges less).
+  // next ray, which is still correct, only merges less). Capped at 80 registers for
+  // three resident blocks: the kernel waits on gathers, and the few spills cost less.
   constexpr int CPL = C / 4;
   const int64_t pair = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
   const int sub = threadIdx.x & 3;
