@@ -249,8 +249,7 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
     b.dX0 = ws.take<float>(M * F);
   }
   if (c.sampler == TVM_SAMPLER_PROPOSAL) {
-    const int64_t S = R * c.proposal_samples;
-    b.sig_p = ws.take<float>(S);
+      b.sig_p = ws.take<float>(S);
     b.delta_p = ws.take<float>(S);
     b.w_p = ws.take<float>(S);
     b.t_main = ws.take<float>(R * N);

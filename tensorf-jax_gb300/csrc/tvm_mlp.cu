@@ -84,14 +84,6 @@ struct EpiReluMask {
     }
   }
 };
-// out[m] = softplus(v + b + shift): the proposal density head (single column).
-struct EpiSoftplus {
-  float* out;
-  const float* bias;
-  float shift;
-  __device__ void operator()(int64_t m, int n, float v) const { out[m] = softplus_f(v + __ldg(bias) + shift); }
-  __device__ void vec4(int64_t m, int n, const float (&v)[4], int N) const { vec4_scalar(*this, m, n, v, N); }
-};
 struct EpiAtomic {
   float* C;
   int ldc;

@@ -28,7 +28,6 @@ constexpr int ENC = 150, ENCP = 160;   // encoded width, padded K of L1
 constexpr int U = 128;                 // hidden units
 constexpr int OUTP = 16;               // padded N of L3
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
-constexpr float kHalfPi = 1.57079632679489661923f;
 
 // Shared-memory map (bytes). SBO of a tile = (K / 8) * 128.
 constexpr int SBO_F = (F / 8) * 128, SBO_E = (ENCP / 8) * 128, SBO_U = (U / 8) * 128;

@@ -14,8 +14,9 @@
 //    proposal mass over the bins their interval overlaps,
 //    L = lambda/R * sum_i max(0, w_i - bound_i)^2 / (w_i + 1e-7), gradient into w^ only.
 //
-// The MLP layers run on the shared tensor-core GEMM (tvm_mlp.cu); these kernels are
-// the per-sample VM features and their scatter, the resampler and the loss.
+// The 16 -> U -> 1 MLP is evaluated inside the per-sample feature kernel. Its backward
+// runs fused with the field scatter: on tcgen05 for BF16 models with U = 64 (bf16
+// operands, as the rest of that mode), in FP32 SIMT otherwise.
 #include "tvm_internal.h"
 #include "tvm_tc.cuh"
 
@@ -23,7 +24,6 @@ namespace tvm {
 
 constexpr int PROP_C = 4;      // components per pair
 constexpr int PROP_IN = 16;    // MLP input width
-constexpr int PROP_MAXN = 512; // max proposal bins / main samples per ray
 
 // Bin edge j (0..Np) of a ray: t_min + j * step over its aabb segment (step = segment
 // length / Np, as the bounded sampler computes it), or the caller's edges.
@@ -90,8 +90,6 @@ __device__ __forceinline__ void prop_sample(const RayGeom& g, const SamplerArgs&
 // + b2 + shift). The weights sit in shared memory and every thread reads the same
 // element at the same time (broadcast). X and h are written only when the backward
 // needs them.
-constexpr int PROP_MAXU = 256;
-
 template <typename T>
 __global__ void __launch_bounds__(128) prop_features_kernel(
     const T* __restrict__ lines, const T* __restrict__ planes, int G, const float* __restrict__ origins,
