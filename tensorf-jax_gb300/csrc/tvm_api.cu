@@ -249,7 +249,8 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
     b.dX0 = ws.take<float>(M * F);
   }
   if (c.sampler == TVM_SAMPLER_PROPOSAL) {
-      b.sig_p = ws.take<float>(S);
+    const int64_t S = R * c.proposal_samples;
+    b.sig_p = ws.take<float>(S);
     b.delta_p = ws.take<float>(S);
     b.w_p = ws.take<float>(S);
     b.t_main = ws.take<float>(R * N);
@@ -310,7 +311,6 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   const bool proposal = c.sampler == TVM_SAMPLER_PROPOSAL;
   const SamplerArgs sp = proposal ? proposal_sampler(c) : SamplerArgs{};
   const float* edges = (proposal && c.contract) ? c.schedule : nullptr;
-  const int64_t S = R * c.proposal_samples;
   phase_mark(0, st);
   if (proposal) {
     // Proposal network forward, then resampling into explicit main samples.
