@@ -334,13 +334,17 @@ def algorithmic_bytes(w, phase):
     s = 2 if w["precision"] == "bf16" else 4
     dens_el, app_el = 18 * w["Cd"], 18 * w["Ca"]
     G = w["grid"]
-    n_params = 3 * G * (G + 1) * (w["Cd"] + w["Ca"]) + 40115
+    n_field = 3 * G * (G + 1) * (w["Cd"] + w["Ca"])
+    if w["prop_grid"]:
+        n_field += 3 * w["prop_grid"] * (w["prop_grid"] + 1) * 4
+    n_params = n_field + 40115
     return {
         "density_fwd": R * N * dens_el * s + R * N * 4,
         "density_bwd": R * N * dens_el * (s + 4) + R * N * 4,
         "appearance_fwd": R * k * app_el * s + R * k * 3 * w["Ca"] * 4,
         "appearance_bwd": R * k * app_el * (s + 4) + R * k * 3 * w["Ca"] * 4,
-        "adam": n_params * 32,
+        # p, g, m, v read; p, m, v, zeroed g written; plus the bf16 shadow of the field.
+        "adam": n_params * 32 + (n_field * 2 if w["precision"] == "bf16" else 0),
     }.get(phase)
 
 
