@@ -11,7 +11,7 @@
 // significant bits of every input: FP32-level accuracy on the tensor cores.
 //
 // Tile: 128 rows of D per CTA (one TMEM lane per row) and all N <= NT columns in one
-// TMEM accumulator; K in stages of 128 bytes per row. 256 threads stage; thread 0 issues
+// TMEM accumulator; K in stages of 64 (row-major A) or 128 bytes (transposed A) per row. 256 threads stage; thread 0 issues
 // the MMAs and commits to an mbarrier; the global loads of stage s+1 are issued into
 // registers before waiting for the MMAs of stage s. TMEM is read back by warps w and
 // w+4 (TMEM sub-partition w % 4), each half of the columns. Split-K over gridDim.z.
@@ -27,7 +27,7 @@ namespace tcg {
 
 constexpr int BM = 128;
 constexpr int THREADS = 256;
-constexpr int KCH = 8;           // 16-byte chunks per row per stage (128 bytes)
+constexpr int KCH = 8;           // default 16-byte chunks per row per stage (128 bytes)
 constexpr int PAD = 8192;        // slack after the operand tiles
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr int FMT_BF16 = 0, FMT_TF32 = 1;
@@ -45,17 +45,17 @@ __device__ __forceinline__ float ld1<__nv_bfloat16>(const __nv_bfloat16* p) { re
 // Loads one stage (rows [r0, r0+R) x k in [k0, k0 + 8*EPC)) of X into registers and
 // writes it to the canonical tile. X(r, k) = KCONTIG ? X[r*ld + k] : X[k*ld + r]; rows
 // >= rlim and k >= kend read as zero.
-template <int R, bool KCONTIG, typename T, int FMT>
+template <int R, bool KCONTIG, typename T, int FMT, int KC = KCH>
 struct Stager {
   static constexpr int EPC = epc(FMT);
-  static constexpr int CHUNKS = R * KCH;
+  static constexpr int CHUNKS = R * KC;
   static constexpr int PER = (CHUNKS + THREADS - 1) / THREADS;
   float v[PER][EPC];
 
   // KCONTIG: a warp covers 8 rows x 4 chunks, so each 16-byte shared store of the warp
   // fills whole 128-byte core matrices (no bank conflicts) while each row still reads 64
   // contiguous bytes of global memory. Otherwise consecutive lanes take consecutive rows.
-  static_assert(!KCONTIG || (R % 8 == 0 && KCH % 4 == 0), "row / chunk grouping");
+  static_assert(!KCONTIG || (R % 8 == 0 && KC % 4 == 0), "row / chunk grouping");
   __device__ __forceinline__ static void chunk_rc(int c, int& r, int& kc) {
     if (KCONTIG) {
       const int grp = c >> 5, lane = c & 31;
@@ -137,17 +137,17 @@ struct Stager {
           if (SPLIT) l[j] = tc::to_tf32(v[i][j] - __uint_as_float(h[j]));
         }
       }
-      const int off = (r >> 3) * (KCH * 128) + kc * 128 + (r & 7) * 16;
+      const int off = (r >> 3) * (KC * 128) + kc * 128 + (r & 7) * 16;
       *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
       if (SPLIT) *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
     }
   }
 };
 
-template <int NT, bool SPLIT>
+template <int NT, bool SPLIT, int KC = KCH>
 struct Smem {
-  static constexpr int A_BYTES = BM * KCH * 16;
-  static constexpr int B_BYTES = NT * KCH * 16;
+  static constexpr int A_BYTES = BM * KC * 16;
+  static constexpr int B_BYTES = NT * KC * 16;
   static constexpr int NPASS = SPLIT ? 2 : 1;
   static constexpr int TILES = NPASS * (A_BYTES + B_BYTES);
   static constexpr int TOTAL = TILES + PAD + 64;
@@ -158,17 +158,17 @@ struct Smem {
   static constexpr int BYTES = TOTAL > FLOOR ? TOTAL : FLOOR;
 };
 
-template <int NT, bool AT, bool BT, typename TA, typename TB, int FMT, bool SPLIT, class Epi>
+template <int NT, bool AT, bool BT, typename TA, typename TB, int FMT, bool SPLIT, class Epi, int KC>
 __global__ void __launch_bounds__(THREADS) tc_gemm_kernel(int64_t M, int N, int64_t K, const TA* __restrict__ A,
                                                         int64_t lda, const TB* __restrict__ B, int64_t ldb,
                                                         int64_t kc, Epi epi) {
-  using S = Smem<NT, SPLIT>;
+  using S = Smem<NT, SPLIT, KC>;
   constexpr int EPC = epc(FMT);
-  constexpr int BK = KCH * EPC;                 // K elements per stage
+  constexpr int BK = KC * EPC;                  // K elements per stage
   constexpr int KSTEP = (FMT == FMT_BF16) ? 16 : 8;
   constexpr uint32_t NCOLS = ncols_for(NT);
   constexpr uint32_t IDESC = tc::idesc(BM, NT, FMT == FMT_BF16 ? 1u : 2u);
-  constexpr uint32_t SBO = KCH * 128;  // next 8-row group
+  constexpr uint32_t SBO = KC * 128;   // next 8-row group
   constexpr uint32_t LBO = 128;        // next core matrix along K
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sB_hi = smem;
@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(THREADS) tc_gemm_kernel(int64_t M, int N, int6
 
   const TB* Bn = BT ? B + n0 * ldb : B + n0;  // this CTA's column block
   const int64_t nlim = (int64_t)N - n0;
-  Stager<BM, !AT, TA, FMT> sa;
-  Stager<NT, BT, TB, FMT> sb;
+  Stager<BM, !AT, TA, FMT, KC> sa;
+  Stager<NT, BT, TB, FMT, KC> sb;
   uint32_t phase = 0;
   int ok = 1;
   if (nst > 0) {
@@ -305,8 +305,11 @@ static int tc_gemm(int64_t M, int N, int64_t K, const TA* A, int64_t lda, const 
   const unsigned gz = (unsigned)ceil_div(K, kc);
   auto launch = [&](auto nt_tag) -> int {
     constexpr int NT = decltype(nt_tag)::value;
-    using S = tcg::Smem<NT, SPLIT>;
-    auto fn = tcg::tc_gemm_kernel<NT, AT, BT, TA, TB, FMT, SPLIT, Epi>;
+    // Row-major A streams 64-byte stages (smaller tiles, one more CTA per SM); the
+    // transposed-A weight-gradient products keep 128-byte stages.
+    constexpr int KC = AT ? 8 : 4;
+    using S = tcg::Smem<NT, SPLIT, KC>;
+    auto fn = tcg::tc_gemm_kernel<NT, AT, BT, TA, TB, FMT, SPLIT, Epi, KC>;
     static bool attr_done = false;  // per instantiation
     if (!attr_done) {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES);
