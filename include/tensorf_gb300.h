@@ -200,6 +200,15 @@ TVM_API int tvm_vm_to_channel_last(int32_t grid_dim, int32_t channels, const flo
 TVM_API int tvm_vm_to_channel_first(int32_t grid_dim, int32_t channels, const float* lines,
                             const float* planes, float* vector_cf, float* matrix_cf, void* stream);
 
+/* TensorVMSingle.resize (tensor_vm.py:182-198) for all three pairs of one tensor:
+ * float32 channel-last lines [3][old][C] / planes [3][old][old][C] -> [3][new][C] /
+ * [3][new][new][C], resampled like resize_with_aligned_corners (tensor_vm.py:202-223):
+ * jax.image.scale_and_translate, linear kernel, antialias, aligned corners. Used on the
+ * parameters and on both Adam moments when training upsamples the grid
+ * (TrainState.resize_grid, training.py:245-276). dst must not alias src. */
+TVM_API int tvm_resize_field(int32_t old_grid, int32_t new_grid, int32_t channels, const float* src_lines,
+                             const float* src_planes, float* dst_lines, float* dst_planes, void* stream);
+
 /* ---- (a) VM feature evaluation: TensorVM.interpolate (tensor_vm.py:42-89) --------- */
 /* coords (3, n) float32 in [-1, 1]; out (3C, n) float32, mode-major like the
  * reference. */

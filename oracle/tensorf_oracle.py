@@ -105,6 +105,54 @@ def vm_interpolate(vector: torch.Tensor, matrix: torch.Tensor, ijk: torch.Tensor
     return out.reshape((3 * vector.shape[1],) + tuple(batch))
 
 
+def scale_translate_weights(in_size: int, out_size: int, scale: float, translation: float,
+                            antialias: bool = True) -> onp.ndarray:
+    """Weight matrix (in, out) of jax.image.scale_and_translate with method="linear"
+    (triangle kernel), as resize_with_aligned_corners calls it (tensor_vm.py:202-223).
+    The algorithm is jax's published one (jax 0.9.0.1, uv.lock:529; not vendored under
+    the reference): output o samples input position f = (o + 0.5)/s - t/s - 0.5; weights
+    max(0, 1 - |f - i| / k) with k = max(1/s, 1) under antialias, normalised by their
+    sum (when that sum exceeds 1000 float32 eps), zero when f is outside
+    [-0.5, in - 0.5]. Float32 scalars, as under jax with x64 off."""
+    f32 = onp.float32
+    scale = f32(scale)
+    translation = f32(translation)
+    inv_scale = f32(1.0) / scale
+    kernel_scale = max(inv_scale, f32(1.0)) if antialias else f32(1.0)
+    sample_f = (onp.arange(out_size, dtype=f32) + f32(0.5)) * inv_scale - translation * inv_scale - f32(0.5)
+    x = onp.abs(sample_f[None, :] - onp.arange(in_size, dtype=f32)[:, None]) / kernel_scale
+    w = onp.maximum(f32(0.0), f32(1.0) - x)
+    tot = w.sum(axis=0, keepdims=True)
+    w = onp.where(onp.abs(tot) > 1000.0 * onp.finfo(onp.float32).eps, w / onp.where(tot != 0, tot, 1), 0.0)
+    valid = (sample_f >= -0.5) & (sample_f <= in_size - 0.5)
+    return onp.where(valid[None, :], w, 0.0).astype(onp.float64)
+
+
+def resize_with_aligned_corners(image: torch.Tensor, shape: Sequence[int]) -> torch.Tensor:
+    """resize_with_aligned_corners(image, shape, "linear", antialias=True)
+    (tensor_vm.py:202-223): scale (out - 1)/(in - 1) and translation -(scale/2 - 0.5) on
+    every axis whose size changes, contracted one axis after the other."""
+    out = image
+    for d in range(image.dim()):
+        m, n = image.shape[d], shape[d]
+        if m == n:
+            continue
+        sc = onp.float32((n - 1.0) / (m - 1.0))
+        tr = -(sc / onp.float32(2.0) - onp.float32(0.5))
+        w = torch.as_tensor(scale_translate_weights(m, n, float(sc), float(tr)), dtype=out.dtype)
+        out = torch.movedim(torch.tensordot(out, w, dims=([d], [0])), -1, d)
+    return out
+
+
+def vm_resize(vector: torch.Tensor, matrix: torch.Tensor, grid_dim: int) -> Tuple[torch.Tensor, torch.Tensor]:
+    """TensorVMSingle.resize vmapped over the three pairs (tensor_vm.py:91-100, 182-198):
+    vector (3, C, G) and matrix (3, C, G, G) to grid_dim."""
+    c = vector.shape[1]
+    v = torch.stack([resize_with_aligned_corners(vector[m], (c, grid_dim)) for m in range(3)])
+    mt = torch.stack([resize_with_aligned_corners(matrix[m], (c, grid_dim, grid_dim)) for m in range(3)])
+    return v, mt
+
+
 def vm_init(grid_dim: int, channels: int, gen: torch.Generator, dtype=torch.float64) -> Tuple[torch.Tensor, torch.Tensor]:
     """``TensorVM.initialize`` with N(0, 0.1^2) (tensor_vm.py:21-40, 116-138,
     training.py:44). Returns (vector (3,C,G), matrix (3,C,G,G)), channel-first."""

@@ -683,6 +683,16 @@ int tvm_loss_f64(const tvm_model_desc* model, const void* params, const tvm_rays
                          *cfg, static_cast<double*>(workspace), loss_out, as_stream(stream));
 }
 
+int tvm_resize_field(int32_t old_grid, int32_t new_grid, int32_t channels, const float* src_lines,
+                     const float* src_planes, float* dst_lines, float* dst_planes, void* stream) {
+  TVM_REQUIRE(old_grid >= 2 && old_grid <= 4096 && new_grid >= 2 && new_grid <= 4096, TVM_ERR_SHAPE,
+              "grid sizes %d -> %d outside [2, 4096]", old_grid, new_grid);
+  TVM_REQUIRE(channels >= 1 && channels <= 1024, TVM_ERR_SHAPE, "channels=%d outside [1, 1024]", channels);
+  TVM_REQUIRE(src_lines && src_planes && dst_lines && dst_planes, TVM_ERR_INVALID, "NULL pointer");
+  return launch_resize_field(old_grid, new_grid, channels, src_lines, src_planes, dst_lines, dst_planes,
+                             as_stream(stream));
+}
+
 int tvm_device_status(int32_t* out, void* stream) {
   TVM_REQUIRE(out != nullptr, TVM_ERR_INVALID, "out is NULL");
   return device_status(out, as_stream(stream));

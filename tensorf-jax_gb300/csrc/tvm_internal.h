@@ -35,6 +35,8 @@ int launch_points(const float* origins, const float* dirs, int64_t R, const Samp
                   float* points, float* ts, float* steps, cudaStream_t st);
 int launch_to_channel_last(int G, int C, const float* vec, const float* mat, int dtype, void* lines,
                            void* planes, cudaStream_t st);
+int launch_resize_field(int M, int N, int C, const float* src_lines, const float* src_planes, float* dst_lines,
+                        float* dst_planes, cudaStream_t st);
 int launch_to_channel_first(int G, int C, const float* lines, const float* planes, float* vec,
                             float* mat, cudaStream_t st);
 

@@ -660,6 +660,113 @@ int launch_points(const float* origins, const float* dirs, int64_t R, const Samp
   return check_launch("sample_points");
 }
 
+// ---------------------------------------------------------------------------------
+// Grid resize: TensorVMSingle.resize (tensor_vm.py:182-198) via
+// resize_with_aligned_corners (tensor_vm.py:202-223), i.e. jax.image.scale_and_translate
+// with the linear (triangle) kernel, antialias on, scale s = (N-1)/(M-1) and translation
+// 0.5 - s/2 on every resized axis. Output index o samples input position
+// f = (o + 0.5)/s - t/s - 0.5 = o (M-1)/(N-1); the weights max(0, 1 - |f - i| / k) with
+// k = max(1/s, 1) (wider only when downsampling) are normalised by their sum, and zero
+// when f lies outside [-0.5, M - 0.5]. Float32 arithmetic, as jax runs it.
+// ---------------------------------------------------------------------------------
+struct ResizeAxis {
+  int M;            // input size
+  float inv_scale;  // 1 / s
+  float tinv;       // translation / s
+  float kscale;     // kernel width
+};
+
+constexpr int RESIZE_MAXTAPS = 64;  // host rejects kernels wider than this
+
+__device__ int resize_taps(const ResizeAxis& ax, int o, int (&idx)[RESIZE_MAXTAPS], float (&w)[RESIZE_MAXTAPS]) {
+  const float f = ((float)o + 0.5f) * ax.inv_scale - ax.tinv - 0.5f;
+  if (!(f >= -0.5f && f <= (float)ax.M - 0.5f)) return 0;
+  int lo = (int)ceilf(f - ax.kscale), hi = (int)floorf(f + ax.kscale);
+  lo = max(lo, 0);
+  hi = min(hi, ax.M - 1);
+  int n = 0;
+  float tot = 0.f;
+  for (int i = lo; i <= hi && n < RESIZE_MAXTAPS; ++i) {
+    const float x = fabsf(f - (float)i) / ax.kscale;
+    const float wi = fmaxf(0.f, 1.f - x);
+    if (wi > 0.f) {
+      idx[n] = i;
+      w[n] = wi;
+      tot += wi;
+      ++n;
+    }
+  }
+  if (!(fabsf(tot) > 1000.f * 1.1920929e-7f)) return 0;
+  for (int k = 0; k < n; ++k) w[k] = w[k] / tot;
+  return n;
+}
+
+// lines [3][M][C] -> [3][N][C]; one thread per output (pair, position, channel).
+__global__ void resize_lines_kernel(const float* __restrict__ src, float* __restrict__ dst, int N, int C,
+                                    ResizeAxis ax) {
+  const int64_t total = 3LL * N * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e % C);
+    const int o = (int)((e / C) % N);
+    const int m = (int)(e / ((int64_t)C * N));
+    int idx[RESIZE_MAXTAPS];
+    float w[RESIZE_MAXTAPS];
+    const int n = resize_taps(ax, o, idx, w);
+    float acc = 0.f;
+    for (int k = 0; k < n; ++k) acc += w[k] * __ldg(src + ((int64_t)m * ax.M + idx[k]) * C + c);
+    dst[e] = acc;
+  }
+}
+
+// planes [3][M][M][C] -> [3][N][N][C], separable: rows first, then columns (the order
+// scale_and_translate contracts its spatial axes in).
+__global__ void resize_planes_kernel(const float* __restrict__ src, float* __restrict__ dst, int N, int C,
+                                     ResizeAxis ax) {
+  const int64_t total = 3LL * N * N * C;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e % C);
+    const int q = (int)((e / C) % N);
+    const int r = (int)((e / ((int64_t)C * N)) % N);
+    const int m = (int)(e / ((int64_t)C * N * N));
+    int ri[RESIZE_MAXTAPS], qi[RESIZE_MAXTAPS];
+    float rw[RESIZE_MAXTAPS], qw[RESIZE_MAXTAPS];
+    const int nr = resize_taps(ax, r, ri, rw);
+    const int nq = resize_taps(ax, q, qi, qw);
+    float acc = 0.f;
+    for (int b = 0; b < nq; ++b) {
+      float col = 0.f;
+      for (int a = 0; a < nr; ++a)
+        col += rw[a] * __ldg(src + (((int64_t)m * ax.M + ri[a]) * ax.M + qi[b]) * C + c);
+      acc += qw[b] * col;
+    }
+    dst[e] = acc;
+  }
+}
+
+int launch_resize_field(int M, int N, int C, const float* src_lines, const float* src_planes, float* dst_lines,
+                        float* dst_planes, cudaStream_t st) {
+  ResizeAxis ax;
+  ax.M = M;
+  // jax: scale = float32((N - 1) / (M - 1)), translation = -(scale / 2 - 0.5),
+  // inv_scale = 1 / scale, sample_f = (o + 0.5) * inv_scale - translation * inv_scale - 0.5.
+  const float scale = (float)((N - 1.0) / (M - 1.0));
+  const float translation = -(scale / 2.0f - 0.5f);
+  ax.inv_scale = 1.0f / scale;
+  ax.tinv = translation * ax.inv_scale;
+  ax.kscale = ax.inv_scale > 1.0f ? ax.inv_scale : 1.0f;
+  if (2.0f * ax.kscale + 2.0f > (float)RESIZE_MAXTAPS) {
+    set_error("resize from %d to %d: the antialiasing kernel spans more than %d taps", M, N, RESIZE_MAXTAPS);
+    return TVM_ERR_UNSUPPORTED;
+  }
+  const int64_t nl = 3LL * N * C, np = 3LL * N * N * C;
+  resize_lines_kernel<<<(unsigned)std::min<int64_t>(ceil_div(nl, 256), 152 * 16), 256, 0, st>>>(src_lines, dst_lines,
+                                                                                                N, C, ax);
+  TVM_TRY(check_launch("resize_lines"));
+  resize_planes_kernel<<<(unsigned)std::min<int64_t>(ceil_div(np, 256), 152 * 16), 256, 0, st>>>(src_planes,
+                                                                                                 dst_planes, N, C, ax);
+  return check_launch("resize_planes");
+}
+
 int launch_to_channel_last(int G, int C, const float* vec, const float* mat, int dtype, void* lines,
                            void* planes, cudaStream_t st) {
   const int64_t n = 3LL * G * C * (G + 1);

@@ -97,6 +97,7 @@ _SIGNATURES = {
     "tvm_loss_f64_workspace_size": (c_size_t, [POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
     "tvm_loss_f64": (c_int32, [POINTER(ModelDesc), c_void_p, POINTER(Rays), c_void_p, POINTER(RenderDesc), c_int64,
                                ctypes.c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tvm_resize_field": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tvm_gemm": (c_int32, [c_int32, c_int32, c_int32, c_int64, c_int32, c_int64, c_void_p, c_int64, c_void_p,
                            c_int64, c_void_p, c_int64, c_int32, c_void_p]),
     "tvm_device_status": (c_int32, [POINTER(c_int32), c_void_p]),

@@ -101,13 +101,12 @@ class LearnableParams:
         if params.numel() != self.layout.total or params.dtype != torch.float32 or not params.is_cuda:
             raise ValueError("params must be a CUDA float32 buffer of layout.total elements")
         self.params = params
-        if spec.precision == "bf16" and shadow is None:
-            shadow = torch.empty(self.layout.shadow_total, dtype=torch.bfloat16, device=params.device)
-            self._md = spec.desc()
-            self.refresh_shadow()
-        self.shadow = shadow
-        self.scene_contraction = scene_contraction
         self._md = spec.desc()
+        self.scene_contraction = scene_contraction
+        self.shadow = shadow
+        if spec.precision == "bf16" and shadow is None:
+            self.shadow = torch.empty(self.layout.shadow_total, dtype=torch.bfloat16, device=params.device)
+            self.refresh_shadow()
 
     # ---- views -----------------------------------------------------------------
     def model_desc(self) -> _lib.ModelDesc:

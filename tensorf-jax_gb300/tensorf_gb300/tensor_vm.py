@@ -103,6 +103,18 @@ class TensorVM:
         out = _Interpolate.apply(coords, self.lines, self.planes)
         return out.reshape((out.shape[0],) + tuple(batch))
 
+    def resize(self, grid_dim: int) -> "TensorVM":
+        """TensorVM.resize (tensor_vm.py:91-100): every pair resampled to grid_dim like
+        resize_with_aligned_corners (linear, antialias, aligned corners). float32."""
+        src_l = self.lines.float().contiguous()
+        src_p = self.planes.float().contiguous()
+        c = src_l.shape[-1]
+        lines = torch.empty((3, grid_dim, c), dtype=torch.float32, device=src_l.device)
+        planes = torch.empty((3, grid_dim, grid_dim, c), dtype=torch.float32, device=src_l.device)
+        _lib.call("tvm_resize_field", self.grid_dim(), grid_dim, c, ptr(src_l), ptr(src_p), ptr(lines), ptr(planes),
+                  stream_handle())
+        return TensorVM(lines, planes)
+
     def grid_dim(self) -> int:
         return int(self.planes.shape[1])
 

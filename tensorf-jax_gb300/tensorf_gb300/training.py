@@ -38,6 +38,8 @@ class TrainConfig:
     initial_aabb_min: Tuple[float, float, float] = (-1.0, -1.0, -1.0)
     initial_aabb_max: Tuple[float, float, float] = (1.0, 1.0, 1.0)
     upsamp_iters: Tuple[int, ...] = (2000, 3000, 4000, 5500, 7000)
+    grid_dim_init: int = 128   # train_config.py:54
+    grid_dim_final: int = 300  # train_config.py:55
     scene_contraction: bool = False
     # Plain contracted sampler: "reference" keeps render.py's heuristic schedule
     # (render.py:127-151), "disparity" spaces the samples linearly in disparity.
@@ -64,6 +66,15 @@ def lr_decay_coeff(step: int, cfg: TrainConfig) -> float:
         return 1.0
     v = float(onp.power(onp.float32(o.lr_decay_target_ratio), onp.float32(s) / onp.float32(di)))
     return max(v, o.lr_decay_target_ratio)
+
+
+def upsampled_grid_dim(cfg: TrainConfig, train_step: int) -> Optional[int]:
+    """The grid dimension training moves to at train_step, or None (training.py:358-367:
+    linear from grid_dim_init to grid_dim_final over the upsampling iterations)."""
+    if train_step not in cfg.upsamp_iters:
+        return None
+    index = cfg.upsamp_iters.index(train_step)
+    return int(cfg.grid_dim_init + (cfg.grid_dim_final - cfg.grid_dim_init) * ((index + 1) / len(cfg.upsamp_iters)))
 
 
 def sample_counts(grid_dim: int, cfg: TrainConfig) -> Tuple[int, int]:
@@ -97,6 +108,47 @@ class TrainState:
     def initialize(config: TrainConfig, spec: render.ModelSpec, seed: int = 94709) -> "TrainState":
         lp = render.LearnableParams.initialize(spec, seed=seed, scene_contraction=config.scene_contraction)
         return TrainState(config, lp, seed=seed)
+
+    def resize_grid(self, new_grid_dim: int) -> "TrainState":
+        """TrainState.resize_grid (training.py:245-276): both VM tensors and their Adam
+        moments resampled to new_grid_dim (tvm_resize_field), MLP and proposal network
+        parameters and moments carried over, gradients zero. The step count is kept; the
+        learning-rate decay restarts through upsamp_iters. Mutates and returns self."""
+        lp = self.learnable_params
+        old_g = lp.spec.grid_dim
+        new_spec = dataclasses.replace(lp.spec, grid_dim=int(new_grid_dim))
+        dev = lp.params.device
+        new_lp = render.LearnableParams(new_spec, torch.zeros(render.param_layout(new_spec).total,
+                                                               dtype=torch.float32, device=dev),
+                                        scene_contraction=lp.scene_contraction)
+
+        def transfer(src: torch.Tensor) -> torch.Tensor:
+            dst = torch.zeros(new_lp.layout.total, dtype=torch.float32, device=dev)
+            for which in ("density", "appearance"):
+                sl, sp = lp.field_views(which, src)
+                dl, dp = new_lp.field_views(which, dst)
+                _lib.call("tvm_resize_field", old_g, int(new_grid_dim), sl.shape[-1], ptr(sl), ptr(sp), ptr(dl),
+                          ptr(dp), stream_handle())
+            new_mlp = new_lp.mlp_views(dst)
+            for layer, tensors in lp.mlp_views(src).items():
+                for name, t in tensors.items():
+                    new_mlp[layer][name].copy_(t)
+            if new_spec.proposal_grid:
+                new_prop = new_lp.proposal_views(dst)
+                for name, t in lp.proposal_views(src).items():
+                    new_prop[name].copy_(t)
+            return dst
+
+        new_lp.params.copy_(transfer(lp.params))
+        new_lp.refresh_shadow()
+        self.mu = transfer(self.mu)
+        self.nu = transfer(self.nu)
+        self.grads = torch.zeros_like(new_lp.params)
+        self.learnable_params = new_lp
+        self.appearance_mlp = new_spec.mlp()
+        self._ws = None
+        self._ws_key = None
+        return self
 
     def render_config(self) -> render.RenderConfig:
         n, k = sample_counts(self.learnable_params.spec.grid_dim, self.config)

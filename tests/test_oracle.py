@@ -263,3 +263,48 @@ def test_resample_quantiles_follow_the_histogram():
     inside = ((t > 0.625) & (t < 0.75)).double().mean()
     assert inside > 0.95
     assert float(delta.sum()) == pytest.approx(1.0)
+
+
+def test_resize_upsampling_matches_torch_align_corners():
+    """resize_with_aligned_corners (tensor_vm.py:202-223) upsampling = bilinear
+    interpolation with aligned corners: pinned against torch's own implementation."""
+    gen = torch.Generator().manual_seed(4)
+    vec = torch.randn((6, 9), generator=gen, dtype=torch.float64)
+    mat = torch.randn((6, 9, 9), generator=gen, dtype=torch.float64)
+    for n in (9, 17, 23):
+        got_v = O.resize_with_aligned_corners(vec, (6, n))
+        got_m = O.resize_with_aligned_corners(mat, (6, n, n))
+        want_v = torch.nn.functional.interpolate(vec[None], size=n, mode="linear", align_corners=True)[0]
+        want_m = torch.nn.functional.interpolate(mat[None], size=(n, n), mode="bilinear", align_corners=True)[0]
+        # The sample positions are float32 under jax (x64 off): agreement to float32 rounding.
+        assert float((got_v - want_v).abs().max()) < 1e-5
+        assert float((got_m - want_m).abs().max()) < 1e-5
+
+
+def test_resize_downsampling_antialias_properties():
+    """Downsampling widens the triangle kernel (antialias): the weights of every output
+    sum to one, constants stay constant, and a ramp stays increasing and inside its range
+    (the wide, truncated kernels are not exact on a ramp)."""
+    import numpy as np
+    w = O.scale_translate_weights(40, 12, 11 / 39, -(11 / 39 / 2 - 0.5))
+    assert np.allclose(w.sum(axis=0), 1.0, atol=1e-6)
+    assert int((w > 0).sum(axis=0).max()) > 2  # wider than linear interpolation
+    ramp = torch.linspace(-1.0, 3.0, 40, dtype=torch.float64)[None]
+    out = O.resize_with_aligned_corners(ramp, (1, 12))[0]
+    want = torch.linspace(-1.0, 3.0, 12, dtype=torch.float64)
+    assert bool((out[1:] > out[:-1]).all())
+    assert float(out.min()) >= -1.0 and float(out.max()) <= 3.0
+    assert float((out[1:-1] - want[1:-1]).abs().max()) < 5e-3
+    const = torch.full((2, 40, 40), 0.7, dtype=torch.float64)
+    assert float((O.resize_with_aligned_corners(const, (2, 12, 12)) - 0.7).abs().max()) < 1e-6
+
+
+def test_upsampling_schedule():
+    """training.py:358-367: linear from grid_dim_init to grid_dim_final."""
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tensorf-jax_gb300"))
+    from tensorf_gb300 import training
+    cfg = training.TrainConfig()
+    dims = [training.upsampled_grid_dim(cfg, s) for s in cfg.upsamp_iters]
+    assert dims == [162, 196, 231, 265, 300]
+    assert training.upsampled_grid_dim(cfg, 2001) is None
