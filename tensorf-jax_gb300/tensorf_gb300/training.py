@@ -150,6 +150,30 @@ class TrainState:
         self._ws_key = None
         return self
 
+    def state_dict(self) -> dict:
+        """The training state in the reference's array layout, on the CPU: params, Adam mu
+        and nu as LearnableParams-shaped trees (density / appearance (vector (3,C,G),
+        matrix (3,C,G,G)), flax "mlp" tree, "proposal"), the step and the model spec. The
+        reference checkpoints the same TrainState fields through its experiment tooling
+        (training.py:351-356); torch.save / numpy can store this dict."""
+        lp = self.learnable_params
+        return {"spec": dataclasses.asdict(lp.spec), "scene_contraction": lp.scene_contraction, "step": self.step,
+                "aabb": self.aabb.clone(), "params": lp.to_reference(), "mu": lp.to_reference(self.mu),
+                "nu": lp.to_reference(self.nu), "prng_key": dataclasses.asdict(self.prng_key)}
+
+    @staticmethod
+    def from_state_dict(config: TrainConfig, state: dict) -> "TrainState":
+        """Inverse of state_dict(): device buffers rebuilt in this library's layout."""
+        spec = render.ModelSpec(**state["spec"])
+        lp = render.LearnableParams.from_reference(spec, state["params"], scene_contraction=state["scene_contraction"])
+        ts = TrainState(config, lp)
+        ts.mu = render.LearnableParams.from_reference(dataclasses.replace(spec, precision="fp32"), state["mu"]).params
+        ts.nu = render.LearnableParams.from_reference(dataclasses.replace(spec, precision="fp32"), state["nu"]).params
+        ts.step = int(state["step"])
+        ts.aabb = state["aabb"].clone()
+        ts.prng_key = render.NoiseKey(**state["prng_key"])
+        return ts
+
     def render_config(self) -> render.RenderConfig:
         n, k = sample_counts(self.learnable_params.spec.grid_dim, self.config)
         return render.RenderConfig(near=self.config.render_near, far=self.config.render_far,
