@@ -330,12 +330,13 @@ static int tc_gemm(int64_t M, int N, int64_t K, const TA* A, int64_t lda, const 
   return launch(std::integral_constant<int, 256>{});
 }
 
-// Split-K chunk for a K-long reduction onto an M x N output: enough CTAs for two
-// waves of the 152 SMs at two CTAs each.
+// Split-K chunk for a K-long reduction onto an M x N output: one resident wave (152 SMs
+// x 3 CTAs) of equal chunks, so no SM runs a tail wave and each CTA adds its partial
+// tile to global memory once.
 static inline int64_t splitk_chunk(int64_t M, int64_t K) {
   const int64_t mtiles = ceil_div(M, 128);
-  const int64_t want = std::max<int64_t>(1, 608 / mtiles);
-  return std::max<int64_t>(512, round_up(ceil_div(K, want), 256));
+  const int64_t want = std::max<int64_t>(1, 456 / mtiles);
+  return std::max<int64_t>(256, round_up(ceil_div(K, want), 32));
 }
 
 }  // namespace tvm
