@@ -162,6 +162,14 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
       *reinterpret_cast<uint4*>(smem + OFF_A0 + coff(r, kc, SBO_F)) =
           make_uint4(pack2(p.x, p.y), pack2(p.z, p.w), pack2(q.x, q.y), pack2(q.z, q.w));
     }
+    {  // the next tile's features travel to L2 while this tile computes
+      const int64_t nm0 = (tile + gridDim.x) * BM;
+      if (nm0 < a.M) {
+        const int64_t nbytes = (a.M - nm0 < BM ? a.M - nm0 : BM) * F * 4;
+        for (int64_t off = (int64_t)tid * 128; off < nbytes; off += THREADS * 128)
+          tc::prefetch_l2(reinterpret_cast<const char*>(a.X0 + nm0 * F) + off);
+      }
+    }
     if (!layer(D0, OFF_A0, OFF_W0, F / 16, SBO_F, SBO_F, SQP)) { ok = 0; break; }
 
     // Fourier encoding (networks.py:13-35, 68-76), row r = 32*sub + lane. X1 columns:
@@ -227,16 +235,21 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
     // Hidden layers: +bias, ReLU, bf16 into the next A tile.
     auto hidden = [&](uint32_t Dsrc, const float* bias, int dst_off) {
       const int r = sub * 32 + lane;
-      for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
-        float v[16];
-        tc::tmem_ld16(Dsrc + lane_off + ch * 16, v);
+      for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
+        float vv[2][16];
+        tc::tmem_ld16x2(Dsrc + lane_off + cp * 16, Dsrc + lane_off + (cp + 1) * 16, vv[0], vv[1]);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
+        for (int u = 0; u < 2; ++u) {
+          const int ch = cp + u;
+          float* v = vv[u];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          *reinterpret_cast<uint4*>(smem + dst_off + coff(r, ch * 2 + q, SBO_U)) =
-              make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
-                         pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+          for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            *reinterpret_cast<uint4*>(smem + dst_off + coff(r, ch * 2 + q, SBO_U)) =
+                make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                           pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+          }
         }
       }
     };
@@ -449,24 +462,33 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
   };
   // +bias, ReLU, bf16 into a natural tile.
   auto hidden = [&](const float* bias, int dst, int sbo) {
-    for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
-      float v[16];
-      tc::tmem_ld16(tmem + T_CH + lane_off + ch * 16, v);
+    for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
+      float vv[2][16];
+      tc::tmem_ld16x2(tmem + T_CH + lane_off + cp * 16, tmem + T_CH + lane_off + (cp + 1) * 16, vv[0], vv[1]);
 #pragma unroll
-      for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
+      for (int u = 0; u < 2; ++u) {
+        const int ch = cp + u;
+        float* v = vv[u];
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        *reinterpret_cast<uint4*>(smem + dst + coff(r, ch * 2 + q, sbo)) =
-            make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
-                       pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          *reinterpret_cast<uint4*>(smem + dst + coff(r, ch * 2 + q, sbo)) =
+              make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                         pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
+        }
       }
     }
   };
   // dH = D * [H > 0], written over H in place (H's tile is no longer read by any MMA).
   auto relu_bwd = [&](int reg, int sbo) {
-    for (int ch = half * 4; ch < half * 4 + 4; ++ch) {
-      float v[16];
-      tc::tmem_ld16(tmem + T_CH + lane_off + ch * 16, v);
+    for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
+      float vv[2][16];
+      tc::tmem_ld16x2(tmem + T_CH + lane_off + cp * 16, tmem + T_CH + lane_off + (cp + 1) * 16, vv[0], vv[1]);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+      const int ch = cp + u;
+      float* v = vv[u];
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         uint4* p = reinterpret_cast<uint4*>(smem + reg + coff(r, ch * 2 + q, sbo));
@@ -479,6 +501,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
           o[e] = pack2(f.x > 0.f ? v[8 * q + 2 * e] : 0.f, f.y > 0.f ? v[8 * q + 2 * e + 1] : 0.f);
         }
         *p = make_uint4(o[0], o[1], o[2], o[3]);
+      }
       }
     }
   };
@@ -500,6 +523,15 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
       }
       *reinterpret_cast<uint4*>(smem + RD + coff(tid, 0, SBO_Z)) = make_uint4(pack2(z0, z1), pack2(z2, 0.f), 0u, 0u);
       *reinterpret_cast<uint4*>(smem + RD + coff(tid, 1, SBO_Z)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    {  // the next tile's features and output gradients travel to L2 meanwhile
+      const int64_t nm0 = (tile + gridDim.x) * BM;
+      if (nm0 < a.M) {
+        const int64_t nrows = a.M - nm0 < BM ? a.M - nm0 : BM;
+        for (int64_t off = (int64_t)tid * 128; off < nrows * F * 4; off += THREADS * 128)
+          tc::prefetch_l2(reinterpret_cast<const char*>(a.X0 + nm0 * F) + off);
+        if (tid * 128 < nrows * 12) tc::prefetch_l2(reinterpret_cast<const char*>(a.dZ3 + nm0 * 3) + tid * 128);
+      }
     }
     // L0: h = X0 W0.
     if (!run([&] { mma_run(tmem + T_CH, kmaj(sb + RA, SBO_A), kmaj(sb + OFF_W0, SBO_F), F / 16,
