@@ -15,6 +15,7 @@
 
 #include "tvm_internal.h"
 #include "tvm_tcgemm.cuh"
+#include "tvm_pgemm.cuh"
 
 namespace tvm {
 
@@ -289,15 +290,193 @@ __global__ void sigmoid_bwd_kernel(const float* __restrict__ rgb, const float* _
 
 static int ld_x1(const MlpDims& d) { return (int)round_up(d.enc, 4); }
 
+// ---------------------------------------------------------------------------------
+// FP32 (split-tf32) path on the persistent pipelined GEMM (tvm_pgemm.cuh), for the
+// reference FeatureMlp widths: 27 squash features, 2 encoding frequencies for features
+// and directions (encoded width 150), 128 hidden units.
+//
+//   forward:  X1 = [H0, d, PE(H0), PE(d)] with H0 = X0 W0      (L0 GEMM, encoding in its epilogue)
+//             H1 = relu(X1 W1 + b1)                              (L1 GEMM)
+//             H2 = relu(H1 W2 + b2), rgb = sigmoid(H2 W3 + b3)   (L2 GEMM, layer 3 in its epilogue)
+//   backward: dH2, dW3, db3, db2 from H2 and dZ3                 (l3_bwd_kernel, one pass)
+//             dH1 = (dH2 W2^T) * [H1 > 0], db1 = colsum dH1      (GEMM, mask + column sums in its epilogue)
+//             dH0 = PE^T(dH1 W1^T)                               (GEMM, encoding backward in its epilogue)
+//             dX0 = dH0 W0^T                                     (GEMM)
+//             dW2 = H1^T dH2, dW1 = X1^T dH1, dW0 = X0^T dH0     (split-K tc_gemm)
+// ---------------------------------------------------------------------------------
+static bool pmlp_supported(const MlpDims& d) {
+  return d.math == 1 && d.squash == pg::SQ && d.enc == pg::ENC && d.nf == 2 && d.nv == 2 && d.units == 128 &&
+         d.feat % 4 == 0 && d.feat >= 4 && d.feat <= 160;
+}
+static int pmlp_nt_dx0(const MlpDims& d) { return d.feat <= 64 ? 64 : 160; }
+
+// Byte sizes of the six packed weight images (forward: L0, L1, L2; backward: dH1, dX1, dX0).
+struct PmlpImages {
+  int bytes[6];
+  int total() const { return bytes[0] + bytes[1] + bytes[2] + bytes[3] + bytes[4] + bytes[5]; }
+};
+static PmlpImages pmlp_images(const MlpDims& d) {
+  PmlpImages im;
+  im.bytes[0] = pg::image_bytes(d.feat, 32);
+  im.bytes[1] = pg::image_bytes(pg::LDX1, 128);
+  im.bytes[2] = pg::image_bytes(128, 128);
+  im.bytes[3] = pg::image_bytes(128, 128);
+  im.bytes[4] = pg::image_bytes(128, 160);
+  im.bytes[5] = pg::image_bytes(pg::LDH0, pmlp_nt_dx0(d));
+  return im;
+}
+
+static int num_sms() {
+  static int cached[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cached[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cached[dev] = n > 0 ? n : 1;
+  }
+  return cached[dev];
+}
+
+static int pack_images(const pg::PackJob* jobs, int count, cudaStream_t st) {
+  pg::PackList list{};
+  int most = 0;
+  for (int i = 0; i < count; ++i) {
+    list.job[i] = jobs[i];
+    most = std::max(most, jobs[i].kp * jobs[i].np);
+  }
+  list.count = count;
+  dim3 grid((unsigned)ceil_div(most, 256), (unsigned)count);
+  pg::pack_kernel<<<grid, 256, 0, st>>>(list);
+  return check_launch("pgemm pack");
+}
+
+template <int KIND, int NT>
+static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uint8_t* bimg, const pg::EpiArgs& ea,
+                 cudaStream_t st) {
+  if (M == 0) return TVM_OK;
+  TVM_REQUIRE(K % 4 == 0 && aligned(bimg, 16) && N <= NT &&
+                  ((KIND != pg::EPI_BIAS_RELU && KIND != pg::EPI_BIAS_RELU_L3 && KIND != pg::EPI_MASK_COLSUM) ||
+                   N == NT),
+              TVM_ERR_INVALID, "pgemm: unsupported operands (K=%d, lda=%lld, N=%d)", K, (long long)lda, N);
+  constexpr int EF = pg::epi_smem_floats<KIND, NT>();
+  const int base = pg::smem_base_bytes<NT>(K, EF);
+  const int slots = std::min(pg::MAX_SLOTS, (pg::SMEM_LIMIT - base) / pg::SLOT_BYTES);
+  TVM_REQUIRE(slots >= 2, TVM_ERR_UNSUPPORTED, "pgemm: K=%d, N=%d leaves %d pipeline slots", K, NT, slots);
+  const int bytes = std::max(base + slots * pg::SLOT_BYTES, pg::MIN_SMEM);
+  auto fn = pg::pgemm_kernel<KIND, NT>;
+  static bool attr_done = false;  // per instantiation
+  if (!attr_done) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::SMEM_LIMIT);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pgemm smem attribute: %s", cudaGetErrorString(e));
+    attr_done = true;
+  }
+  const int64_t tiles = ceil_div(M, pg::BM);
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
+  fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, A, lda, bimg, slots, ea);
+  return check_launch("pgemm");
+}
+
+// Layer 3 of the backward in one pass over H2 (networks.py:112-121, sigmoid folded
+// into dZ3): dH2 = (dZ3 W3^T) * [H2 > 0], dW3 += H2^T dZ3, db3 += sum dZ3,
+// db2 += sum dH2. A warp takes four consecutive rows at a time (grid-stride), lane l
+// columns 4l..4l+3 of the 128 units; partial sums stay in registers, are reduced
+// over the block in shared memory and added once per block.
+constexpr int L3_THREADS = 512;
+__global__ void __launch_bounds__(L3_THREADS) l3_bwd_kernel(int64_t M, const float* __restrict__ H2,
+                                                           const float* __restrict__ dZ3,
+                                                           const float* __restrict__ W3, float* __restrict__ dH2,
+                                                           float* __restrict__ gW3, float* __restrict__ gb3,
+                                                           float* __restrict__ gb2) {
+  __shared__ float sW[128 * 3], sB2[128], sB3[4];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < 128 * 3; i += L3_THREADS) sW[i] = 0.0f;
+  if (tid < 128) sB2[tid] = 0.0f;
+  if (tid < 4) sB3[tid] = 0.0f;
+  float w[4][3], aw[4][3], ab2[4], ab3[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    ab2[c] = 0.0f;
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      w[c][o] = __ldg(W3 + (4 * lane + c) * 3 + o);
+      aw[c][o] = 0.0f;
+    }
+  }
+  __syncthreads();
+  const int64_t nwarps = (int64_t)gridDim.x * (L3_THREADS / 32);
+  for (int64_t m0 = ((int64_t)blockIdx.x * (L3_THREADS / 32) + warp) * 4; m0 < M; m0 += nwarps * 4) {
+    float4 h[4];
+    float z[4][3];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t m = m0 + r;
+      if (m < M) {
+        h[r] = __ldg(reinterpret_cast<const float4*>(H2 + m * 128) + lane);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) z[r][o] = __ldg(dZ3 + m * 3 + o);
+      } else {
+        h[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) z[r][o] = 0.0f;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float hv[4] = {h[r].x, h[r].y, h[r].z, h[r].w};
+      float dv[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float g = z[r][0] * w[c][0] + z[r][1] * w[c][1] + z[r][2] * w[c][2];
+        dv[c] = hv[c] > 0.0f ? g : 0.0f;
+        ab2[c] += dv[c];
+#pragma unroll
+        for (int o = 0; o < 3; ++o) aw[c][o] = fmaf(hv[c], z[r][o], aw[c][o]);
+      }
+#pragma unroll
+      for (int o = 0; o < 3; ++o) ab3[o] += z[r][o];
+      if (m0 + r < M)
+        *reinterpret_cast<float4*>(dH2 + (m0 + r) * 128 + 4 * lane) = make_float4(dv[0], dv[1], dv[2], dv[3]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    atomicAdd(&sB2[4 * lane + c], ab2[c]);
+#pragma unroll
+    for (int o = 0; o < 3; ++o) atomicAdd(&sW[(4 * lane + c) * 3 + o], aw[c][o]);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int o = 0; o < 3; ++o) atomicAdd(&sB3[o], ab3[o]);
+  }
+  __syncthreads();
+  for (int i = tid; i < 128 * 3; i += L3_THREADS) atomicAdd(gW3 + i, sW[i]);
+  if (tid < 128) atomicAdd(gb2 + tid, sB2[tid]);
+  if (tid < 3) atomicAdd(gb3 + tid, sB3[tid]);
+}
+
 // Workspace carve-out shared by forward and backward (same order).
 struct MlpBufs {
   float *X1, *H1, *H2, *dH2, *dH1, *dX1, *dH0;
   uint8_t* wpack;
+  uint8_t* img[6];
 };
 static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   MlpBufs b{};
   if (mlp_fused_supported(d)) {  // the fused kernels keep every activation on chip
     b.wpack = ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes());
+    return b;
+  }
+  if (pmlp_supported(d)) {
+    const PmlpImages im = pmlp_images(d);
+    for (int i = 0; i < 6; ++i) b.img[i] = ws.take<uint8_t>(im.bytes[i]);
+    b.X1 = ws.take<float>(M * pg::LDX1);
+    b.H1 = ws.take<float>(M * 128);
+    b.H2 = ws.take<float>(M * 128);
+    b.dH2 = ws.take<float>(M * 128);
+    b.dH1 = ws.take<float>(M * 128);
+    b.dH0 = ws.take<float>(M * pg::LDH0);
     return b;
   }
   b.X1 = ws.take<float>(M * ld_x1(d));
@@ -330,6 +509,31 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
     // which recomputes the activations from X0 (only the packed weights are reused).
     return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st);
   }
+  if (pmlp_supported(d)) {
+    const pg::PackJob jobs[3] = {{w.w0, d.squash, d.feat, d.squash, pg::kpad(d.feat), 32, 0, b.img[0]},
+                                 {w.w1, 128, d.enc, 128, pg::kpad(pg::LDX1), 128, 0, b.img[1]},
+                                 {w.w2, 128, 128, 128, 128, 128, 0, b.img[2]}};
+    TVM_TRY(pack_images(jobs, 3, st));
+    pg::EpiArgs e0{};
+    e0.out = b.X1;
+    e0.ldo = pg::LDX1;
+    e0.dirs = dirs;
+    e0.rows_per_dir = rows_per_dir;
+    TVM_TRY((pgemm<pg::EPI_PE_FWD, 32>(M, d.squash, d.feat, X0, d.feat, b.img[0], e0, st)));
+    pg::EpiArgs e1{};
+    e1.out = b.H1;
+    e1.ldo = 128;
+    e1.bias = w.b1;
+    TVM_TRY((pgemm<pg::EPI_BIAS_RELU, 128>(M, 128, pg::LDX1, b.X1, pg::LDX1, b.img[1], e1, st)));
+    pg::EpiArgs e2{};
+    e2.out = b.H2;
+    e2.ldo = 128;
+    e2.bias = w.b2;
+    e2.w3 = w.w3;
+    e2.b3 = w.b3;
+    e2.rgb = rgb;
+    return pgemm<pg::EPI_BIAS_RELU_L3, 128>(M, 128, 128, b.H1, 128, b.img[2], e2, st);
+  }
   TVM_TRY((mm<false, false>(d.math, M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, l1}, st)));
   pe_fwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.X1, l1, M, d.squash, d.enc, d.nf, d.nv, dirs,
                                                                  rows_per_dir);
@@ -354,6 +558,45 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
   }
   const int l1 = ld_x1(d);
   const int64_t kc = -1;  // weight gradients: split-K over the rows, sized per GEMM
+  if (pmlp_supported(d)) {
+    const int ntx = pmlp_nt_dx0(d);
+    const pg::PackJob jobs[3] = {{w.w2, 128, 128, 128, 128, 128, 1, b.img[3]},
+                                 {w.w1, 128, 128, d.enc, 128, 160, 1, b.img[4]},
+                                 {w.w0, d.squash, d.squash, d.feat, pg::kpad(pg::LDH0), ntx, 1, b.img[5]}};
+    TVM_TRY(pack_images(jobs, 3, st));
+    if (M > 0) {
+      const unsigned blocks = (unsigned)std::min<int64_t>(2 * num_sms(), ceil_div(M, 4 * (L3_THREADS / 32)));
+      l3_bwd_kernel<<<blocks, L3_THREADS, 0, st>>>(M, b.H2, dZ3, w.w3, b.dH2, g.w3, g.b3, g.b2);
+      TVM_TRY(check_launch("l3_bwd"));
+    }
+    pg::EpiArgs e1{};
+    e1.out = b.dH1;
+    e1.ldo = 128;
+    e1.H = b.H1;
+    e1.ldh = 128;
+    e1.colsum = g.b1;
+    TVM_TRY((pgemm<pg::EPI_MASK_COLSUM, 128>(M, 128, 128, b.dH2, 128, b.img[3], e1, st)));
+    TVM_TRY((mm<true, false>(d.math, 128, 128, M, b.H1, 128, b.dH2, 128, EpiAtomic{g.w2, 128}, st, kc)));
+    pg::EpiArgs e0{};
+    e0.out = b.dH0;
+    e0.H = b.X1;
+    e0.ldh = pg::LDX1;
+    TVM_TRY((pgemm<pg::EPI_PE_BWD, 160>(M, d.enc, 128, b.dH1, 128, b.img[4], e0, st)));
+    TVM_TRY((mm<true, false>(d.math, d.enc, 128, M, b.X1, pg::LDX1, b.dH1, 128, EpiAtomic{g.w1, 128}, st, kc)));
+    TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, pg::LDH0, EpiAtomic{g.w0, d.squash},
+                             st, kc)));
+    if (dX0) {
+      pg::EpiArgs ex{};
+      ex.out = dX0;
+      ex.ldo = d.feat;
+      if (ntx == 64) {
+        TVM_TRY((pgemm<pg::EPI_STORE, 64>(M, d.feat, pg::LDH0, b.dH0, pg::LDH0, b.img[5], ex, st)));
+      } else {
+        TVM_TRY((pgemm<pg::EPI_STORE, 160>(M, d.feat, pg::LDH0, b.dH0, pg::LDH0, b.img[5], ex, st)));
+      }
+    }
+    return TVM_OK;
+  }
   {
     // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
     TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
