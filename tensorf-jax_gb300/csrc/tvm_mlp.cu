@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <type_traits>
 
+#include <cudaTypedefs.h>
+
 #include "tvm_internal.h"
 #include "tvm_tcgemm.cuh"
 #include "tvm_pgemm.cuh"
@@ -308,7 +310,8 @@ static bool pmlp_supported(const MlpDims& d) {
   return d.math == 1 && d.squash == pg::SQ && d.enc == pg::ENC && d.nf == 2 && d.nv == 2 && d.units == 128 &&
          d.feat % 4 == 0 && d.feat >= 4 && d.feat <= 160;
 }
-static int pmlp_nt_dx0(const MlpDims& d) { return d.feat <= 64 ? 64 : 160; }
+static int pmlp_nt_dx0(const MlpDims& d) { return d.feat <= 64 ? 64 : d.feat <= 144 ? 144 : 160; }
+constexpr int PMLP_NT_DX1 = 144;  // dX1 columns the encoding backward reads: [h | d | PE(h)] = 138
 
 // Byte sizes of the six packed weight images (forward: L0, L1, L2; backward: dH1, dX1, dX0).
 struct PmlpImages {
@@ -318,11 +321,11 @@ struct PmlpImages {
 static PmlpImages pmlp_images(const MlpDims& d) {
   PmlpImages im;
   im.bytes[0] = pg::image_bytes(d.feat, 32);
-  im.bytes[1] = pg::image_bytes(pg::LDX1, 128);
+  im.bytes[1] = pg::image_bytes(pg::ENC, 128);
   im.bytes[2] = pg::image_bytes(128, 128);
   im.bytes[3] = pg::image_bytes(128, 128);
-  im.bytes[4] = pg::image_bytes(128, 160);
-  im.bytes[5] = pg::image_bytes(pg::LDH0, pmlp_nt_dx0(d));
+  im.bytes[4] = pg::image_bytes(128, PMLP_NT_DX1);
+  im.bytes[5] = pg::image_bytes(pg::SQ, pmlp_nt_dx0(d));
   return im;
 }
 
@@ -352,14 +355,55 @@ static int pack_images(const pg::PackJob* jobs, int count, cudaStream_t st) {
   return check_launch("pgemm pack");
 }
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// Row-major fp32 matrix (cols wide, rows high, row pitch ld elements) as a 2-D tensor map
+// with a box of bx columns x by rows; reads past the edges return zero.
+static int make_map(CUtensorMap* m, const float* base, int64_t cols, int64_t rows, int64_t ld, int bx, int by) {
+  auto enc = tensor_map_encoder();
+  TVM_REQUIRE(enc != nullptr, TVM_ERR_LAUNCH, "cuTensorMapEncodeTiled is unavailable");
+  TVM_REQUIRE(aligned(base, 16) && (ld * 4) % 16 == 0 && cols > 0 && rows > 0, TVM_ERR_ALIGN,
+              "tensor map: base %p / pitch %lld not 16-byte aligned", (const void*)base, (long long)(ld * 4));
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)(ld * 4)};
+  const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  TVM_REQUIRE(r == CUDA_SUCCESS, TVM_ERR_LAUNCH, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return TVM_OK;
+}
+
+// ocols: the output width the TMA-stored epilogues write (ea.out with row pitch ea.ldo).
 template <int KIND, int NT>
 static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uint8_t* bimg, const pg::EpiArgs& ea,
-                 cudaStream_t st) {
+                 cudaStream_t st, int ocols = 0) {
   if (M == 0) return TVM_OK;
-  TVM_REQUIRE(K % 4 == 0 && aligned(bimg, 16) && N <= NT &&
+  constexpr bool tma_out = KIND == pg::EPI_BIAS_RELU || KIND == pg::EPI_BIAS_RELU_L3 ||
+                           KIND == pg::EPI_MASK_COLSUM || KIND == pg::EPI_PE_FWD;
+  TVM_REQUIRE(aligned(bimg, 16) && N <= NT && K > 0 && M <= INT32_MAX &&
                   ((KIND != pg::EPI_BIAS_RELU && KIND != pg::EPI_BIAS_RELU_L3 && KIND != pg::EPI_MASK_COLSUM) ||
                    N == NT),
               TVM_ERR_INVALID, "pgemm: unsupported operands (K=%d, lda=%lld, N=%d)", K, (long long)lda, N);
+  CUtensorMap tmA, tmO;
+  TVM_TRY(make_map(&tmA, A, K, M, lda, 4, pg::BM));
+  if (tma_out) {
+    TVM_TRY(make_map(&tmO, ea.out, ocols > 0 ? ocols : N, M, ea.ldo, pg::OUT_BOX_COLS, pg::OUT_BOX_ROWS));
+  } else {
+    tmO = tmA;
+  }
   constexpr int EF = pg::epi_smem_floats<KIND, NT>();
   const int base = pg::smem_base_bytes<NT>(K, EF);
   const int slots = std::min(pg::MAX_SLOTS, (pg::SMEM_LIMIT - base) / pg::SLOT_BYTES);
@@ -374,7 +418,7 @@ static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uin
   }
   const int64_t tiles = ceil_div(M, pg::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
-  fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, A, lda, bimg, slots, ea);
+  fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, tmA, tmO, bimg, slots, ea);
   return check_launch("pgemm");
 }
 
@@ -511,20 +555,28 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
   }
   if (pmlp_supported(d)) {
     const pg::PackJob jobs[3] = {{w.w0, d.squash, d.feat, d.squash, pg::kpad(d.feat), 32, 0, b.img[0]},
-                                 {w.w1, 128, d.enc, 128, pg::kpad(pg::LDX1), 128, 0, b.img[1]},
+                                 {w.w1, 128, d.enc, 128, pg::kpad(pg::ENC), 128, 0, b.img[1]},
                                  {w.w2, 128, 128, 128, 128, 128, 0, b.img[2]}};
     TVM_TRY(pack_images(jobs, 3, st));
-    pg::EpiArgs e0{};
-    e0.out = b.X1;
-    e0.ldo = pg::LDX1;
-    e0.dirs = dirs;
-    e0.rows_per_dir = rows_per_dir;
-    TVM_TRY((pgemm<pg::EPI_PE_FWD, 32>(M, d.squash, d.feat, X0, d.feat, b.img[0], e0, st)));
+    if (aligned(X0, 16) && d.feat % 4 == 0) {
+      pg::EpiArgs e0{};
+      e0.out = b.X1;
+      e0.ldo = pg::LDX1;
+      e0.dirs = dirs;
+      e0.rows_per_dir = rows_per_dir;
+      TVM_TRY((pgemm<pg::EPI_PE_FWD, 32>(M, d.squash, d.feat, X0, d.feat, b.img[0], e0, st, pg::ENC)));
+    } else {  // features the tensor unit cannot address: layered L0 and encoding
+      TVM_TRY((mm<false, false>(d.math, M, d.squash, d.feat, X0, d.feat, w.w0, d.squash, EpiStore{b.X1, pg::LDX1},
+                                st)));
+      pe_fwd_kernel<<<(unsigned)ceil_div(M, PE_ROWS), 256, 0, st>>>(b.X1, pg::LDX1, M, d.squash, d.enc, d.nf, d.nv,
+                                                                     dirs, rows_per_dir);
+      TVM_TRY(check_launch("pe_fwd"));
+    }
     pg::EpiArgs e1{};
     e1.out = b.H1;
     e1.ldo = 128;
     e1.bias = w.b1;
-    TVM_TRY((pgemm<pg::EPI_BIAS_RELU, 128>(M, 128, pg::LDX1, b.X1, pg::LDX1, b.img[1], e1, st)));
+    TVM_TRY((pgemm<pg::EPI_BIAS_RELU, 128>(M, 128, d.enc, b.X1, pg::LDX1, b.img[1], e1, st)));
     pg::EpiArgs e2{};
     e2.out = b.H2;
     e2.ldo = 128;
@@ -561,8 +613,8 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
   if (pmlp_supported(d)) {
     const int ntx = pmlp_nt_dx0(d);
     const pg::PackJob jobs[3] = {{w.w2, 128, 128, 128, 128, 128, 1, b.img[3]},
-                                 {w.w1, 128, 128, d.enc, 128, 160, 1, b.img[4]},
-                                 {w.w0, d.squash, d.squash, d.feat, pg::kpad(pg::LDH0), ntx, 1, b.img[5]}};
+                                 {w.w1, 128, 128, pg::PED, 128, PMLP_NT_DX1, 1, b.img[4]},
+                                 {w.w0, d.squash, d.squash, d.feat, pg::kpad(pg::SQ), ntx, 1, b.img[5]}};
     TVM_TRY(pack_images(jobs, 3, st));
     if (M > 0) {
       const unsigned blocks = (unsigned)std::min<int64_t>(2 * num_sms(), ceil_div(M, 4 * (L3_THREADS / 32)));
@@ -581,7 +633,7 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     e0.out = b.dH0;
     e0.H = b.X1;
     e0.ldh = pg::LDX1;
-    TVM_TRY((pgemm<pg::EPI_PE_BWD, 160>(M, d.enc, 128, b.dH1, 128, b.img[4], e0, st)));
+    TVM_TRY((pgemm<pg::EPI_PE_BWD, PMLP_NT_DX1>(M, pg::PED, 128, b.dH1, 128, b.img[4], e0, st)));
     TVM_TRY((mm<true, false>(d.math, d.enc, 128, M, b.X1, pg::LDX1, b.dH1, 128, EpiAtomic{g.w1, 128}, st, kc)));
     TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, pg::LDH0, EpiAtomic{g.w0, d.squash},
                              st, kc)));
@@ -590,9 +642,11 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
       ex.out = dX0;
       ex.ldo = d.feat;
       if (ntx == 64) {
-        TVM_TRY((pgemm<pg::EPI_STORE, 64>(M, d.feat, pg::LDH0, b.dH0, pg::LDH0, b.img[5], ex, st)));
+        TVM_TRY((pgemm<pg::EPI_STORE, 64>(M, d.feat, pg::SQ, b.dH0, pg::LDH0, b.img[5], ex, st)));
+      } else if (ntx == 144) {
+        TVM_TRY((pgemm<pg::EPI_STORE, 144>(M, d.feat, pg::SQ, b.dH0, pg::LDH0, b.img[5], ex, st)));
       } else {
-        TVM_TRY((pgemm<pg::EPI_STORE, 160>(M, d.feat, pg::LDH0, b.dH0, pg::LDH0, b.img[5], ex, st)));
+        TVM_TRY((pgemm<pg::EPI_STORE, 160>(M, d.feat, pg::SQ, b.dH0, pg::LDH0, b.img[5], ex, st)));
       }
     }
     return TVM_OK;

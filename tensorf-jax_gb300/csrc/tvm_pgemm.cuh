@@ -6,23 +6,29 @@
 // FP32 accuracy comes from three tf32 MMAs per product (hi*hi + hi*lo + lo*hi, hi =
 // round(x), lo = round(x - hi)), which carries ~22 significant bits of every input.
 //
-// One CTA per SM walks 128-row tiles round-robin. Roles (416 threads):
-//   warps 0-7   producers: load a 128 x 32 stage of A into registers (DEPTH stages in
-//               flight per thread), split it into tf32 hi/lo and store both tiles into a
-//               shared-memory ring slot (K-major no-swizzle canonical layout), then
-//               arrive on the slot's "full" mbarrier;
-//   warp 12     one thread issues the MMAs of each stage into a TMEM accumulator and
+// One CTA per SM walks 128-row tiles round-robin. Roles (320 threads):
+//   warp 8      one thread loads each 128 x 32 stage of A with eight 2-D TMA copies
+//               (box 4 x 128: one 16-byte column of the K-major no-swizzle canonical
+//               layout each) into a shared-memory ring slot; rows past M and columns
+//               past K arrive as zeros;
+//   warps 0-3   converters: split the landed fp32 stage into tf32 hi (in place) and lo
+//               tiles, then arrive on the slot's "full" mbarrier. They make no global
+//               accesses, so the load/store unit stays free for the epilogue;
+//   warp 9      one thread issues the MMAs of each stage into a TMEM accumulator and
 //               commits to the slot's "empty" mbarrier (and, after a tile's last stage,
 //               to the accumulator's "full" mbarrier);
-//   warps 8-11  epilogue: warp 8+e reads TMEM lanes 32e..32e+31 (one row per thread)
-//               with tcgen05.ld and applies the fused epilogue, then releases the
-//               accumulator. Two accumulators alternate, so the epilogue of tile t runs
-//               under the MMAs of tile t+1.
+//   warps 4-7   epilogue: warp 4+e reads TMEM lanes 32e..32e+31 (one row per thread)
+//               with tcgen05.ld and applies the fused epilogue; plain row-major outputs
+//               leave through a 32 x 16 shared-memory block per warp and a 2-D TMA
+//               store. Two accumulators alternate, so the epilogue of tile t runs under
+//               the MMAs of tile t+1.
 // The B operand (hi and lo images, packed once per call by pack_kernel) stays resident
-// in shared memory; one bulk copy brings it in. Every wait is bounded: a wait that
-// gives up sets bit 0 of g_tc_status and its role stops; the MMA thread drains its
-// MMAs before TMEM is freed.
+// in shared memory; bulk copies bring it in. Every wait is bounded: a wait that gives
+// up sets bit 0 of g_tc_status and its role stops; the MMA thread drains its MMAs
+// before TMEM is freed.
 #pragma once
+
+#include <cuda.h>
 
 #include "tvm_tc.cuh"
 
@@ -34,24 +40,46 @@ constexpr int BK = 32;                    // K elements per stage
 constexpr int KCH = BK / 4;               // 16-byte chunks per row per stage
 constexpr int TILE_BYTES = BM * BK * 4;   // one hi (or lo) stage tile
 constexpr int SLOT_BYTES = 2 * TILE_BYTES;
-constexpr int PROD_WARPS = 8, EPI_WARPS = 4;
-constexpr int PROD_THREADS = PROD_WARPS * 32;
+constexpr int COL_BYTES = BM * 16;        // one 16-byte column of a stage tile (LBO)
+constexpr int CONV_WARPS = 4, EPI_WARPS = 4;
+constexpr int CONV_THREADS = CONV_WARPS * 32;
 constexpr int EPI_THREADS = EPI_WARPS * 32;
-constexpr int MMA_WARP = PROD_WARPS + EPI_WARPS;
+constexpr int EPI_WARP0 = CONV_WARPS;
+constexpr int TMA_WARP = CONV_WARPS + EPI_WARPS;
+constexpr int MMA_WARP = TMA_WARP + 1;
 constexpr int THREADS = (MMA_WARP + 1) * 32;
-constexpr int CHUNKS_PER_THREAD = BM * KCH / PROD_THREADS;  // 4
-constexpr int DEPTH = 4;                  // register prefetch depth, in stages
+constexpr int CHUNKS_PER_THREAD = BM * KCH / CONV_THREADS;  // 8
 constexpr int MAX_SLOTS = 4;
 constexpr int SMEM_LIMIT = 232448;        // opt-in dynamic shared memory per block
 constexpr int MIN_SMEM = 120 * 1024;      // above half an SM: one CTA per SM (TMEM budget)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
-static_assert(CHUNKS_PER_THREAD * PROD_THREADS == BM * KCH, "stage split");
+constexpr int OUT_BOX_COLS = 16, OUT_BOX_ROWS = 32;  // TMA store block of one epilogue warp
+constexpr int STAGE_BYTES = EPI_WARPS * OUT_BOX_COLS * OUT_BOX_ROWS * 4;
+static_assert(CHUNKS_PER_THREAD * CONV_THREADS == BM * KCH, "stage split");
 
 __host__ __device__ constexpr int kpad(int K) { return (K + 7) / 8 * 8; }
 __host__ __device__ constexpr int npad(int N) { return (N + 15) / 16 * 16; }
 __host__ __device__ constexpr uint32_t acc_cols(int nt) { return nt <= 32 ? 32 : nt <= 64 ? 64 : nt <= 128 ? 128 : 256; }
 // Bytes of one packed B image (hi, then lo) for K x N.
 __host__ __device__ constexpr int image_bytes(int K, int N) { return 2 * npad(N) * kpad(K) * 4; }
+
+// 2-D TMA copies (tensor maps built on the host with cuTensorMapEncodeTiled).
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          tc::smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(tc::smem_u32(mbar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* tm, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(tm)),
+               "r"(x), "r"(y), "r"(tc::smem_u32(src))
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void tma_store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------------
 // B images: B(k, n) = BT ? W[n * ldw + k] : W[k * ldw + n] for k < K, n < N, zero in
@@ -158,6 +186,22 @@ __device__ __forceinline__ float warp_colsum16(float (&v)[16], int lane) {
   return d + __shfl_xor_sync(0xffffffffu, d, 1);
 }
 
+// Writes this warp's 32 x 16 block (lane l holds row y + l, columns x..x+15) through
+// the warp's shared-memory block sb with one TMA store; rows past M and columns past
+// the map's width are dropped by the TMA unit. sb is reused once the previous store
+// has read it.
+__device__ __forceinline__ void put_block(float* sb, const float (&v)[16], const CUtensorMap* tm, int x, int y,
+                                          int lane) {
+  if (lane == 0) tma_store_wait_read();
+  __syncwarp();
+  float4* d = reinterpret_cast<float4*>(sb + lane * OUT_BOX_COLS);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) d[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  tc::fence_proxy_async();
+  __syncwarp();
+  if (lane == 0) tma_store_2d(tm, x, y, sb);
+}
+
 template <int KIND, int NT>
 struct Epilogue {
   static constexpr int NCH = NT / 16;
@@ -168,9 +212,12 @@ struct Epilogue {
     for (int i = 0; i < (KIND == EPI_MASK_COLSUM ? NCH : 1); ++i) cs[i] = 0.0f;
   }
 
-  // esm: the epilogue's constants in shared memory (W3 and b2 for the L3 kind).
-  __device__ void tile(const EpiArgs& a, int N, uint32_t taddr, int64_t row, bool valid, int lane,
-                       const float* esm) {
+  // esm: the epilogue's constants in shared memory (W3 and b2 for the L3 kind); sb: the
+  // warp's TMA store block; tm: the output tensor map; row0: the warp's first row.
+  __device__ void tile(const EpiArgs& a, int N, uint32_t taddr, int64_t row0, int64_t M, int lane, const float* esm,
+                       float* sb, const CUtensorMap* tm) {
+    const int64_t row = row0 + lane;
+    const bool valid = row < M;
     if constexpr (KIND == EPI_BIAS_RELU || KIND == EPI_BIAS_RELU_L3) {
       float z0 = 0.f, z1 = 0.f, z2 = 0.f;
 #pragma unroll
@@ -189,13 +236,8 @@ struct Epilogue {
             z2 = fmaf(x, esm[3 * n + 2], z2);
           }
         }
-        if (valid) {
-          float* p = a.out + row * a.ldo + c * 16;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) st4(p + 4 * q, v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) st4(p + 16 + 4 * q, w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
-        }
+        put_block(sb, v, tm, c * 16, (int)row0, lane);
+        put_block(sb, w, tm, c * 16 + 16, (int)row0, lane);
       }
       if constexpr (KIND == EPI_BIAS_RELU_L3) {
         if (valid) {
@@ -206,47 +248,45 @@ struct Epilogue {
         }
       }
     } else if constexpr (KIND == EPI_PE_FWD) {
-      // X1 row (networks.py:68-76): [h | d | PE(h_j) for j | PE(d_a) for a | 0, 0] with
+      // X1 row (networks.py:68-76): [h | d | PE(h_j) for j | PE(d_a) for a] with
       // PE(v) = [sin v, sin 2v, sin(v + pi/2), sin(2v + pi/2)] = [s, 2sc, c, c^2 - s^2].
-      float h[32];
+      float x[SQ + 3];
       {
         float v[16], w[16];
         tc::tmem_ld16x2(taddr, taddr + 16, v, w);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          h[j] = v[j];
-          h[16 + j] = w[j];
+        for (int j = 0; j < 16; ++j) x[j] = v[j];
+#pragma unroll
+        for (int j = 16; j < SQ; ++j) x[j] = w[j - 16];
+      }
+      if (valid) {
+        const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
+        x[SQ] = __ldg(dp);
+        x[SQ + 1] = __ldg(dp + 1);
+        x[SQ + 2] = __ldg(dp + 2);
+      } else {
+        x[SQ] = x[SQ + 1] = x[SQ + 2] = 0.0f;
+      }
+      float sn[SQ + 3], cn[SQ + 3];
+#pragma unroll
+      for (int j = 0; j < SQ + 3; ++j) sincosf(x[j], &sn[j], &cn[j]);
+#pragma unroll
+      for (int b = 0; b < (ENC + 15) / 16; ++b) {
+        float blk[16];
+#pragma unroll
+        for (int jj = 0; jj < 16; ++jj) {
+          const int col = b * 16 + jj;
+          float val = 0.0f;
+          if (col < PEH) {
+            val = x[col];
+          } else if (col < ENC) {
+            const int j = (col - PEH) >> 2, t = (col - PEH) & 3;
+            val = t == 0 ? sn[j] : t == 1 ? 2.0f * sn[j] * cn[j] : t == 2 ? cn[j] : cn[j] * cn[j] - sn[j] * sn[j];
+          }
+          blk[jj] = val;
         }
+        put_block(sb, blk, tm, b * 16, (int)row0, lane);
       }
-      if (!valid) return;
-      const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
-      const float d0 = __ldg(dp), d1 = __ldg(dp + 1), d2 = __ldg(dp + 2);
-      float* o = a.out + row * LDX1;
-      float buf[4];
-#define PG_EMIT(col, val)                                             \
-  do {                                                                \
-    buf[(col) & 3] = (val);                                           \
-    if (((col) & 3) == 3) st4(o + (col) - 3, buf[0], buf[1], buf[2], buf[3]); \
-  } while (0)
-#pragma unroll
-      for (int j = 0; j < SQ; ++j) PG_EMIT(j, h[j]);
-      PG_EMIT(SQ, d0);
-      PG_EMIT(SQ + 1, d1);
-      PG_EMIT(SQ + 2, d2);
-#pragma unroll
-      for (int j = 0; j < SQ + 3; ++j) {
-        const float x = j < SQ ? h[j] : (j == SQ ? d0 : (j == SQ + 1 ? d1 : d2));
-        float sn, cs_;
-        sincosf(x, &sn, &cs_);
-        const int col = PEH + 4 * j;
-        PG_EMIT(col, sn);
-        PG_EMIT(col + 1, 2.0f * sn * cs_);
-        PG_EMIT(col + 2, cs_);
-        PG_EMIT(col + 3, cs_ * cs_ - sn * sn);
-      }
-      PG_EMIT(ENC, 0.0f);
-      PG_EMIT(ENC + 1, 0.0f);
-#undef PG_EMIT
     } else if constexpr (KIND == EPI_MASK_COLSUM) {
 #pragma unroll
       for (int c = 0; c < NCH; c += 2) {
@@ -270,15 +310,12 @@ struct Epilogue {
             w[4 * q + 2] = m.z > 0.f ? w[4 * q + 2] : 0.f;
             w[4 * q + 3] = m.w > 0.f ? w[4 * q + 3] : 0.f;
           }
-          float* p = a.out + row * a.ldo + c * 16;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) st4(p + 4 * q, v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) st4(p + 16 + 4 * q, w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
         } else {
 #pragma unroll
           for (int j = 0; j < 16; ++j) v[j] = w[j] = 0.0f;
         }
+        put_block(sb, v, tm, c * 16, (int)row0, lane);
+        put_block(sb, w, tm, c * 16 + 16, (int)row0, lane);
         cs[c] += warp_colsum16(v, lane);
         cs[c + 1] += warp_colsum16(w, lane);
       }
@@ -384,6 +421,7 @@ struct Epilogue {
   }
 
   __device__ void finish(const EpiArgs& a, int N, int lane) {
+    if (lane == 0) tma_store_wait_all();
     if constexpr (KIND == EPI_MASK_COLSUM) {
       if ((lane & 1) == 0) {
 #pragma unroll
@@ -404,13 +442,16 @@ __host__ __device__ constexpr int epi_smem_floats() {
 
 template <int NT>
 __host__ __device__ constexpr int smem_base_bytes(int K, int epi_floats) {
-  return image_bytes(K, NT) + epi_floats * 4 + 256;
+  return image_bytes(K, NT) + ((epi_floats * 4 + 127) & ~127) + STAGE_BYTES + 256;
 }
 
+// tmA: A as a (K wide, M high) fp32 map with a 4 x 128 box. tmO: the output map with a
+// 16 x 32 box (TMA-stored kinds). The A map's width is the K of the product: columns past
+// it (row padding) read as zero.
 template <int KIND, int NT>
 __global__ void __launch_bounds__(THREADS, 1)
-    pgemm_kernel(int64_t M, int N, int K, const float* __restrict__ A, int64_t lda, const uint8_t* __restrict__ bimg,
-                 int slots, EpiArgs ea) {
+    pgemm_kernel(int64_t M, int N, int K, const __grid_constant__ CUtensorMap tmA,
+                 const __grid_constant__ CUtensorMap tmO, const uint8_t* __restrict__ bimg, int slots, EpiArgs ea) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t NCOLS = acc_cols(NT);
   constexpr uint32_t IDESC = tc::idesc(BM, NT, 2u);
@@ -420,11 +461,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* sB = smem;                                   // hi image, then lo image
   uint8_t* sRing = smem + img;                          // slots x (hi tile, lo tile)
   float* sEpi = reinterpret_cast<float*>(sRing + slots * SLOT_BYTES);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(sEpi) + ((EF * 4 + 15) & ~15));
-  uint64_t* full = bars;                  // [MAX_SLOTS]
-  uint64_t* empty = bars + MAX_SLOTS;     // [MAX_SLOTS]
-  uint64_t* accf = bars + 2 * MAX_SLOTS;  // [2]
-  uint64_t* acce = accf + 2;              // [2]
+  float* sStage = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sEpi) + ((EF * 4 + 127) & ~127));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(sStage) + STAGE_BYTES);
+  uint64_t* landed = bars;                  // [MAX_SLOTS] TMA bytes arrived
+  uint64_t* full = bars + MAX_SLOTS;        // [MAX_SLOTS] hi/lo tiles ready
+  uint64_t* empty = bars + 2 * MAX_SLOTS;   // [MAX_SLOTS] MMAs done with the slot
+  uint64_t* accf = bars + 3 * MAX_SLOTS;    // [2]
+  uint64_t* acce = accf + 2;                // [2]
   uint64_t* wbar = acce + 2;
   uint64_t* drain = wbar + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
@@ -438,7 +481,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp == 0) tc::tmem_alloc(tslot, 2 * NCOLS);
   if (tid == 0) {
     for (int s = 0; s < MAX_SLOTS; ++s) {
-      tc::mbar_init(full + s, PROD_THREADS);
+      tc::mbar_init(landed + s, 1);
+      tc::mbar_init(full + s, CONV_THREADS);
       tc::mbar_init(empty + s, 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -458,69 +502,33 @@ __global__ void __launch_bounds__(THREADS, 1)
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
 
-  if (warp < PROD_WARPS) {
-    // ---------------- producers ----------------
-    float4 buf[DEPTH][CHUNKS_PER_THREAD];
-    int rr[CHUNKS_PER_THREAD], kk[CHUNKS_PER_THREAD];
-#pragma unroll
-    for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
-      const int task = warp * CHUNKS_PER_THREAD + i;  // 32 tasks: 16 row groups x 2 chunk halves
-      rr[i] = 8 * (task % (BM / 8)) + (lane & 7);
-      kk[i] = 4 * (task / (BM / 8)) + (lane >> 3);
-    }
-    // 16-byte loads when A and its row pitch allow them (K is a multiple of 4).
-    const bool avec = ((reinterpret_cast<uintptr_t>(A) | (uintptr_t)(lda * 4)) & 15) == 0;
-    auto load = [&](int64_t q, float4 (&dst)[CHUNKS_PER_THREAD]) {
-      const int64_t tl = q / KS;
-      const int ks = (int)(q - tl * KS);
-      const int64_t m0 = ((int64_t)blockIdx.x + tl * gridDim.x) * BM;
+  if (warp < CONV_WARPS) {
+    // ---------------- converters: fp32 stage -> tf32 hi (in place) + lo ----------------
+    for (int64_t q = 0; q < nq; ++q) {
+      const int slot = (int)(q % slots);
+      if (!tc::mbar_wait(landed + slot, (uint32_t)((q / slots) & 1), WAIT_LIMIT)) {
+        atomicOr(&g_tc_status, 1);
+        break;
+      }
+      uint8_t* hi = sRing + slot * SLOT_BYTES;
+      uint8_t* lo = hi + TILE_BYTES;
 #pragma unroll
       for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
-        const int64_t r = m0 + rr[i];
-        const int k = ks * BK + 4 * kk[i];
-        const float* p = A + r * lda + k;
-        dst[i] = (r < M && k < K)
-                     ? (avec ? __ldg(reinterpret_cast<const float4*>(p))
-                             : make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3)))
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int off = (tid + i * CONV_THREADS) * 16;  // layout-agnostic: every chunk alike
+        const float4 x = *reinterpret_cast<const float4*>(hi + off);
+        const uint32_t h0 = tc::to_tf32(x.x), h1 = tc::to_tf32(x.y), h2 = tc::to_tf32(x.z), h3 = tc::to_tf32(x.w);
+        const uint32_t l0 = tc::to_tf32(x.x - __uint_as_float(h0)), l1 = tc::to_tf32(x.y - __uint_as_float(h1));
+        const uint32_t l2 = tc::to_tf32(x.z - __uint_as_float(h2)), l3 = tc::to_tf32(x.w - __uint_as_float(h3));
+        *reinterpret_cast<uint4*>(hi + off) = make_uint4(h0, h1, h2, h3);
+        *reinterpret_cast<uint4*>(lo + off) = make_uint4(l0, l1, l2, l3);
       }
-    };
-#pragma unroll
-    for (int j = 0; j < DEPTH; ++j)
-      if (j < nq) load(j, buf[j]);
-    bool ok = true;
-    for (int64_t q0 = 0; q0 < nq && ok; q0 += DEPTH) {
-#pragma unroll
-      for (int j = 0; j < DEPTH; ++j) {
-        const int64_t q = q0 + j;
-        if (q >= nq) break;
-        const int slot = (int)(q % slots);
-        const int64_t use = q / slots;
-        if (use > 0 && !tc::mbar_wait(empty + slot, (uint32_t)((use - 1) & 1), WAIT_LIMIT)) {
-          atomicOr(&g_tc_status, 1);
-          ok = false;
-          break;
-        }
-        uint8_t* hi = sRing + slot * SLOT_BYTES;
-        uint8_t* lo = hi + TILE_BYTES;
-#pragma unroll
-        for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
-          const float4 x = buf[j][i];
-          const uint32_t h0 = tc::to_tf32(x.x), h1 = tc::to_tf32(x.y), h2 = tc::to_tf32(x.z), h3 = tc::to_tf32(x.w);
-          const uint32_t l0 = tc::to_tf32(x.x - __uint_as_float(h0)), l1 = tc::to_tf32(x.y - __uint_as_float(h1));
-          const uint32_t l2 = tc::to_tf32(x.z - __uint_as_float(h2)), l3 = tc::to_tf32(x.w - __uint_as_float(h3));
-          const int off = (rr[i] >> 3) * (KCH * 128) + kk[i] * 128 + (rr[i] & 7) * 16;
-          *reinterpret_cast<uint4*>(hi + off) = make_uint4(h0, h1, h2, h3);
-          *reinterpret_cast<uint4*>(lo + off) = make_uint4(l0, l1, l2, l3);
-        }
-        tc::fence_proxy_async();
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(full + slot)) : "memory");
-        if (q + DEPTH < nq) load(q + DEPTH, buf[j]);
-      }
+      tc::fence_proxy_async();
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(full + slot)) : "memory");
     }
-  } else if (warp < MMA_WARP) {
+  } else if (warp < TMA_WARP) {
     // ---------------- epilogue ----------------
-    const int e = warp - PROD_WARPS;  // TMEM sub-partition (warp % 4 == e)
+    const int e = warp - EPI_WARP0;  // TMEM sub-partition (warp % 4 == e)
+    float* sb = sStage + e * OUT_BOX_COLS * OUT_BOX_ROWS;
     Epilogue<KIND, NT> epi;
     epi.init();
     bool ok = true;
@@ -532,13 +540,36 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       tc::fence_after_sync();
-      const int64_t row = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * BM + 32 * e + lane;
+      const int64_t row0 = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * BM + 32 * e;
       const uint32_t taddr = tmem + (uint32_t)(b * NCOLS) + ((uint32_t)(32 * e) << 16);
-      epi.tile(ea, N, taddr, row, row < M, lane, sEpi);
+      epi.tile(ea, N, taddr, row0, M, lane, sEpi, sb, &tmO);
       tc::fence_before_sync();
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(acce + b)) : "memory");
     }
     epi.finish(ea, N, lane);
+  } else if (warp == TMA_WARP) {
+    // ---------------- TMA loads of A ----------------
+    if (lane == 0) {
+      for (int64_t q = 0; q < nq; ++q) {
+        const int slot = (int)(q % slots);
+        const int64_t use = q / slots;
+        if (use > 0 && !tc::mbar_wait(empty + slot, (uint32_t)((use - 1) & 1), WAIT_LIMIT)) {
+          atomicOr(&g_tc_status, 1);
+          break;
+        }
+        const int64_t tl = q / KS;
+        const int ks = (int)(q - tl * KS);
+        const int y = (int)(((int64_t)blockIdx.x + tl * gridDim.x) * BM);
+        uint8_t* hi = sRing + slot * SLOT_BYTES;
+        tc::mbar_expect_tx(landed + slot, TILE_BYTES);
+#pragma unroll
+        for (int c = 0; c < KCH; ++c) tma_load_2d(hi + c * COL_BYTES, &tmA, ks * BK + 4 * c, y, landed + slot);
+      }
+      // No copy may still be writing shared memory when the CTA exits (the converters
+      // wait for every stage unless a wait gave up).
+      for (int64_t q = nq - slots > 0 ? nq - slots : 0; q < nq; ++q)
+        if (!tc::mbar_wait(landed + (int)(q % slots), (uint32_t)((q / slots) & 1), WAIT_LIMIT)) atomicOr(&g_tc_status, 1);
+    }
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
     const int bytes = img;
@@ -573,8 +604,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int kleft = K - ks * BK;
         const int steps = (kleft >= BK ? BK : kleft + 7) / 8;
         for (int s = 0; s < steps; ++s) {
+          // A: [16-byte column][row] (LBO = one column, SBO = 8 rows); B: packed image.
           const uint32_t kb = (uint32_t)(ks * KCH + 2 * s) * 128;
-          const uint64_t ah = tc::sdesc(a_hi + s * 256, 128, KCH * 128), al = tc::sdesc(a_lo + s * 256, 128, KCH * 128);
+          const uint64_t ah = tc::sdesc(a_hi + 2 * s * COL_BYTES, COL_BYTES, 128);
+          const uint64_t al = tc::sdesc(a_lo + 2 * s * COL_BYTES, COL_BYTES, 128);
           const uint64_t bh = tc::sdesc(b_hi + kb, 128, sbo_b), bl = tc::sdesc(b_lo + kb, 128, sbo_b);
           tc::mma_tf32(d, ah, bh, IDESC, (ks > 0 || s > 0) ? 1u : 0u);
           tc::mma_tf32(d, ah, bl, IDESC, 1u);
