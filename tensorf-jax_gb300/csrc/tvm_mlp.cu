@@ -369,8 +369,10 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Row-major fp32 matrix (cols wide, rows high, row pitch ld elements) as a 2-D tensor map
-// with a box of bx columns x by rows; reads past the edges return zero.
-static int make_map(CUtensorMap* m, const float* base, int64_t cols, int64_t rows, int64_t ld, int bx, int by) {
+// with a box of bx columns x by rows and the given shared-memory swizzle; reads past the
+// edges return zero.
+static int make_map(CUtensorMap* m, const float* base, int64_t cols, int64_t rows, int64_t ld, int bx, int by,
+                    CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE) {
   auto enc = tensor_map_encoder();
   TVM_REQUIRE(enc != nullptr, TVM_ERR_LAUNCH, "cuTensorMapEncodeTiled is unavailable");
   TVM_REQUIRE(aligned(base, 16) && (ld * 4) % 16 == 0 && cols > 0 && rows > 0, TVM_ERR_ALIGN,
@@ -380,7 +382,7 @@ static int make_map(CUtensorMap* m, const float* base, int64_t cols, int64_t row
   const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   TVM_REQUIRE(r == CUDA_SUCCESS, TVM_ERR_LAUNCH, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return TVM_OK;
@@ -398,17 +400,30 @@ static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uin
                    N == NT),
               TVM_ERR_INVALID, "pgemm: unsupported operands (K=%d, lda=%lld, N=%d)", K, (long long)lda, N);
   CUtensorMap tmA, tmO;
-  TVM_TRY(make_map(&tmA, A, K, M, lda, 4, pg::BM));
+  TVM_TRY(make_map(&tmA, A, K, M, lda, pg::BK, pg::BM, CU_TENSOR_MAP_SWIZZLE_128B));
   if (tma_out) {
     TVM_TRY(make_map(&tmO, ea.out, ocols > 0 ? ocols : N, M, ea.ldo, pg::OUT_BOX_COLS, pg::OUT_BOX_ROWS));
   } else {
     tmO = tmA;
   }
+  // Shared memory left after the B images goes to store blocks (up to 4 per epilogue warp
+  // while at least 4 TMA stages still fit) and then to the TMA ring.
   constexpr int EF = pg::epi_smem_floats<KIND, NT>();
   const int base = pg::smem_base_bytes<NT>(K, EF);
-  const int slots = std::min(pg::MAX_SLOTS, (pg::SMEM_LIMIT - base) / pg::SLOT_BYTES);
+  const int avail = pg::SMEM_LIMIT - base;
+  int nsb = 0;
+  if (tma_out) {
+    nsb = 1;
+    for (int cand : {4, 2})
+      if (avail - cand * pg::EPI_WARPS * pg::OUT_BOX_FLOATS * 4 >= 4 * pg::TILE_BYTES) {
+        nsb = cand;
+        break;
+      }
+  }
+  const int stage = nsb * pg::EPI_WARPS * pg::OUT_BOX_FLOATS * 4;
+  const int slots = std::min(pg::MAX_SLOTS, (avail - stage) / pg::TILE_BYTES);
   TVM_REQUIRE(slots >= 2, TVM_ERR_UNSUPPORTED, "pgemm: K=%d, N=%d leaves %d pipeline slots", K, NT, slots);
-  const int bytes = std::max(base + slots * pg::SLOT_BYTES, pg::MIN_SMEM);
+  const int bytes = std::max(base + slots * pg::TILE_BYTES + stage, pg::MIN_SMEM);
   auto fn = pg::pgemm_kernel<KIND, NT>;
   static bool attr_done = false;  // per instantiation
   if (!attr_done) {
@@ -418,7 +433,7 @@ static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uin
   }
   const int64_t tiles = ceil_div(M, pg::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
-  fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, tmA, tmO, bimg, slots, ea);
+  fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, tmA, tmO, bimg, slots, nsb, ea);
   return check_launch("pgemm");
 }
 
@@ -505,6 +520,7 @@ struct MlpBufs {
   float *X1, *H1, *H2, *dH2, *dH1, *dX1, *dH0;
   uint8_t* wpack;
   uint8_t* img[6];
+  uint32_t* mask1;  // ReLU bits of H1 (4 words per row), for the dH1 product
 };
 static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   MlpBufs b{};
@@ -521,6 +537,7 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
     b.dH2 = ws.take<float>(M * 128);
     b.dH1 = ws.take<float>(M * 128);
     b.dH0 = ws.take<float>(M * pg::LDH0);
+    b.mask1 = ws.take<uint32_t>(M * 4);
     return b;
   }
   b.X1 = ws.take<float>(M * ld_x1(d));
@@ -576,6 +593,7 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
     e1.out = b.H1;
     e1.ldo = 128;
     e1.bias = w.b1;
+    e1.mask = b.mask1;
     TVM_TRY((pgemm<pg::EPI_BIAS_RELU, 128>(M, 128, d.enc, b.X1, pg::LDX1, b.img[1], e1, st)));
     pg::EpiArgs e2{};
     e2.out = b.H2;
@@ -624,8 +642,7 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     pg::EpiArgs e1{};
     e1.out = b.dH1;
     e1.ldo = 128;
-    e1.H = b.H1;
-    e1.ldh = 128;
+    e1.mask = b.mask1;
     e1.colsum = g.b1;
     TVM_TRY((pgemm<pg::EPI_MASK_COLSUM, 128>(M, 128, 128, b.dH2, 128, b.img[3], e1, st)));
     TVM_TRY((mm<true, false>(d.math, 128, 128, M, b.H1, 128, b.dH2, 128, EpiAtomic{g.w2, 128}, st, kc)));

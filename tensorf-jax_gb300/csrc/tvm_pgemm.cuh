@@ -7,20 +7,20 @@
 // round(x), lo = round(x - hi)), which carries ~22 significant bits of every input.
 //
 // One CTA per SM walks 128-row tiles round-robin. Roles (320 threads):
-//   warp 8      one thread loads each 128 x 32 stage of A with eight 2-D TMA copies
-//               (box 4 x 128: one 16-byte column of the K-major no-swizzle canonical
-//               layout each) into a shared-memory ring slot; rows past M and columns
-//               past K arrive as zeros;
-//   warps 0-3   converters: split the landed fp32 stage into tf32 hi (in place) and lo
-//               tiles, then arrive on the slot's "full" mbarrier. They make no global
-//               accesses, so the load/store unit stays free for the epilogue;
+//   warp 8      one thread loads each 128 x 32 stage of A (128-byte rows) with one 2-D
+//               TMA copy in the 128-byte-swizzle layout, which is the K-major SWIZZLE_128B
+//               operand layout of the MMA, into a shared-memory ring slot; rows past M
+//               and columns past K arrive as zeros;
+//   warps 0-3   converters: split the landed fp32 stage into tf32 hi (in place) and a lo
+//               tile (a ring of two), then arrive on the slot's "full" mbarrier. They make
+//               no global accesses, so the load/store unit stays free for the epilogue;
 //   warp 9      one thread issues the MMAs of each stage into a TMEM accumulator and
 //               commits to the slot's "empty" mbarrier (and, after a tile's last stage,
 //               to the accumulator's "full" mbarrier);
 //   warps 4-7   epilogue: warp 4+e reads TMEM lanes 32e..32e+31 (one row per thread)
 //               with tcgen05.ld and applies the fused epilogue; plain row-major outputs
-//               leave through a 32 x 16 shared-memory block per warp and a 2-D TMA
-//               store. Two accumulators alternate, so the epilogue of tile t runs under
+//               leave through 32 x 16 shared-memory blocks (a ring per warp) and 2-D TMA
+//               stores. Two accumulators alternate, so the epilogue of tile t runs under
 //               the MMAs of tile t+1.
 // The B operand (hi and lo images, packed once per call by pack_kernel) stays resident
 // in shared memory; bulk copies bring it in. Every wait is bounded: a wait that gives
@@ -36,11 +36,11 @@ namespace tvm {
 namespace pg {
 
 constexpr int BM = 128;
-constexpr int BK = 32;                    // K elements per stage
+constexpr int BK = 32;                    // K elements per stage (one 128-byte swizzle row)
 constexpr int KCH = BK / 4;               // 16-byte chunks per row per stage
-constexpr int TILE_BYTES = BM * BK * 4;   // one hi (or lo) stage tile
-constexpr int SLOT_BYTES = 2 * TILE_BYTES;
-constexpr int COL_BYTES = BM * 16;        // one 16-byte column of a stage tile (LBO)
+constexpr int TILE_BYTES = BM * BK * 4;   // one stage tile (fp32 / tf32 hi, or tf32 lo)
+constexpr int LO_SLOTS = 2;               // lo tiles: converted stages waiting for their MMAs
+constexpr int SW_ATOM = 1024;             // 8 rows x 128 bytes: one 128-byte-swizzle atom
 constexpr int CONV_WARPS = 4, EPI_WARPS = 4;
 constexpr int CONV_THREADS = CONV_WARPS * 32;
 constexpr int EPI_THREADS = EPI_WARPS * 32;
@@ -49,12 +49,13 @@ constexpr int TMA_WARP = CONV_WARPS + EPI_WARPS;
 constexpr int MMA_WARP = TMA_WARP + 1;
 constexpr int THREADS = (MMA_WARP + 1) * 32;
 constexpr int CHUNKS_PER_THREAD = BM * KCH / CONV_THREADS;  // 8
-constexpr int MAX_SLOTS = 4;
+constexpr int MAX_SLOTS = 8;              // TMA ring depth (stages in flight)
 constexpr int SMEM_LIMIT = 232448;        // opt-in dynamic shared memory per block
 constexpr int MIN_SMEM = 120 * 1024;      // above half an SM: one CTA per SM (TMEM budget)
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 constexpr int OUT_BOX_COLS = 16, OUT_BOX_ROWS = 32;  // TMA store block of one epilogue warp
-constexpr int STAGE_BYTES = EPI_WARPS * OUT_BOX_COLS * OUT_BOX_ROWS * 4;
+constexpr int OUT_BOX_FLOATS = OUT_BOX_COLS * OUT_BOX_ROWS;
+constexpr int BAR_BYTES = 512;
 static_assert(CHUNKS_PER_THREAD * CONV_THREADS == BM * KCH, "stage split");
 
 __host__ __device__ constexpr int kpad(int K) { return (K + 7) / 8 * 8; }
@@ -62,6 +63,14 @@ __host__ __device__ constexpr int npad(int N) { return (N + 15) / 16 * 16; }
 __host__ __device__ constexpr uint32_t acc_cols(int nt) { return nt <= 32 ? 32 : nt <= 64 ? 64 : nt <= 128 ? 128 : 256; }
 // Bytes of one packed B image (hi, then lo) for K x N.
 __host__ __device__ constexpr int image_bytes(int K, int N) { return 2 * npad(N) * kpad(K) * 4; }
+
+// K-major SWIZZLE_128B operand: 8-row x 128-byte atoms (SBO = 1024 bytes between
+// 8-row groups), swizzle mode 2 in bits 61-63 of the descriptor; the leading offset is
+// unused for this layout (encoded as 1). A K step inside the atom advances the start
+// address by its byte offset.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  return tc::sdesc(saddr, 16, SW_ATOM) | (2ull << 61);
+}
 
 // 2-D TMA copies (tensor maps built on the host with cuTensorMapEncodeTiled).
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* mbar) {
@@ -125,7 +134,7 @@ enum EpiKind : int {
   EPI_BIAS_RELU = 0,     // out = relu(acc + bias)                       (H1)
   EPI_BIAS_RELU_L3 = 1,  // out = relu(acc + bias); rgb = sigmoid(out W3 + b3)   (H2, rgb)
   EPI_PE_FWD = 2,        // X1 row = [h, d, PE(h), PE(d), 0 pad] from h = acc (N = 27)
-  EPI_MASK_COLSUM = 3,   // out = acc * [H > 0]; colsum += out            (dH1, db1)
+  EPI_MASK_COLSUM = 3,   // out = acc * [H > 0] (H's ReLU bits); colsum += out    (dH1, db1)
   EPI_PE_BWD = 4,        // dH0 = acc[h] + d PE / d h . acc[PE(h)]        (dX1 -> dH0)
   EPI_STORE = 5,         // out = acc                                      (dX0)
 };
@@ -137,9 +146,10 @@ struct EpiArgs {
   const float* w3;       // EPI_BIAS_RELU_L3: (N, 3) row-major
   const float* b3;       // EPI_BIAS_RELU_L3: (3)
   float* rgb;            // EPI_BIAS_RELU_L3: (M, 3)
-  const float* H;        // EPI_MASK_COLSUM: ReLU output (M, ldh); EPI_PE_BWD: X1 (M, ldh)
+  const float* H;        // EPI_PE_BWD: X1 (M, ldh)
   int ldh;
   float* colsum;         // EPI_MASK_COLSUM: (N), accumulated
+  uint32_t* mask;        // EPI_BIAS_RELU (optional, written) / EPI_MASK_COLSUM (read): (M, 4) ReLU bits
   const float* dirs;     // EPI_PE_FWD: view direction of row m at dirs[(m / rows_per_dir) * 3]
   int rows_per_dir;
 };
@@ -186,14 +196,24 @@ __device__ __forceinline__ float warp_colsum16(float (&v)[16], int lane) {
   return d + __shfl_xor_sync(0xffffffffu, d, 1);
 }
 
-// Writes this warp's 32 x 16 block (lane l holds row y + l, columns x..x+15) through
-// the warp's shared-memory block sb with one TMA store; rows past M and columns past
-// the map's width are dropped by the TMA unit. sb is reused once the previous store
-// has read it.
-__device__ __forceinline__ void put_block(float* sb, const float (&v)[16], const CUtensorMap* tm, int x, int y,
+// Writes this warp's 32 x 16 block (lane l holds row y + l, columns x..x+15) with one
+// TMA store from the next of the warp's nsb shared-memory blocks; rows past M and
+// columns past the map's width are dropped by the TMA unit. A block is rewritten once
+// at most nsb - 1 later stores are still reading.
+struct StoreRing {
+  float* base;
+  int nsb, next;
+};
+__device__ __forceinline__ void put_block(StoreRing& r, const float (&v)[16], const CUtensorMap* tm, int x, int y,
                                           int lane) {
-  if (lane == 0) tma_store_wait_read();
+  if (lane == 0) {
+    if (r.nsb >= 4) asm volatile("cp.async.bulk.wait_group.read 3;" ::: "memory");
+    else if (r.nsb >= 2) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+    else tma_store_wait_read();
+  }
   __syncwarp();
+  float* sb = r.base + r.next * OUT_BOX_FLOATS;
+  r.next = r.next + 1 == r.nsb ? 0 : r.next + 1;
   float4* d = reinterpret_cast<float4*>(sb + lane * OUT_BOX_COLS);
 #pragma unroll
   for (int q = 0; q < 4; ++q) d[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
@@ -214,21 +234,25 @@ struct Epilogue {
 
   // esm: the epilogue's constants in shared memory (W3 and b2 for the L3 kind); sb: the
   // warp's TMA store block; tm: the output tensor map; row0: the warp's first row.
+  // pre: the row's prefetched global input (the ReLU bit mask, or X1's first 28 columns).
   __device__ void tile(const EpiArgs& a, int N, uint32_t taddr, int64_t row0, int64_t M, int lane, const float* esm,
-                       float* sb, const CUtensorMap* tm) {
+                       StoreRing& sr, const CUtensorMap* tm, const float4 (&pre)[7]) {
     const int64_t row = row0 + lane;
     const bool valid = row < M;
     if constexpr (KIND == EPI_BIAS_RELU || KIND == EPI_BIAS_RELU_L3) {
       float z0 = 0.f, z1 = 0.f, z2 = 0.f;
+      uint32_t bits[NCH / 2];
 #pragma unroll
       for (int c = 0; c < NCH; c += 2) {
         float v[16], w[16];
         tc::tmem_ld16x2(taddr + c * 16, taddr + c * 16 + 16, v, w);
+        uint32_t word = 0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int n = c * 16 + j;
           float x = (j < 16) ? v[j] : w[j - 16];
           x = fmaxf(x + (KIND == EPI_BIAS_RELU_L3 ? esm[3 * NT + n] : __ldg(a.bias + n)), 0.0f);
+          word |= (x > 0.0f ? 1u : 0u) << j;
           if (j < 16) v[j] = x; else w[j - 16] = x;
           if constexpr (KIND == EPI_BIAS_RELU_L3) {
             z0 = fmaf(x, esm[3 * n], z0);
@@ -236,8 +260,13 @@ struct Epilogue {
             z2 = fmaf(x, esm[3 * n + 2], z2);
           }
         }
-        put_block(sb, v, tm, c * 16, (int)row0, lane);
-        put_block(sb, w, tm, c * 16 + 16, (int)row0, lane);
+        bits[c / 2] = word;
+        put_block(sr, v, tm, c * 16, (int)row0, lane);
+        put_block(sr, w, tm, c * 16 + 16, (int)row0, lane);
+      }
+      if (a.mask && valid) {  // ReLU bits of the row (bit j of word c: column 32c + j > 0)
+        static_assert(NCH == 8, "mask rows hold 128 columns");
+        *reinterpret_cast<uint4*>(a.mask + row * 4) = make_uint4(bits[0], bits[1], bits[2], bits[3]);
       }
       if constexpr (KIND == EPI_BIAS_RELU_L3) {
         if (valid) {
@@ -285,37 +314,24 @@ struct Epilogue {
           }
           blk[jj] = val;
         }
-        put_block(sb, blk, tm, b * 16, (int)row0, lane);
+        put_block(sr, blk, tm, b * 16, (int)row0, lane);
       }
     } else if constexpr (KIND == EPI_MASK_COLSUM) {
+      static_assert(NCH == 8, "mask rows hold 128 columns");
+      const uint32_t bits[4] = {__float_as_uint(pre[0].x), __float_as_uint(pre[0].y), __float_as_uint(pre[0].z),
+                                __float_as_uint(pre[0].w)};  // zero for rows past M
 #pragma unroll
       for (int c = 0; c < NCH; c += 2) {
         float v[16], w[16];
         tc::tmem_ld16x2(taddr + c * 16, taddr + c * 16 + 16, v, w);
-        if (valid) {
-          const float* hp = a.H + row * a.ldh + c * 16;
+        const uint32_t word = bits[c / 2];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float4 m = __ldg(reinterpret_cast<const float4*>(hp) + q);
-            v[4 * q] = m.x > 0.f ? v[4 * q] : 0.f;
-            v[4 * q + 1] = m.y > 0.f ? v[4 * q + 1] : 0.f;
-            v[4 * q + 2] = m.z > 0.f ? v[4 * q + 2] : 0.f;
-            v[4 * q + 3] = m.w > 0.f ? v[4 * q + 3] : 0.f;
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const float4 m = __ldg(reinterpret_cast<const float4*>(hp + 16) + q);
-            w[4 * q] = m.x > 0.f ? w[4 * q] : 0.f;
-            w[4 * q + 1] = m.y > 0.f ? w[4 * q + 1] : 0.f;
-            w[4 * q + 2] = m.z > 0.f ? w[4 * q + 2] : 0.f;
-            w[4 * q + 3] = m.w > 0.f ? w[4 * q + 3] : 0.f;
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = w[j] = 0.0f;
+        for (int j = 0; j < 16; ++j) {
+          v[j] = (word >> j) & 1u ? v[j] : 0.0f;
+          w[j] = (word >> (16 + j)) & 1u ? w[j] : 0.0f;
         }
-        put_block(sb, v, tm, c * 16, (int)row0, lane);
-        put_block(sb, w, tm, c * 16 + 16, (int)row0, lane);
+        put_block(sr, v, tm, c * 16, (int)row0, lane);
+        put_block(sr, w, tm, c * 16 + 16, (int)row0, lane);
         cs[c] += warp_colsum16(v, lane);
         cs[c + 1] += warp_colsum16(w, lane);
       }
@@ -323,19 +339,12 @@ struct Epilogue {
       // dH0[j] = dX1[j] + sum_f dX1[sin 2^f h_j] * 2^f cos(2^f h_j)
       //                 + dX1[sin(2^f h_j + pi/2)] * (-2^f sin(2^f h_j))   (networks.py:13-35)
       float hv[28];
-      if (valid) {
-        const float4* hp = reinterpret_cast<const float4*>(a.H + row * a.ldh);
 #pragma unroll
-        for (int q = 0; q < 7; ++q) {
-          const float4 t = __ldg(hp + q);
-          hv[4 * q] = t.x;
-          hv[4 * q + 1] = t.y;
-          hv[4 * q + 2] = t.z;
-          hv[4 * q + 3] = t.w;
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 28; ++j) hv[j] = 0.0f;
+      for (int q = 0; q < 7; ++q) {
+        hv[4 * q] = pre[q].x;
+        hv[4 * q + 1] = pre[q].y;
+        hv[4 * q + 2] = pre[q].z;
+        hv[4 * q + 3] = pre[q].w;
       }
       float s1[SQ], c1[SQ];
 #pragma unroll
@@ -440,34 +449,44 @@ __host__ __device__ constexpr int epi_smem_floats() {
   return KIND == EPI_BIAS_RELU_L3 ? 4 * NT + 4 : 0;
 }
 
+// Shared memory besides the TMA ring and the store blocks: alignment slack, B images,
+// epilogue constants, the lo ring and the mbarriers.
 template <int NT>
 __host__ __device__ constexpr int smem_base_bytes(int K, int epi_floats) {
-  return image_bytes(K, NT) + ((epi_floats * 4 + 127) & ~127) + STAGE_BYTES + 256;
+  return SW_ATOM + image_bytes(K, NT) + ((epi_floats * 4 + SW_ATOM - 1) & ~(SW_ATOM - 1)) + LO_SLOTS * TILE_BYTES +
+         BAR_BYTES;
 }
 
 // tmA: A as a (K wide, M high) fp32 map with a 4 x 128 box. tmO: the output map with a
 // 16 x 32 box (TMA-stored kinds). The A map's width is the K of the product: columns past
-// it (row padding) read as zero.
+// it (row padding) read as zero. slots: TMA ring depth; nsb: store blocks per epilogue
+// warp (1, 2 or 4; 0 for kinds that store directly).
 template <int KIND, int NT>
 __global__ void __launch_bounds__(THREADS, 1)
     pgemm_kernel(int64_t M, int N, int K, const __grid_constant__ CUtensorMap tmA,
-                 const __grid_constant__ CUtensorMap tmO, const uint8_t* __restrict__ bimg, int slots, EpiArgs ea) {
-  extern __shared__ __align__(1024) uint8_t smem[];
+                 const __grid_constant__ CUtensorMap tmO, const uint8_t* __restrict__ bimg, int slots, int nsb,
+                 EpiArgs ea) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // The swizzled tiles need 1024-byte alignment in the shared window (1 KB is reserved).
+  uint8_t* smem = smem_raw + ((SW_ATOM - (tc::smem_u32(smem_raw) & (SW_ATOM - 1))) & (SW_ATOM - 1));
   constexpr uint32_t NCOLS = acc_cols(NT);
   constexpr uint32_t IDESC = tc::idesc(BM, NT, 2u);
   constexpr int EF = epi_smem_floats<KIND, NT>();
   const int KP = kpad(K);
   const int img = image_bytes(K, NT);
-  uint8_t* sB = smem;                                   // hi image, then lo image
-  uint8_t* sRing = smem + img;                          // slots x (hi tile, lo tile)
-  float* sEpi = reinterpret_cast<float*>(sRing + slots * SLOT_BYTES);
-  float* sStage = reinterpret_cast<float*>(reinterpret_cast<uint8_t*>(sEpi) + ((EF * 4 + 127) & ~127));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(sStage) + STAGE_BYTES);
-  uint64_t* landed = bars;                  // [MAX_SLOTS] TMA bytes arrived
-  uint64_t* full = bars + MAX_SLOTS;        // [MAX_SLOTS] hi/lo tiles ready
-  uint64_t* empty = bars + 2 * MAX_SLOTS;   // [MAX_SLOTS] MMAs done with the slot
-  uint64_t* accf = bars + 3 * MAX_SLOTS;    // [2]
-  uint64_t* acce = accf + 2;                // [2]
+  // Tiles read through swizzled descriptors start on 1024-byte atoms.
+  uint8_t* sB = smem;                                                       // hi image, lo image
+  float* sEpi = reinterpret_cast<float*>(smem + img);                       // epilogue constants
+  uint8_t* sLo = smem + img + ((EF * 4 + SW_ATOM - 1) & ~(SW_ATOM - 1));    // LO_SLOTS lo tiles
+  uint8_t* sRing = sLo + LO_SLOTS * TILE_BYTES;                             // slots fp32 / hi tiles
+  float* sStage = reinterpret_cast<float*>(sRing + slots * TILE_BYTES);     // store blocks
+  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(sStage) + nsb * EPI_WARPS * OUT_BOX_FLOATS * 4);
+  uint64_t* landed = bars;                   // [MAX_SLOTS] TMA bytes arrived
+  uint64_t* full = bars + MAX_SLOTS;         // [MAX_SLOTS] hi/lo tiles ready
+  uint64_t* empty = bars + 2 * MAX_SLOTS;    // [MAX_SLOTS] MMAs done with the slot
+  uint64_t* lo_empty = bars + 3 * MAX_SLOTS; // [LO_SLOTS] MMAs done with the lo tile
+  uint64_t* accf = lo_empty + LO_SLOTS;      // [2]
+  uint64_t* acce = accf + 2;                 // [2]
   uint64_t* wbar = acce + 2;
   uint64_t* drain = wbar + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(drain + 1);
@@ -485,6 +504,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc::mbar_init(full + s, CONV_THREADS);
       tc::mbar_init(empty + s, 1);
     }
+    for (int s = 0; s < LO_SLOTS; ++s) tc::mbar_init(lo_empty + s, 1);
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(accf + b, 1);
       tc::mbar_init(acce + b, EPI_THREADS);
@@ -505,13 +525,14 @@ __global__ void __launch_bounds__(THREADS, 1)
   if (warp < CONV_WARPS) {
     // ---------------- converters: fp32 stage -> tf32 hi (in place) + lo ----------------
     for (int64_t q = 0; q < nq; ++q) {
-      const int slot = (int)(q % slots);
-      if (!tc::mbar_wait(landed + slot, (uint32_t)((q / slots) & 1), WAIT_LIMIT)) {
+      const int slot = (int)(q % slots), lj = (int)(q % LO_SLOTS);
+      if (!tc::mbar_wait(landed + slot, (uint32_t)((q / slots) & 1), WAIT_LIMIT) ||
+          (q >= LO_SLOTS && !tc::mbar_wait(lo_empty + lj, (uint32_t)((q / LO_SLOTS - 1) & 1), WAIT_LIMIT))) {
         atomicOr(&g_tc_status, 1);
         break;
       }
-      uint8_t* hi = sRing + slot * SLOT_BYTES;
-      uint8_t* lo = hi + TILE_BYTES;
+      uint8_t* hi = sRing + slot * TILE_BYTES;
+      uint8_t* lo = sLo + lj * TILE_BYTES;
 #pragma unroll
       for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
         const int off = (tid + i * CONV_THREADS) * 16;  // layout-agnostic: every chunk alike
@@ -528,21 +549,31 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else if (warp < TMA_WARP) {
     // ---------------- epilogue ----------------
     const int e = warp - EPI_WARP0;  // TMEM sub-partition (warp % 4 == e)
-    float* sb = sStage + e * OUT_BOX_COLS * OUT_BOX_ROWS;
+    StoreRing sr{sStage + e * nsb * OUT_BOX_FLOATS, nsb, 0};
     Epilogue<KIND, NT> epi;
     epi.init();
     bool ok = true;
     for (int i = 0; i < my_tiles && ok; ++i) {
       const int b = i & 1;
+      const int64_t row0 = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * BM + 32 * e;
+      const int64_t row = row0 + lane;
+      // The row's global input is requested before the accumulator wait.
+      float4 pre[7];
+#pragma unroll
+      for (int q = 0; q < 7; ++q) pre[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (KIND == EPI_MASK_COLSUM && row < M) pre[0] = __ldg(reinterpret_cast<const float4*>(ea.mask + row * 4));
+      if (KIND == EPI_PE_BWD && row < M) {
+#pragma unroll
+        for (int q = 0; q < 7; ++q) pre[q] = __ldg(reinterpret_cast<const float4*>(ea.H + row * ea.ldh) + q);
+      }
       ok = __all_sync(0xffffffffu, tc::mbar_wait(accf + b, (uint32_t)((i >> 1) & 1), WAIT_LIMIT));
       if (!ok) {
         if (lane == 0) atomicOr(&g_tc_status, 1);
         break;
       }
       tc::fence_after_sync();
-      const int64_t row0 = ((int64_t)blockIdx.x + (int64_t)i * gridDim.x) * BM + 32 * e;
       const uint32_t taddr = tmem + (uint32_t)(b * NCOLS) + ((uint32_t)(32 * e) << 16);
-      epi.tile(ea, N, taddr, row0, M, lane, sEpi, sb, &tmO);
+      epi.tile(ea, N, taddr, row0, M, lane, sEpi, sr, &tmO, pre);
       tc::fence_before_sync();
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(acce + b)) : "memory");
     }
@@ -560,10 +591,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int64_t tl = q / KS;
         const int ks = (int)(q - tl * KS);
         const int y = (int)(((int64_t)blockIdx.x + tl * gridDim.x) * BM);
-        uint8_t* hi = sRing + slot * SLOT_BYTES;
+        uint8_t* hi = sRing + slot * TILE_BYTES;
         tc::mbar_expect_tx(landed + slot, TILE_BYTES);
-#pragma unroll
-        for (int c = 0; c < KCH; ++c) tma_load_2d(hi + c * COL_BYTES, &tmA, ks * BK + 4 * c, y, landed + slot);
+        tma_load_2d(hi, &tmA, ks * BK, y, landed + slot);
       }
       // No copy may still be writing shared memory when the CTA exits (the converters
       // wait for every stage unless a wait gave up).
@@ -593,27 +623,27 @@ __global__ void __launch_bounds__(THREADS, 1)
       tc::fence_after_sync();
       const uint32_t d = tmem + (uint32_t)(b * NCOLS);
       for (int ks = 0; ks < KS; ++ks, ++q) {
-        const int slot = (int)(q % slots);
+        const int slot = (int)(q % slots), lj = (int)(q % LO_SLOTS);
         if (!tc::mbar_wait(full + slot, (uint32_t)((q / slots) & 1), WAIT_LIMIT)) {
           atomicOr(&g_tc_status, 1);
           ok = false;
           break;
         }
         tc::fence_after_sync();
-        const uint32_t a_hi = tc::smem_u32(sRing + slot * SLOT_BYTES), a_lo = a_hi + TILE_BYTES;
+        const uint32_t a_hi = tc::smem_u32(sRing + slot * TILE_BYTES), a_lo = tc::smem_u32(sLo + lj * TILE_BYTES);
         const int kleft = K - ks * BK;
         const int steps = (kleft >= BK ? BK : kleft + 7) / 8;
         for (int s = 0; s < steps; ++s) {
-          // A: [16-byte column][row] (LBO = one column, SBO = 8 rows); B: packed image.
+          // A: 128-byte-swizzled rows, K step s at byte 32 s of the atom; B: packed image.
           const uint32_t kb = (uint32_t)(ks * KCH + 2 * s) * 128;
-          const uint64_t ah = tc::sdesc(a_hi + 2 * s * COL_BYTES, COL_BYTES, 128);
-          const uint64_t al = tc::sdesc(a_lo + 2 * s * COL_BYTES, COL_BYTES, 128);
+          const uint64_t ah = sdesc_sw128(a_hi + 32 * s), al = sdesc_sw128(a_lo + 32 * s);
           const uint64_t bh = tc::sdesc(b_hi + kb, 128, sbo_b), bl = tc::sdesc(b_lo + kb, 128, sbo_b);
           tc::mma_tf32(d, ah, bh, IDESC, (ks > 0 || s > 0) ? 1u : 0u);
           tc::mma_tf32(d, ah, bl, IDESC, 1u);
           tc::mma_tf32(d, al, bh, IDESC, 1u);
         }
         tc::mma_commit(empty + slot);
+        tc::mma_commit(lo_empty + lj);
       }
       if (!ok) break;
       tc::mma_commit(accf + b);
