@@ -38,6 +38,7 @@ __device__ __forceinline__ bool vec_ok(const float* p, int n, int N) {
 }
 
 struct EpiStore {
+  static constexpr bool kColumns = false;
   float* C;
   int ldc;
   __device__ void operator()(int64_t m, int n, float v) const { C[m * ldc + n] = v; }
@@ -49,6 +50,7 @@ struct EpiStore {
 };
 // act: 0 none, 1 relu, 2 sigmoid
 struct EpiBiasAct {
+  static constexpr bool kColumns = false;
   float* C;
   int ldc;
   const float* bias;
@@ -68,6 +70,7 @@ struct EpiBiasAct {
 };
 // C = v * (H > 0): backward through a ReLU whose output is H.
 struct EpiReluMask {
+  static constexpr bool kColumns = false;
   float* C;
   int ldc;
   const float* H;
@@ -88,6 +91,7 @@ struct EpiReluMask {
   }
 };
 struct EpiAtomic {
+  static constexpr bool kColumns = false;
   float* C;
   int ldc;
   __device__ void operator()(int64_t m, int n, float v) const { atomicAdd(C + m * ldc + n, v); }
@@ -95,6 +99,25 @@ struct EpiAtomic {
     float* p = C + m * ldc + n;
     if (vec_ok(p, n, N)) atomicAdd(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
     else vec4_scalar(*this, m, n, v, N);
+  }
+};
+// C[n * ldc + m] += v: accumulates the transpose of the product (a weight gradient
+// computed as dY^T X, so that each activation is read once). vec4_col gets rows
+// m..m+3 of column n (clipped at M).
+struct EpiAtomicT {
+  static constexpr bool kColumns = true;
+  float* C;
+  int ldc;
+  __device__ void operator()(int64_t m, int n, float v) const { atomicAdd(C + (int64_t)n * ldc + m, v); }
+  __device__ void vec4_col(int64_t m, int n, const float (&v)[4], int64_t M) const {
+    float* p = C + (int64_t)n * ldc + m;
+    if (m + 3 < M && (reinterpret_cast<uintptr_t>(p) & 15) == 0) {
+      atomicAdd(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (m + j < M) atomicAdd(p + j, v[j]);
+    }
   }
 };
 }  // namespace
@@ -646,12 +669,14 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     e1.colsum = g.b1;
     TVM_TRY((pgemm<pg::EPI_MASK_COLSUM, 128>(M, 128, 128, b.dH2, 128, b.img[3], e1, st)));
     TVM_TRY((mm<true, false>(d.math, 128, 128, M, b.H1, 128, b.dH2, 128, EpiAtomic{g.w2, 128}, st, kc)));
+    // dW1 = X1^T dH1 is computed transposed (dH1^T X1: the output width is the M of one
+    // 128-row tile, so each activation is read once).
     pg::EpiArgs e0{};
     e0.out = b.dH0;
     e0.H = b.X1;
     e0.ldh = pg::LDX1;
     TVM_TRY((pgemm<pg::EPI_PE_BWD, PMLP_NT_DX1>(M, pg::PED, 128, b.dH1, 128, b.img[4], e0, st)));
-    TVM_TRY((mm<true, false>(d.math, d.enc, 128, M, b.X1, pg::LDX1, b.dH1, 128, EpiAtomic{g.w1, 128}, st, kc)));
+    TVM_TRY((mm<true, false>(d.math, 128, d.enc, M, b.dH1, 128, b.X1, pg::LDX1, EpiAtomicT{g.w1, 128}, st, kc)));
     TVM_TRY((mm<true, false>(d.math, d.feat, d.squash, M, X0, d.feat, b.dH0, pg::LDH0, EpiAtomic{g.w0, d.squash},
                              st, kc)));
     if (dX0) {

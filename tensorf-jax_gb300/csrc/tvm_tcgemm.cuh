@@ -266,15 +266,31 @@ __global__ void __launch_bounds__(THREADS) tc_gemm_kernel(int64_t M, int N, int6
 #pragma unroll
       for (int j = 0; j < 16; ++j) buf[lane * 17 + j] = v[j];
       __syncwarp();
+      if constexpr (Epi::kColumns) {
+        // Four consecutive rows of one column per thread (the epilogue writes D^T).
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int idx = q * 32 + lane;
-        const int r = idx >> 2, c4 = (idx & 3) * 4;
-        const int64_t row = m0 + sub * 32 + r;
-        const int64_t col = n0 + ch * 16 + c4;
-        if (row < M && col < N) {
-          const float w4[4] = {buf[r * 17 + c4], buf[r * 17 + c4 + 1], buf[r * 17 + c4 + 2], buf[r * 17 + c4 + 3]};
-          epi.vec4(row, (int)col, w4, N);
+        for (int q = 0; q < 4; ++q) {
+          const int idx = q * 32 + lane;
+          const int c = idx >> 3, r4 = (idx & 7) * 4;
+          const int64_t row = m0 + sub * 32 + r4;
+          const int64_t col = n0 + ch * 16 + c;
+          if (row < M && col < N) {
+            const float w4[4] = {buf[r4 * 17 + c], buf[(r4 + 1) * 17 + c], buf[(r4 + 2) * 17 + c],
+                                 buf[(r4 + 3) * 17 + c]};
+            epi.vec4_col(row, (int)col, w4, M);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int idx = q * 32 + lane;
+          const int r = idx >> 2, c4 = (idx & 3) * 4;
+          const int64_t row = m0 + sub * 32 + r;
+          const int64_t col = n0 + ch * 16 + c4;
+          if (row < M && col < N) {
+            const float w4[4] = {buf[r * 17 + c4], buf[r * 17 + c4 + 1], buf[r * 17 + c4 + 2], buf[r * 17 + c4 + 3]};
+            epi.vec4(row, (int)col, w4, N);
+          }
         }
       }
       __syncwarp();
