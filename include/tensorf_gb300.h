@@ -275,7 +275,7 @@ TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const f
  *
  * Limit: n is at most the number of rows whose tvm_mlp_fwd workspace fits the array.
  * For the default TVM_F32 model (144 features, 27 squash, 2/2 frequencies, 128
- * units) that is 9,950 rows. A TVM_BF16 model with those dimensions runs the fused
+ * units) that is 11,822 rows. A TVM_BF16 model with those dimensions runs the fused
  * kernel: it needs only the 87,040-byte packed weights, so n is not limited. Larger n
  * returns TVM_ERR_SHAPE before any launch, and the message gives the maximum for the
  * model.

@@ -1,15 +1,19 @@
-// FeatureMlp (networks.py:38-121) in FP32: the plain-precision path.
+// FeatureMlp (networks.py:38-121) for the FP32 and the generic paths.
 //
 //   H0 = X0 @ W0                      (3C -> 27, no bias; the folded basis matrix)
 //   X1 = [H0, d, PE(H0), PE(d)]       (networks.py:68-76; PE per networks.py:13-35)
 //   H1 = relu(X1 @ W1 + b1), H2 = relu(H1 @ W2 + b2), rgb = sigmoid(H2 @ W3 + b3)
 //
-// Layered design: each dense layer is one tiled FP32 SIMT GEMM (64x64 tile, 16-deep
-// k-slices staged in shared memory, 4x4 outputs per thread) with its bias / ReLU /
-// sigmoid / ReLU-mask epilogue fused; the Fourier encoding and its backward are
-// elementwise kernels. Weight gradients are split-K GEMMs X^T @ dY over row chunks
-// with one atomic per output per chunk. Activations (H0..H2) are kept in the
-// workspace for the backward.
+// Three implementations, chosen by the model:
+//   - BF16 models with the reference widths: the fused tcgen05 kernels of
+//     tvm_mlpfused.cu (no activations kept);
+//   - FP32 models with the reference widths (27 squash features, 2 frequencies, 128
+//     units): split-tf32 products on the persistent pipelined GEMM of tvm_pgemm.cuh with
+//     the encoding, layer 3, ReLU masks and bias sums fused into its epilogues, a
+//     one-pass layer-3 backward, and split-K tcgen05 weight gradients;
+//   - any other widths: layered products (tcgen05 bf16 / split-tf32 GEMMs of
+//     tvm_tcgemm.cuh, or FP32 SIMT), elementwise encoding kernels and column sums.
+// Activations needed by the backward are kept in the caller's workspace.
 #include <algorithm>
 #include <type_traits>
 
