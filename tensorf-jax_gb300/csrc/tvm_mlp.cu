@@ -420,8 +420,9 @@ template <int KIND, int NT>
 static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uint8_t* bimg, const pg::EpiArgs& ea,
                  cudaStream_t st, int ocols = 0) {
   if (M == 0) return TVM_OK;
-  constexpr bool tma_out = KIND == pg::EPI_BIAS_RELU || KIND == pg::EPI_BIAS_RELU_L3 ||
-                           KIND == pg::EPI_MASK_COLSUM || KIND == pg::EPI_PE_FWD;
+  const bool tma_out = KIND == pg::EPI_BIAS_RELU || KIND == pg::EPI_BIAS_RELU_L3 || KIND == pg::EPI_MASK_COLSUM ||
+                       KIND == pg::EPI_PE_FWD ||
+                       (KIND == pg::EPI_STORE && aligned(ea.out, 16) && ea.ldo % 4 == 0);
   TVM_REQUIRE(aligned(bimg, 16) && N <= NT && K > 0 && M <= INT32_MAX &&
                   ((KIND != pg::EPI_BIAS_RELU && KIND != pg::EPI_BIAS_RELU_L3 && KIND != pg::EPI_MASK_COLSUM) ||
                    N == NT),

@@ -136,7 +136,7 @@ enum EpiKind : int {
   EPI_PE_FWD = 2,        // X1 row = [h, d, PE(h), PE(d), 0 pad] from h = acc (N = 27)
   EPI_MASK_COLSUM = 3,   // out = acc * [H > 0] (H's ReLU bits); colsum += out    (dH1, db1)
   EPI_PE_BWD = 4,        // dH0 = acc[h] + d PE / d h . acc[PE(h)]        (dX1 -> dH0)
-  EPI_STORE = 5,         // out = acc                                      (dX0)
+  EPI_STORE = 5,         // out = acc (TMA-stored when out is 16-byte aligned)   (dX0)
 };
 
 struct EpiArgs {
@@ -412,18 +412,24 @@ struct Epilogue {
           }
         }
       };
+      // TMA stores when the host gave store blocks (an aligned output), else direct ones.
+      const bool tma = sr.nsb > 0;
 #pragma unroll
       for (int c = 0; c < NCH; c += 2) {
         float v[16], w[16];
         if (c + 1 < NCH) {
           tc::tmem_ld16x2(taddr + c * 16, taddr + c * 16 + 16, v, w);
-          if (valid) {
+          if (tma) {
+            put_block(sr, v, tm, c * 16, (int)row0, lane);
+            put_block(sr, w, tm, c * 16 + 16, (int)row0, lane);
+          } else if (valid) {
             put16(c * 16, v);
             put16(c * 16 + 16, w);
           }
         } else {
           tc::tmem_ld16(taddr + c * 16, v);
-          if (valid) put16(c * 16, v);
+          if (tma) put_block(sr, v, tm, c * 16, (int)row0, lane);
+          else if (valid) put16(c * 16, v);
         }
       }
     }
