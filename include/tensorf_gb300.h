@@ -51,7 +51,7 @@ extern "C" {
 #define TVM_ERR_SHAPE (-2)       /* sizes out of the supported range */
 #define TVM_ERR_DTYPE (-3)       /* unsupported dtype / dtype combination */
 #define TVM_ERR_ALIGN (-4)       /* pointer not aligned as the layout requires */
-#define TVM_ERR_UNSUPPORTED (-5) /* valid request this build does not implement */
+#define TVM_ERR_UNSUPPORTED (-5) /* valid request the library does not implement */
 #define TVM_ERR_LAUNCH (-6)      /* CUDA launch or runtime error */
 #define TVM_ERR_NONFINITE (-7)   /* non-finite value detected */
 #define TVM_ERR_TIMEOUT (-8)     /* a bounded device wait gave up */

@@ -1,7 +1,7 @@
 """CPU oracle for the TensoRF-VM render-and-train hot path.
 
 TEST INFRASTRUCTURE ONLY. Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` may import this module, and only as the checker (or as
+baseline leg of ``bench.py`` may import this module, and only to check results (or as
 the timed CPU restatement). The product path never calls it.
 
 What it is: a line-by-line restatement, in PyTorch on the CPU, of brentyi/tensorf-jax's
