@@ -1,7 +1,8 @@
 """GPU tests of the FP32 FeatureMlp entry points (tvm_mlp_fwd / tvm_mlp_bwd) on the
 split-tf32 pipelined GEMM path, against the float64 oracle (networks.py:45-121):
 
-- row counts around the 128-row tile and past one tile per SM, for rgb, the feature
+- row counts around the 128-row tile and past one tile per SM, and appearance widths
+  other than 48 components, for rgb, the feature
   gradient and every weight and bias gradient (the bias and layer-3 gradients come from
   fused epilogues and a one-pass kernel, so each is checked on its own); rows with a
   hidden pre-activation within 1e-4 of a ReLU kink are redrawn;
@@ -27,12 +28,12 @@ def _rel(a, b):
     return float((a - b).abs().max() / (b.abs().max() + 1e-30))
 
 
-def _model(seed):
+def _model(seed, ca=48):
     from tensorf_gb300 import render
-    spec = render.ModelSpec(grid_dim=8, precision="fp32")
+    spec = render.ModelSpec(grid_dim=8, appearance_feat_dim=ca, precision="fp32")
     gen = torch.Generator().manual_seed(seed)
-    ref = {"density": O.vm_init(8, 16, gen, torch.float32), "appearance": O.vm_init(8, 48, gen, torch.float32),
-           "mlp": O.mlp_init(144, 2, 2, gen, dtype=torch.float32)}
+    ref = {"density": O.vm_init(8, 16, gen, torch.float32), "appearance": O.vm_init(8, ca, gen, torch.float32),
+           "mlp": O.mlp_init(3 * ca, 2, 2, gen, dtype=torch.float32)}
     for layer in ("Dense_1", "Dense_2", "Dense_3"):  # non-zero biases, so their gradients matter
         b = ref["mlp"][layer]["bias"]
         b.copy_(torch.randn(b.shape, generator=gen) * 0.1)
@@ -46,9 +47,10 @@ def _inputs(n, seed, ref):
     drawn again rather than compared."""
     gen = torch.Generator().manual_seed(seed)
     W = {k: {nm: t.double() for nm, t in d.items()} for k, d in ref["mlp"].items()}
+    feat = W["Dense_0"]["kernel"].shape[0]
     keep_f, keep_d = [], []
     while sum(len(t) for t in keep_f) < n:
-        feats = torch.randn((2 * n + 8, 144), generator=gen) * 0.3
+        feats = torch.randn((2 * n + 8, feat), generator=gen) * 0.3
         dirs = torch.nn.functional.normalize(torch.randn((2 * n + 8, 3), generator=gen), dim=-1)
         f = feats.double() @ W["Dense_0"]["kernel"]
         x1 = torch.cat([f, dirs.double(), O.fourier_encode(f, 2), O.fourier_encode(dirs.double(), 2)], dim=-1)
@@ -80,7 +82,8 @@ def _run(lp, feats, dirs, grad_rgb, out_offset=False):
     rgb = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     _lib.call("tvm_mlp_fwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(rgb), ptr(ws),
               ws.numel(), stream_handle())
-    gfeat = _offset(torch.zeros((n, 144))) if out_offset else torch.zeros((n, 144), device="cuda")
+    feat = feats.shape[1]
+    gfeat = _offset(torch.zeros((n, feat))) if out_offset else torch.zeros((n, feat), device="cuda")
     grads = torch.zeros_like(lp.params)
     _lib.call("tvm_mlp_bwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(grad_rgb), ptr(gfeat),
               ptr(grads), ptr(ws), ws.numel(), stream_handle())
@@ -91,10 +94,8 @@ def _run(lp, feats, dirs, grad_rgb, out_offset=False):
     return rgb, gfeat, lp.mlp_views(grads)
 
 
-@pytest.mark.parametrize("n", [1, 127, 128, 129, 1000, 152 * 128 + 77])
-def test_fp32_mlp_matches_oracle_at_tile_edges(n):
-    _, ref, lp = _model(7)
-    feats, dirs, grad_rgb = _inputs(n, 1000 + n, ref)
+def _check_against_oracle(ref, lp, n, seed):
+    feats, dirs, grad_rgb = _inputs(n, seed, ref)
     rgb, gfeat, got = _run(lp, feats.cuda(), dirs.cuda(), grad_rgb.cuda())
 
     mlp64 = {k: {nm: t.double().requires_grad_(True) for nm, t in d.items()} for k, d in ref["mlp"].items()}
@@ -107,6 +108,20 @@ def test_fp32_mlp_matches_oracle_at_tile_edges(n):
         for name, t in v.items():
             err = _rel(got[layer][name], t.grad)
             assert err < GRAD_RTOL, (layer, name, err)
+
+
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 1000, 152 * 128 + 77])
+def test_fp32_mlp_matches_oracle_at_tile_edges(n):
+    _, ref, lp = _model(7)
+    _check_against_oracle(ref, lp, n, 1000 + n)
+
+
+@pytest.mark.parametrize("ca", [8, 16, 24])
+def test_fp32_mlp_other_appearance_widths(ca):
+    """3 C appearance features other than 144: 24, 48 and the reference's default 72
+    (train_config.py:44-45), with a narrower first product and a padded dX0 tile."""
+    _, ref, lp = _model(9, ca)
+    _check_against_oracle(ref, lp, 1000, 77 + ca)
 
 
 def test_fp32_mlp_unaligned_buffers_match_aligned():
