@@ -273,16 +273,21 @@ TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const f
  *   - code that must not stall other streams, because cudaFree synchronises the
  *     device.
  *
- * Limit: n is at most the number of rows whose tvm_mlp_fwd workspace fits the array.
- * For the default TVM_F32 model (144 features, 27 squash, 2/2 frequencies, 128
- * units) that is 11,822 rows. A TVM_BF16 model with those dimensions runs the fused
- * kernel: it needs only the 87,040-byte packed weights, so n is not limited. Larger n
- * returns TVM_ERR_SHAPE before any launch, and the message gives the maximum for the
- * model.
+ * Limit: n is at most the number of rows whose forward scratch (the part of the
+ * tvm_mlp_fwd workspace the forward writes) fits the array. For the default TVM_F32
+ * model (144 features, 27 squash, 2/2 frequencies, 128 units) that is 20,164 rows. A
+ * TVM_BF16 model with those dimensions runs the fused kernel: it needs only the
+ * 87,040-byte packed weights, so n is not limited. Larger n returns TVM_ERR_SHAPE
+ * before any launch, and the message gives the maximum for the model.
+ *
+ * Alignment: params must be 16-byte aligned (TVM_ERR_ALIGN otherwise). TVM_F32
+ * models accept any features pointer; TVM_BF16 models read features with 16-byte
+ * loads and return TVM_ERR_ALIGN when it is not 16-byte aligned, as tvm_mlp_fwd does.
  *
  * Set-up: the first call with a device current looks up the array's device address
  * for that device. That lookup may load the library's module and reserve the array.
- * Make that first call before any stream capture.
+ * Make that first call before any stream capture. The address is kept for the life
+ * of the process: do not call this function on a device after cudaDeviceReset.
  *
  * Calls whose GPU work overlaps race on the shared array: different streams, or
  * different threads, with no ordering between them. Order them on one stream or with

@@ -4,7 +4,10 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "tvm_internal.h"
 
@@ -33,6 +36,43 @@ int check_launch(const char* what) {
     set_error("%s: %s", what, cudaGetErrorString(e));
     return TVM_ERR_LAUNCH;
   }
+  return TVM_OK;
+}
+
+// Per-device launch set-up. Both tables are keyed by device ordinal: a kernel's
+// shared-memory limit and the SM count belong to one device, and a process may drive
+// several.
+static std::mutex g_setup_mu;
+
+static int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  return dev;
+}
+
+int device_sms() {
+  static std::vector<int> sms;
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  if ((int)sms.size() <= dev) sms.resize(dev + 1, 0);
+  if (sms[dev] == 0) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = n > 0 ? n : 1;
+  }
+  return sms[dev];
+}
+
+int ensure_smem_limit(const void* fn, int bytes, const char* what) {
+  static std::map<std::pair<int, const void*>, int> raised;  // (device, kernel) -> bytes
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  int& have = raised[{dev, fn}];
+  if (have >= bytes) return TVM_OK;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "%s: shared-memory attribute (%d bytes): %s", what, bytes,
+              cudaGetErrorString(e));
+  have = bytes;
   return TVM_OK;
 }
 
@@ -723,10 +763,13 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
 // fused path's packed bf16 weights, laid out exactly as for tvm_mlp_fwd) lives in one
 // static device array owned by this file.
 //
-// The array holds TVM_MLP_STATIC_SCRATCH_BYTES (32 MiB). Its device address is
-// looked up once per device, by the first call made with that device current
-// (cudaGetSymbolAddress, which may load this module and so reserve the array); that
-// first call should come before any stream capture. Later calls only launch kernels.
+// The array holds TVM_MLP_STATIC_SCRATCH_BYTES (32 MiB), and a call may use it for the
+// forward's buffers only (mlp_fwd_workspace_bytes), not the backward's. Its device
+// address is looked up once per device, by the first call made with that device
+// current (cudaGetSymbolAddress, which may load this module and so reserve the array);
+// that first call should come before any stream capture. Later calls only launch
+// kernels. The address is kept for the life of the process, so the entry point must
+// not be used on a device after cudaDeviceReset there.
 //
 // Every call on a device shares the one array, so calls whose GPU work overlaps
 // (different streams, or different host threads, without an ordering between them)
@@ -768,7 +811,7 @@ static int64_t static_scratch_max_rows(const MlpDims& d) {
   int64_t lo = 0, hi = int64_t(1) << 32;
   while (lo < hi) {
     const int64_t mid = lo + (hi - lo + 1) / 2;
-    if (mlp_workspace_bytes(d, mid) <= kMlpStaticScratchBytes) lo = mid;
+    if (mlp_fwd_workspace_bytes(d, mid) <= kMlpStaticScratchBytes) lo = mid;
     else hi = mid - 1;
   }
   return lo;
@@ -783,15 +826,14 @@ int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params, 
   TVM_TRY(validate_model(model));
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
   const MlpDims d = mlp_dims(*model);
-  const size_t need = mlp_workspace_bytes(d, n);
+  const size_t need = mlp_fwd_workspace_bytes(d, n);
   TVM_REQUIRE(need <= kMlpStaticScratchBytes, TVM_ERR_SHAPE,
               "n=%lld rows need %zu bytes of MLP scratch; the static scratch holds %zu bytes, "
               "at most %lld rows for this model",
               (long long)n, need, kMlpStaticScratchBytes, (long long)static_scratch_max_rows(d));
   if (n == 0) return TVM_OK;
   TVM_REQUIRE(params && features && viewdirs && rgb, TVM_ERR_INVALID, "NULL pointer");
-  TVM_REQUIRE(aligned(params, 16) && aligned(features, 16), TVM_ERR_ALIGN,
-              "params and features must be 16-byte aligned");
+  TVM_REQUIRE(aligned(params, 16), TVM_ERR_ALIGN, "params must be 16-byte aligned");
   void* scratch = nullptr;
   TVM_TRY(static_scratch_address(&scratch));
   tvm_param_layout L;

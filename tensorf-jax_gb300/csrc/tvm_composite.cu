@@ -381,13 +381,7 @@ static int warps_for_smem(size_t per_warp, int max_warps = 8) {
 }
 
 static int set_smem(const void* fn, size_t bytes) {
-  if (bytes > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) {
-      set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-      return TVM_ERR_LAUNCH;
-    }
-  }
+  if (bytes > 48 * 1024) return ensure_smem_limit(fn, (int)bytes, "compositing");
   return TVM_OK;
 }
 

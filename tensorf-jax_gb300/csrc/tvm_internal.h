@@ -8,6 +8,14 @@
 
 namespace tvm {
 
+// ---- per-device launch set-up (tvm_api.cu) ----
+// SM count of the current device (looked up once per device).
+int device_sms();
+// Raise fn's dynamic shared-memory limit to at least `bytes` on the current device.
+// Kernel attributes are per device, so this is done once per (device, kernel); safe to
+// call from several host threads.
+int ensure_smem_limit(const void* fn, int bytes, const char* what);
+
 // Field view with a typed storage pointer (dtype decides the cast).
 struct FieldView {
   int G, C, dtype;
@@ -78,7 +86,8 @@ struct MlpWeights {
 struct MlpGrads {
   float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
 };
-size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);
+size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);      // forward + backward
+size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M);  // forward only (a prefix of the above)
 // rgb = FeatureMlp(X0, viewdir). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...].
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st);

@@ -356,19 +356,6 @@ static PmlpImages pmlp_images(const MlpDims& d) {
   return im;
 }
 
-static int num_sms() {
-  static int cached[64] = {};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (cached[dev] == 0) {
-    int n = 0;
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cached[dev] = n > 0 ? n : 1;
-  }
-  return cached[dev];
-}
-
 static int pack_images(const pg::PackJob* jobs, int count, cudaStream_t st) {
   pg::PackList list{};
   int most = 0;
@@ -453,14 +440,9 @@ static int pgemm(int64_t M, int N, int K, const float* A, int64_t lda, const uin
   TVM_REQUIRE(slots >= 2, TVM_ERR_UNSUPPORTED, "pgemm: K=%d, N=%d leaves %d pipeline slots", K, NT, slots);
   const int bytes = std::max(base + slots * pg::TILE_BYTES + stage, pg::MIN_SMEM);
   auto fn = pg::pgemm_kernel<KIND, NT>;
-  static bool attr_done = false;  // per instantiation
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pg::SMEM_LIMIT);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pgemm smem attribute: %s", cudaGetErrorString(e));
-    attr_done = true;
-  }
+  TVM_TRY(ensure_smem_limit((const void*)fn, pg::SMEM_LIMIT, "pgemm"));
   const int64_t tiles = ceil_div(M, pg::BM);
-  const unsigned grid = (unsigned)std::min<int64_t>(tiles, num_sms());
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, device_sms());
   fn<<<grid, pg::THREADS, bytes, st>>>(M, N, K, tmA, tmO, bimg, slots, nsb, ea);
   return check_launch("pgemm");
 }
@@ -543,14 +525,16 @@ __global__ void __launch_bounds__(L3_THREADS) l3_bwd_kernel(int64_t M, const flo
   if (tid < 3) atomicAdd(gb3 + tid, sB3[tid]);
 }
 
-// Workspace carve-out shared by forward and backward (same order).
+// Workspace carve-out shared by forward and backward. The buffers the forward writes
+// come first, so a forward-only carve is a prefix of the full one and a forward
+// followed by a backward on the same workspace sees the same addresses.
 struct MlpBufs {
   float *X1, *H1, *H2, *dH2, *dH1, *dX1, *dH0;
   uint8_t* wpack;
   uint8_t* img[6];
   uint32_t* mask1;  // ReLU bits of H1 (4 words per row), for the dH1 product
 };
-static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
+static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws, bool fwd_only) {
   MlpBufs b{};
   if (mlp_fused_supported(d)) {  // the fused kernels keep every activation on chip
     b.wpack = ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes());
@@ -558,19 +542,22 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
   }
   if (pmlp_supported(d)) {
     const PmlpImages im = pmlp_images(d);
-    for (int i = 0; i < 6; ++i) b.img[i] = ws.take<uint8_t>(im.bytes[i]);
+    for (int i = 0; i < 3; ++i) b.img[i] = ws.take<uint8_t>(im.bytes[i]);
     b.X1 = ws.take<float>(M * pg::LDX1);
     b.H1 = ws.take<float>(M * 128);
     b.H2 = ws.take<float>(M * 128);
+    b.mask1 = ws.take<uint32_t>(M * 4);
+    if (fwd_only) return b;
+    for (int i = 3; i < 6; ++i) b.img[i] = ws.take<uint8_t>(im.bytes[i]);
     b.dH2 = ws.take<float>(M * 128);
     b.dH1 = ws.take<float>(M * 128);
     b.dH0 = ws.take<float>(M * pg::LDH0);
-    b.mask1 = ws.take<uint32_t>(M * 4);
     return b;
   }
   b.X1 = ws.take<float>(M * ld_x1(d));
   b.H1 = ws.take<float>(M * d.units);
   b.H2 = ws.take<float>(M * d.units);
+  if (fwd_only) return b;
   b.dH2 = ws.take<float>(M * d.units);
   b.dH1 = ws.take<float>(M * d.units);
   b.dX1 = ws.take<float>(M * ld_x1(d));
@@ -580,14 +567,19 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws) {
 
 size_t mlp_workspace_bytes(const MlpDims& d, int64_t M) {
   Workspace ws{nullptr, 0, 0, true};
-  carve(d, M, ws);
+  carve(d, M, ws, false);
   return ws.used + 256;
 }
 
+size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M) {
+  Workspace ws{nullptr, 0, 0, true};
+  carve(d, M, ws, true);
+  return ws.used + 256;
+}
 
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st) {
-  MlpBufs b = carve(d, M, ws);
+  MlpBufs b = carve(d, M, ws, true);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
     return TVM_ERR_WORKSPACE;
@@ -646,7 +638,7 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
 
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                  int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st) {
-  MlpBufs b = carve(d, M, ws);
+  MlpBufs b = carve(d, M, ws, false);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
     return TVM_ERR_WORKSPACE;
@@ -663,7 +655,7 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
                                  {w.w0, d.squash, d.squash, d.feat, pg::kpad(pg::SQ), ntx, 1, b.img[5]}};
     TVM_TRY(pack_images(jobs, 3, st));
     if (M > 0) {
-      const unsigned blocks = (unsigned)std::min<int64_t>(2 * num_sms(), ceil_div(M, 4 * (L3_THREADS / 32)));
+      const unsigned blocks = (unsigned)std::min<int64_t>(2 * device_sms(), ceil_div(M, 4 * (L3_THREADS / 32)));
       l3_bwd_kernel<<<blocks, L3_THREADS, 0, st>>>(M, b.H2, dZ3, w.w3, b.dH2, g.w3, g.b3, g.b2);
       TVM_TRY(check_launch("l3_bwd"));
     }
@@ -780,9 +772,5 @@ int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const floa
 #undef TVM_GEMM_CASE
   return TVM_ERR_INVALID;
 }
-
-}  // namespace tvm
-
-namespace tvm {
 
 }  // namespace tvm

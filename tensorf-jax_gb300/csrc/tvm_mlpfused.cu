@@ -775,22 +775,10 @@ size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
                          int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st) {
   if (M == 0) return TVM_OK;
-  static int sms = 0;
-  static bool attr = false;
-  if (!attr) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaFuncSetAttribute(fmlp::mlp_fwd_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         fmlp::SMEM);
-    if (e != cudaSuccess) {
-      set_error("fused mlp smem attribute: %s", cudaGetErrorString(e));
-      return TVM_ERR_LAUNCH;
-    }
-    attr = true;
-  }
-  if (!aligned(wpack, 16)) {
-    set_error("packed weights must be 16-byte aligned");
+  TVM_TRY(ensure_smem_limit((const void*)fmlp::mlp_fwd_fused_kernel, fmlp::SMEM, "fused mlp"));
+  const int sms = device_sms();
+  if (!aligned(wpack, 16) || !aligned(X0, 16)) {  // both are read with 16-byte loads
+    set_error("fused mlp: packed weights and features must be 16-byte aligned");
     return TVM_ERR_ALIGN;
   }
   fmlp::pack_weights_kernel<<<64, 256, 0, st>>>(wpack, w.w0, w.w1, w.w2, w.w3);
@@ -806,20 +794,8 @@ int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0
                          int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
                          cudaStream_t st) {
   if (M == 0) return TVM_OK;
-  static int sms = 0;
-  static bool attr = false;
-  if (!attr) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaFuncSetAttribute(fmlp::bwd::mlp_bwd_fused_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, fmlp::bwd::SMEM);
-    if (e != cudaSuccess) {
-      set_error("fused mlp backward smem attribute: %s", cudaGetErrorString(e));
-      return TVM_ERR_LAUNCH;
-    }
-    attr = true;
-  }
+  TVM_TRY(ensure_smem_limit((const void*)fmlp::bwd::mlp_bwd_fused_kernel, fmlp::bwd::SMEM, "fused mlp backward"));
+  const int sms = device_sms();
   if (!aligned(wpack, 16) || !aligned(X0, 16) || (dX0 && !aligned(dX0, 16))) {
     set_error("fused mlp backward: packed weights, features and dX0 must be 16-byte aligned");
     return TVM_ERR_ALIGN;

@@ -754,20 +754,8 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
   if (n == 0) return TVM_OK;
   const int U = mlp.units;
   if (f.dtype == TVM_BF16 && U == ptc::U) {
-    static int sms = 0;
-    static bool attr = false;
-    if (!attr) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaError_t e = cudaFuncSetAttribute(ptc::prop_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           ptc::SMEM);
-      if (e != cudaSuccess) {
-        set_error("proposal backward smem attribute: %s", cudaGetErrorString(e));
-        return TVM_ERR_LAUNCH;
-      }
-      attr = true;
-    }
+    TVM_TRY(ensure_smem_limit((const void*)ptc::prop_bwd_tc_kernel, ptc::SMEM, "proposal backward"));
+    const int sms = device_sms();
     const int64_t tiles = ceil_div(n, ptc::THREADS);
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * std::max(sms, 1));  // 2 CTAs fit an SM
     ptc::prop_bwd_tc_kernel<<<grid, ptc::THREADS, ptc::SMEM, st>>>(
@@ -779,13 +767,13 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
   const unsigned blocks = (unsigned)ceil_div(n, PBWD_THREADS);
   if (f.dtype == TVM_BF16) {
     auto fn = prop_bwd_kernel<__nv_bfloat16>;
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines,
                                            gplanes, origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2,
                                            gw1, gb1, gw2, gb2);
   } else {
     auto fn = prop_bwd_kernel<float>;
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines, gplanes,
                                            origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2, gw1, gb1,
                                            gw2, gb2);

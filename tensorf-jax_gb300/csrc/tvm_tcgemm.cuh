@@ -326,15 +326,7 @@ static int tc_gemm(int64_t M, int N, int64_t K, const TA* A, int64_t lda, const 
     constexpr int KC = AT ? 8 : 4;
     using S = tcg::Smem<NT, SPLIT, KC>;
     auto fn = tcg::tc_gemm_kernel<NT, AT, BT, TA, TB, FMT, SPLIT, Epi, KC>;
-    static bool attr_done = false;  // per instantiation
-    if (!attr_done) {
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, S::BYTES);
-      if (e != cudaSuccess) {
-        set_error("tc_gemm smem attribute: %s", cudaGetErrorString(e));
-        return TVM_ERR_LAUNCH;
-      }
-      attr_done = true;
-    }
+    TVM_TRY(ensure_smem_limit((const void*)fn, S::BYTES, "tc_gemm"));
     dim3 grid((unsigned)ceil_div(N, NT), (unsigned)ceil_div(M, tcg::BM), gz);
     fn<<<grid, tcg::THREADS, S::BYTES, st>>>(M, N, K, A, lda, B, ldb, kc, epi);
     return check_launch("tc_gemm");

@@ -149,9 +149,11 @@ def test_workspace_sizes_are_monotone_in_rays():
 @pytest.mark.parametrize("dtype,ca", [(_lib.TVM_F32, 48), (_lib.TVM_F32, 24), (_lib.TVM_BF16, 48)])
 def test_static_scratch_limit_matches_workspace_size(dtype, ca):
     """tvm_mlp_fwd_static_scratch rejects oversized calls on the host, naming the largest
-    row count whose MLP workspace (tvm_mlp_workspace_size less the backward's 24 bytes
-    per row and 1 KB) fits the 32 MiB array. The fused BF16 path needs no per-row
-    scratch, so there the size check passes and the NULL pointers are rejected."""
+    row count whose forward scratch fits the 32 MiB array: that row count passes the
+    size check (and then fails on the NULL pointers), one more row fails it. The
+    forward needs less than the forward + backward workspace of tvm_mlp_workspace_size.
+    The fused BF16 path needs no per-row scratch, so there the size check passes and
+    the NULL pointers are rejected."""
     lib = _lib.load()
     md = _model(dtype=dtype, appearance_channels=ca)
     st = lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), None, None, None, 1 << 40, None, None)
@@ -160,8 +162,7 @@ def test_static_scratch_limit_matches_workspace_size(dtype, ca):
         return
     assert st == -2
     n = int(re.search(r"at most (\d+) rows", lib.tvm_last_error_message().decode()).group(1))
-
-    def need(m):
-        return lib.tvm_mlp_workspace_size(ctypes.byref(md), m) - 24 * m - 1024
-
-    assert 0 < n and need(n) <= (32 << 20) < need(n + 1)
+    assert lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), None, None, None, n, None, None) == -1
+    assert lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), None, None, None, n + 1, None, None) == -2
+    assert lib.tvm_mlp_workspace_size(ctypes.byref(md), n) > (32 << 20)
+    assert 0 < n
