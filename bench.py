@@ -386,6 +386,68 @@ def roofline_for(w, phase_ms):
             "note": "gathers/scatters are L2-resident: algorithmic bytes over the measured HBM copy peak"}
 
 
+def measure_l2_peaks(mb=48, passes=20, launches=5):
+    """L2 read and float4-reduction bandwidth of this GPU (tvm_l2_probe over an
+    L2-resident buffer), GB/s of buffer bytes, best of `launches` timed launches."""
+    from tensorf_gb300 import _lib
+    from tensorf_gb300._util import ptr, stream_handle
+
+    nbytes = mb << 20
+    buf = torch.zeros(nbytes // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for kind, name in ((0, "l2_read_gbs"), (1, "l2_red_gbs")):
+        _lib.call("tvm_l2_probe", kind, ptr(buf), nbytes, 2, stream_handle())  # warm L2
+        best = float("inf")
+        for _ in range(launches):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.call("tvm_l2_probe", kind, ptr(buf), nbytes, passes, stream_handle())
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = round(nbytes * passes / (best / 1e3) / 1e9, 1)
+    out["buffer_mb"] = mb
+    out["how"] = ("tvm_l2_probe: 4 CTAs x 512 threads per SM stream a 48 MiB buffer 20 times per launch with 16-byte "
+                  "L1-bypassing loads (read) or float4 reductions to distinct addresses (red); best of 5 launches")
+    return out
+
+
+def gather_scatter_bytes(w, phase):
+    """(L2 read bytes, L2 reduction bytes) of one launch of a gather or scatter phase."""
+    R, N, k = w["R"], w["N"], w["k"]
+    s = 2 if w["precision"] == "bf16" else 4
+    dens_el, app_el = 18 * w["Cd"], 18 * w["Ca"]
+    return {"density_fwd": (R * N * dens_el * s, 0), "density_bwd": (R * N * dens_el * s, R * N * dens_el * 4),
+            "appearance_fwd": (R * k * app_el * s, 0),
+            "appearance_bwd": (R * k * app_el * s, R * k * app_el * 4)}.get(phase)
+
+
+def kernel_rooflines(w, phase_ms, l2):
+    """Per phase: achieved algorithmic GB/s (or TFLOP/s for the MLP) and its fraction of
+    the peak that bounds it: HBM for Adam, L2 (read + reduction time) for the field
+    gathers and scatters, the tensor pipe for the MLP."""
+    hbm, bf16, _ = measured_peaks()
+    out = {}
+    for ph in ("density_fwd", "appearance_fwd", "density_bwd", "appearance_bwd", "adam", "mlp_fwd", "mlp_bwd"):
+        ms = phase_ms.get(ph)
+        if not ms:
+            continue
+        if ph in ("mlp_fwd", "mlp_bwd"):
+            tf = mlp_flops(w, ph) / (ms / 1e3) / 1e12
+            peak = bf16 if w["precision"] == "bf16" else bf16 / 6.0
+            out[ph] = {"ms": round(ms, 4), "tflops": round(tf, 1), "frac_tensor": round(tf / peak, 3)}
+            continue
+        b = algorithmic_bytes(w, ph)
+        e = {"ms": round(ms, 4), "gbs": round(b / (ms / 1e3) / 1e9, 1),
+             "frac_hbm": round(b / (ms / 1e3) / 1e9 / hbm, 3)}
+        rb = gather_scatter_bytes(w, ph)
+        if rb and l2:
+            t_l2 = rb[0] / (l2["l2_read_gbs"] * 1e9) + rb[1] / (l2["l2_red_gbs"] * 1e9)
+            e["frac_l2"] = round(t_l2 / (ms / 1e3), 3)
+        out[ph] = e
+    return out
+
+
 def run_profile_variant(args):
     """Only one variant's warm-up and timed steps (for profiler launch lists)."""
     from tensorf_gb300 import _lib
@@ -430,6 +492,7 @@ def run_ours(args):
     nph = min(args.steps, 50)
     _, phase_ms, _ = time_train(st_plain, data, nph, 0, phases=True, start_step=args.warmup + args.steps)
     done_plain = args.warmup + args.steps + nph
+    l2 = measure_l2_peaks()
 
     # End to end through the public API: pinned host rays and colours copied in every
     # step, the loss read back every step.
@@ -463,18 +526,15 @@ def run_ours(args):
         "metric": METRIC, "value": round(value, 1), "unit": "rays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (32-sphere analytic scene, FP64 quadrature targets, seeded cameras)",
-        "config": {"workload": f"train step fp32: grid {plain['grid']}^3, VM {plain['Cd']}/{plain['Ca']}, "
-                               f"{plain['R']} rays x {plain['N']} uniform samples, top-{plain['k']} appearance, Adam",
-                   "rays_per_step": plain["R"], "density_samples": plain["N"], "appearance_samples": plain["k"],
-                   "grid": plain["grid"], "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "no flush: each step streams params+grads+Adam moments (277 MB) and >2 GB of per-sample "
-                         "work, both larger than the 126 MB L2"},
+        "data": DATA,
+        "config": headline_config(plain, world),
         "phase_ms": {p: round(v, 4) for p, v in phase_ms.items()},
         "e2e": {"value": round(e2e_value, 1), "unit": "rays/s", "h2d_bytes_per_step": R * 9 * 4,
                 "d2h_bytes_per_step": 4},
         "gpu_launches": launches,
         "roofline": roofline_for(plain, phase_ms),
+        "l2_peaks": l2,
+        "kernels": kernel_rooflines(plain, phase_ms, l2),
         "clocks": clk.summary(),
     }
 
@@ -563,50 +623,121 @@ def run_unbounded(args):
 # ---------------------------------------------------------------------------------
 # CPU: the oracle restatement of the reference algorithm on the host cores.
 # ---------------------------------------------------------------------------------
-def _cpu_step_time(w, rays_sample, seed=0):
-    """Seconds for forward+backward of ``rays_sample`` rays of the workload with the
-    float32 oracle, plus seconds for one Adam update of the full parameter set."""
-    from oracle import tensorf_oracle as O
+class CpuTrainer:
+    """The headline training step run by the float32 oracle on the host cores: the same
+    initial parameters, sphere-scene rays and FP64 quadrature targets as the GPU arm
+    (rebuilt on the host, without the CUDA library), forward + backward by torch
+    autograd, and optax's Adam with its moments kept across steps."""
 
-    gen = torch.Generator().manual_seed(seed)
-    G = w["grid"]
-    p = {"density": O.vm_init(G, w["Cd"], gen, torch.float32), "appearance": O.vm_init(G, w["Ca"], gen, torch.float32),
-         "mlp": O.mlp_init(3 * w["Ca"], 2, 2, gen, dtype=torch.float32)}
-    leaves = [*p["density"], *p["appearance"]] + [t for d in p["mlp"].values() for t in d.values()]
-    for t in leaves:
-        t.requires_grad_(True)
-    rng = np.random.default_rng(seed)
-    o = rng.normal(size=(rays_sample, 3))
-    o = o / np.linalg.norm(o, axis=1, keepdims=True) * 4
-    d = -o + rng.normal(scale=0.05, size=o.shape)
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
-    jit = torch.rand(w["N"], generator=gen)
-    gum = -torch.log(-torch.log(torch.rand(w["N"], generator=gen).clamp_min(1e-7)))
-    col = torch.rand((rays_sample, 3), generator=gen)
-    t0 = time.perf_counter()
-    out = O.render_rays(p, aabb, torch.tensor(o, dtype=torch.float32), torch.tensor(d, dtype=torch.float32),
-                        w["N"], w["k"], jit, gum)
-    loss = O.mse(out, col)
-    grads = torch.autograd.grad(loss, leaves)
-    t1 = time.perf_counter()
-    with torch.no_grad():
-        for t, g in zip(leaves, grads):
-            z = torch.zeros_like(t)
-            O.adam_update(t, g, z, z, 1, lr=0.02, lr_decay=1.0)
-    t2 = time.perf_counter()
-    return t1 - t0, t2 - t1
+    def __init__(self, w, rays_per_step, batches=1, seed=0):
+        from oracle import tensorf_oracle as O
+        from tensorf_gb300 import render, scene
+
+        self.O, self.w, self.R = O, w, rays_per_step
+        spec = render.ModelSpec(grid_dim=w["grid"], density_feat_dim=w["Cd"], appearance_feat_dim=w["Ca"])
+        ref = render.initial_reference_params(spec, seed=94709)
+        self.fields = [*ref["density"], *ref["appearance"]]
+        self.mlp = [t for d in ref["mlp"].values() for t in d.values()]
+        self.params = ref
+        for t in self.fields + self.mlp:
+            t.requires_grad_(True)
+        self.mu = [torch.zeros_like(t) for t in self.fields + self.mlp]
+        self.nu = [torch.zeros_like(t) for t in self.fields + self.mlp]
+        self.count = 0
+        # Rays of the GPU arm's first batches (Data(): scene seed 0, cameras seed 1,
+        # pixels seed 2) and their FP64 quadrature targets.
+        sc = scene.SphereScene.random(seed, count=32)
+        cams = sc.cameras(116, seed=seed + 1)[:100]
+        cam_idx, pix = scene.SphereScene.training_pixels(cams, w["R"] * 64, seed=seed + 2)
+        n = rays_per_step * batches
+        o = np.empty((n, 3))
+        d = np.empty((n, 3))
+        for i, cam in enumerate(cams):
+            sel = np.nonzero(cam_idx[:n] == i)[0]
+            if sel.size:
+                o[sel], d[sel] = O.camera_pixel_rays(cam.K, cam.R_world_camera, cam.t_world_camera,
+                                                     cam.image_width, cam.image_height, pixels=pix[sel])
+        aabb64 = torch.tensor(sc.aabb, dtype=torch.float64)
+        t0, t1 = O.ray_segment_from_bounding_box(torch.tensor(o), torch.tensor(d), aabb64)
+        c = O.sphere_scene_quadrature(o, d, sc.centers, sc.radii, sc.colors, sc.density, t0.numpy(), t1.numpy(),
+                                      4096)
+        self.o = torch.tensor(o, dtype=torch.float32)
+        self.d = torch.tensor(d, dtype=torch.float32)
+        self.c = torch.tensor(c, dtype=torch.float32)
+        self.aabb = torch.tensor(sc.aabb, dtype=torch.float32)
+        self.gen = torch.Generator().manual_seed(seed + 9)
+        self.batches = batches
+
+    def step(self, i):
+        O, w, R = self.O, self.w, self.R
+        sl = slice((i % self.batches) * R, (i % self.batches + 1) * R)
+        jit = torch.rand(w["N"], generator=self.gen)
+        gum = -torch.log(-torch.log(torch.rand(w["N"], generator=self.gen).clamp_min(1e-7)))
+        out = O.render_rays(self.params, self.aabb, self.o[sl], self.d[sl], w["N"], w["k"], jit, gum,
+                            density_shift=DENSITY_SHIFT)
+        loss = O.mse(out, self.c[sl])
+        leaves = self.fields + self.mlp
+        grads = torch.autograd.grad(loss, leaves)
+        self.count += 1
+        with torch.no_grad():
+            for j, (t, g) in enumerate(zip(leaves, grads)):
+                lr = 0.02 if j < len(self.fields) else 1e-3
+                new, self.mu[j], self.nu[j] = O.adam_update(t, g, self.mu[j], self.nu[j], self.count, lr=lr,
+                                                            lr_decay=1.0)
+                t.copy_(new)
+        return float(loss.detach())
+
+
+def cpu_rays_per_step(w, budget_s, steps):
+    """Rays per CPU step so that `steps` steps take about budget_s: the largest multiple of
+    256 up to the full batch, from one measured 256-ray step (its fixed Adam cost makes
+    the estimate conservative)."""
+    t = time.perf_counter()
+    CpuTrainer(w, 256).step(0)
+    per_ray = (time.perf_counter() - t) / 256
+    fit = int(budget_s / max(steps, 1) / per_ray) // 256 * 256
+    return max(256, min(w["R"], fit))
+
+
+def cpu_train(w, steps, warmup, budget_s):
+    """Times `steps` oracle train steps after `warmup` untimed ones. Returns (rays/s, rays
+    per step, threads, seconds per step)."""
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    R = cpu_rays_per_step(w, budget_s, steps + warmup)
+    tr = CpuTrainer(w, R)
+    for i in range(warmup):
+        tr.step(i)
+    t = time.perf_counter()
+    for i in range(steps):
+        tr.step(warmup + i)
+    dt = time.perf_counter() - t
+    return R * steps / dt, R, threads, dt / steps
+
+
+def cpu_sample_text(w, R, steps, warmup):
+    return (f"oracle (torch CPU float32) train steps of {R} of the {w['R']} sphere-scene rays of the GPU arm's "
+            f"first batch, forward + backward + Adam over all parameters, {steps} timed after {warmup} warm-up; "
+            f"rays/s measured, not scaled")
 
 
 def cpu_baseline(w, args):
-    threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    sample = args.cpu_sample_rays
-    fb, adam = _cpu_step_time(w, sample)
-    step_s = fb * (w["R"] / sample) + adam
-    return {"value": round(w["R"] / step_s, 2), "unit": "rays/s", "cores": threads, "kind": "port",
-            "sample": f"oracle (torch CPU float32) forward+backward of {sample} of the {w['R']} rays, "
-                      f"scaled x{w['R'] // sample}, plus one full Adam update ({fb:.2f} s + {adam:.2f} s)"}
+    steps, warmup = 4, 1
+    value, R, threads, _ = cpu_train(w, steps, warmup, budget_s=25.0)
+    return {"value": round(value, 2), "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": cpu_sample_text(w, R, steps, warmup)}
+
+
+def headline_config(w, world):
+    return {"workload": f"train step fp32: grid {w['grid']}^3, VM {w['Cd']}/{w['Ca']}, "
+                        f"{w['R']} rays x {w['N']} uniform samples, top-{w['k']} appearance, Adam",
+            "rays_per_step": w["R"], "density_samples": w["N"], "appearance_samples": w["k"],
+            "grid": w["grid"], "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "no flush: each step streams params+grads+Adam moments (277 MB) and >2 GB of per-sample "
+                  "work, both larger than the 126 MB L2"}
+
+
+DATA = "synthetic (32-sphere analytic scene, FP64 quadrature targets, seeded cameras)"
 
 
 def run_reference(args):
@@ -614,31 +745,16 @@ def run_reference(args):
     if rank != 0:
         return
     w = variant_cfg("plain_fp32", args.small)
-    threads = os.cpu_count() or 1
-    torch.set_num_threads(threads)
-    sample = args.cpu_sample_rays
-    for _ in range(max(0, min(args.warmup, 1))):
-        _cpu_step_time(w, max(8, sample // 8))
-    steps = min(args.steps, args.reference_steps)
-    times = []
-    t_start = time.perf_counter()
-    for i in range(steps):
-        fb, adam = _cpu_step_time(w, sample, seed=i)
-        times.append(fb * (w["R"] / sample) + adam)
-    wall = time.perf_counter() - t_start
-    step_s = statistics.mean(times)
-    value = w["R"] / step_s
+    value, R, threads, step_s = cpu_train(w, args.steps, args.warmup, budget_s=args.reference_budget_s)
+    config = headline_config(w, 1)
+    config["rays_per_step"] = R
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "rays/s", "n_gpus": 0,
-        "steps": steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded rays, N(0, 0.1^2) parameters)",
-        "config": {"workload": f"train step fp32: grid {w['grid']}^3, VM {w['Cd']}/{w['Ca']}, "
-                               f"{w['R']} rays x {w['N']} uniform samples, top-{w['k']} appearance, Adam",
-                   "rays_per_step": w["R"]},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+        "config": config,
         "cpu_baseline": {"value": round(value, 2), "unit": "rays/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: oracle forward+backward of {sample} rays scaled to {w['R']}, "
-                                   f"plus one full Adam update; wall {wall:.1f} s"},
+                         "sample": cpu_sample_text(w, R, args.steps, args.warmup)},
         "e2e": {"value": round(value, 2), "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is JAX and JAX is not installed: this is the CPU restatement of its algorithm",
     }
@@ -658,8 +774,8 @@ def main():
     ap.add_argument("--prop-k", type=int, default=7,
                     help="appearance samples of the proposal path (int(0.15 * 48), the reference's heuristic)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-rays", type=int, default=256)
-    ap.add_argument("--reference-steps", type=int, default=10)
+    ap.add_argument("--reference-budget-s", type=float, default=150.0,
+                    help="wall time the reference arm's steps aim for; sets its rays per step (at most the batch)")
     ap.add_argument("--profile-variant", choices=["plain_fp32", "bf16", "proposal_bf16", "unbounded_plain_bf16",
                                                   "unbounded_proposal_bf16"], default=None)
     args = ap.parse_args()

@@ -359,6 +359,15 @@ TVM_API int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads
 TVM_API int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow,
                        void* stream);
 
+/* ---- measurement ------------------------------------------------------------------------ */
+/* L2 bandwidth probe (no counterpart in the reference: it measures the roofline
+ * denominator of the gather and scatter kernels, whose fields stay in L2). Streams
+ * `passes` full passes over `buf` (`bytes`, a multiple of 16, small enough to stay in
+ * L2): kind 0 reads it with 16-byte loads that bypass L1, kind 1 adds 1.0 to every
+ * float with 16-byte float4 reductions (it changes the buffer). The caller times the
+ * launch on `stream`; bytes moved = passes * bytes. */
+TVM_API int tvm_l2_probe(int32_t kind, void* buf, size_t bytes, int32_t passes, void* stream);
+
 /* ---- data generation ---------------------------------------------------------------- */
 /* Counter-based noise: dst[i] = U[0,1) (kind 0) or standard Gumbel (kind 1) from
  * (seed, stream_id, i). */

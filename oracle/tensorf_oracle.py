@@ -467,12 +467,18 @@ def camera_K_from_fov(width: int, height: int, fov_x: Optional[float] = None, fo
 
 
 def camera_pixel_rays(K: onp.ndarray, R_world_camera: onp.ndarray, t_world_camera: onp.ndarray,
-                      width: int, height: int, dtype=onp.float64) -> Tuple[onp.ndarray, onp.ndarray]:
+                      width: int, height: int, dtype=onp.float64,
+                      pixels: Optional[onp.ndarray] = None) -> Tuple[onp.ndarray, onp.ndarray]:
     """``Camera.pixel_rays_wrt_world`` / ``ray_wrt_world_from_uv`` (cameras.py:100-143):
     direction = normalize(R_wc @ K^-1 @ [u, v, 1]) with +1e-8 in the norm, origin =
-    camera position. Returns origins, directions of shape (H*W, 3), row-major pixels."""
-    v, u = onp.mgrid[:height, :width]
-    uv1 = onp.stack([u.ravel(), v.ravel(), onp.ones(u.size)], axis=0).astype(onp.float64)
+    camera position. Returns origins, directions of shape (H*W, 3), row-major pixels, or
+    of the given flat pixel indices."""
+    if pixels is None:
+        v, u = onp.mgrid[:height, :width]
+        u, v = u.ravel(), v.ravel()
+    else:
+        v, u = onp.divmod(onp.asarray(pixels, dtype=onp.int64), width)
+    uv1 = onp.stack([u, v, onp.ones(u.size)], axis=0).astype(onp.float64)
     d = R_world_camera @ onp.linalg.inv(K) @ uv1
     d = d / (onp.linalg.norm(d, axis=0, keepdims=True) + 1e-8)
     o = onp.broadcast_to(t_world_camera[:, None], d.shape)
@@ -488,20 +494,30 @@ def sphere_scene_quadrature(origins: onp.ndarray, directions: onp.ndarray, cente
     """Volume-render spheres of constant density and colour in float64 with
     ``n_samples`` midpoint samples per ray over [t_near, t_far] and a white background.
     sigma(x) = density * #spheres containing x; colour = density-weighted mean of the
-    covering spheres' colours. Small-case reference for the GPU generator."""
+    covering spheres' colours. Reference for the GPU generator; rays are processed in
+    chunks of ``chunk``."""
     out = onp.zeros((origins.shape[0], 3))
-    for r in range(origins.shape[0]):
-        dt = (t_far[r] - t_near[r]) / n_samples
-        ts = t_near[r] + (onp.arange(n_samples) + 0.5) * dt
-        p = origins[r][None, :] + ts[:, None] * directions[r][None, :]
-        inside = (onp.linalg.norm(p[:, None, :] - centers[None, :, :], axis=-1) < radii[None, :])
-        cnt = inside.sum(-1).astype(onp.float64)
+    C = torch.as_tensor(onp.asarray(centers, dtype=onp.float64))
+    rad = torch.as_tensor(onp.asarray(radii, dtype=onp.float64))
+    col_s = torch.as_tensor(onp.asarray(colors, dtype=onp.float64))
+    j = torch.arange(n_samples, dtype=torch.float64) + 0.5
+    chunk = 32
+    for a in range(0, origins.shape[0], chunk):
+        o = torch.as_tensor(onp.asarray(origins[a:a + chunk], dtype=onp.float64))
+        d = torch.as_tensor(onp.asarray(directions[a:a + chunk], dtype=onp.float64))
+        t0 = torch.as_tensor(onp.asarray(t_near[a:a + chunk], dtype=onp.float64))
+        dt = (torch.as_tensor(onp.asarray(t_far[a:a + chunk], dtype=onp.float64)) - t0) / n_samples
+        ts = t0[:, None] + j[None, :] * dt[:, None]
+        p = o[:, None, :] + ts[..., None] * d[:, None, :]
+        inside = torch.linalg.norm(p[:, :, None, :] - C[None, None], dim=-1) < rad
+        cnt = inside.sum(-1).to(torch.float64)
         sig = density * cnt
-        col = (inside.astype(onp.float64) @ colors) / onp.maximum(cnt, 1.0)[:, None]
-        alpha = 1.0 - onp.exp(-sig * dt)
-        trans = onp.concatenate([[1.0], onp.cumprod(1.0 - alpha)[:-1]])
+        col = (inside.to(torch.float64) @ col_s) / torch.clamp(cnt, min=1.0)[..., None]
+        alpha = 1.0 - torch.exp(-sig * dt[:, None])
+        trans = torch.cat([torch.ones_like(alpha[:, :1]), torch.cumprod(1.0 - alpha, dim=-1)[:, :-1]], dim=-1)
         w = trans * alpha
-        out[r] = (w[:, None] * col).sum(0) + trans[-1] * (1.0 - alpha[-1])
+        res = (w[..., None] * col).sum(1) + (trans[:, -1] * (1.0 - alpha[:, -1]))[:, None]
+        out[a:a + chunk] = res.numpy()
     return out
 
 

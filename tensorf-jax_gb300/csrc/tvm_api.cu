@@ -261,9 +261,9 @@ static FieldView appearance_field(const tvm_model_desc& m, const tvm_param_layou
 struct PassBufs {
   float* sigma;
   int32_t* sel;
-  float *w_sel, *p_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
+  float *w_sel, *p_last, *q_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
   // proposal-guided sampling
-  float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p;
+  float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p, *dx_p;
   int32_t* bins;
 };
 
@@ -278,6 +278,7 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
   b.sel = ws.take<int32_t>(M);
   b.w_sel = ws.take<float>(M);
   b.p_last = ws.take<float>(R);
+  b.q_last = ws.take<float>(R);
   b.wsum = ws.take<float>(R);
   b.X0 = ws.take<float>(M * F);
   b.rgb = ws.take<float>(M * 3);
@@ -301,6 +302,7 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
       b.g_wp = ws.take<float>(S);
       b.dz_p = ws.take<float>(S);
       b.loss_p = ws.take<float>(1);
+      b.dx_p = prop_scatter_supported(m.proposal_grid) ? ws.take<float>(S * 12) : nullptr;
     }
   }
   return b;
@@ -380,12 +382,12 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(2, st);
   if (c.mode != TVM_MODE_RGB) {
     TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, 0, nullptr, 0,
-                                    nullptr, nullptr, nullptr, nullptr, out, nullptr, st));
+                                    nullptr, nullptr, nullptr, nullptr, nullptr, out, nullptr, st));
     phase_mark(3, st);
     return TVM_OK;
   }
   TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
-                                  c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.wsum, nullptr,
+                                  c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.q_last, b.wsum, nullptr,
                                   (proposal && backward) ? b.w_dense : nullptr, st));
   phase_mark(3, st);
   TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
@@ -395,12 +397,12 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, st));
   phase_mark(5, st);
   if (!backward) {
-    TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
+    TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
                               nullptr, nullptr, st));
     phase_mark(6, st);
     return TVM_OK;
   }
-  TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.wsum, R, k, colors, out, loss, b.dZ3, b.gw,
+  TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, colors, out, loss, b.dZ3, b.gw,
                             b.gP, st));
   phase_mark(6, st);
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
@@ -427,7 +429,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
                      params + L.proposal_b2, c.proposal_shift, nullptr, nullptr};
     TVM_TRY(launch_prop_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins, rays.directions,
                             R, sp, edges, c.proposal_jitter, b.dz_p, pm, grads + L.proposal_w1,
-                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, st));
+                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, b.dx_p, st));
   }
   phase_mark(11, st);
   return TVM_OK;

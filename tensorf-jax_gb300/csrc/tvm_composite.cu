@@ -105,7 +105,7 @@ __global__ void segment_fwd_kernel(const float* __restrict__ sigmas, const float
     const float excl = (lane == 0) ? carry : prev;
     if (valid) {
       if (p_exits) p_exits[r * N + i] = expf(incl);
-      if (p_term) p_term[r * N + i] = (1.0f - expf(sv)) * expf(excl);
+      if (p_term) p_term[r * N + i] = -expm1f(sv) * expf(excl);
     }
     carry = __shfl_sync(0xffffffffu, incl, 31);
   }
@@ -158,7 +158,7 @@ __global__ void composite_bwd_kernel(const float* __restrict__ sigma, const floa
     const float prev = __shfl_up_sync(0xffffffffu, incl, 1);
     const float excl = (lane == 0) ? carry : prev;
     if (valid) {
-      const float w = (1.0f - expf(sv)) * expf(excl);
+      const float w = -expm1f(sv) * expf(excl);
       const float gw = SPARSE ? GW[i] : (g_pt ? __ldg(g_pt + r * N + i) : 0.f);
       float e = gw * w;
       if (!SPARSE && g_pe) e += __ldg(g_pe + r * N + i) * expf(incl);
@@ -226,8 +226,8 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
                                         int mode, int k, int P, const float* __restrict__ gumbel,
                                         int gumbel_per_ray, int32_t* __restrict__ sel_idx,
                                         float* __restrict__ w_sel, float* __restrict__ p_last_out,
-                                        float* __restrict__ wsum_out, float* __restrict__ dist_out,
-                                        float* __restrict__ w_dense) {
+                                        float* __restrict__ q_last_out, float* __restrict__ wsum_out,
+                                        float* __restrict__ dist_out, float* __restrict__ w_dense) {
   extern __shared__ unsigned char smem_b[];
   const int N = s.N;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -249,7 +249,7 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
     const float incl = warp_inclusive_scan(sv, lane) + carry;
     const float prev = __shfl_up_sync(0xffffffffu, incl, 1);
     const float excl = (lane == 0) ? carry : prev;
-    const float w = (1.0f - expf(sv)) * expf(excl);
+    const float w = -expm1f(sv) * expf(excl);
     if (w_dense && valid) w_dense[r * N + i] = w;
     if (mode == TVM_MODE_RGB) {
       if (valid) {
@@ -296,6 +296,7 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
   ws = warp_sum(ws);
   if (lane == 0) {
     p_last_out[r] = p_last;
+    q_last_out[r] = -expm1f(carry);  // 1 - p_last without cancellation
     wsum_out[r] = ws;
   }
 }
@@ -306,7 +307,7 @@ __global__ void composite_select_kernel(const float* __restrict__ sigma,
 // unbias = (1 - p_last + 1e-8) / (sum_j w_j + 1e-8).
 // ---------------------------------------------------------------------------------
 __global__ void color_loss_kernel(const float* __restrict__ rgb_sel, const float* __restrict__ w_sel,
-                                  const float* __restrict__ p_last_in,
+                                  const float* __restrict__ p_last_in, const float* __restrict__ q_last_in,
                                   const float* __restrict__ wsum_in, int64_t R, int k,
                                   const float* __restrict__ target, float* __restrict__ color_out,
                                   float* __restrict__ loss, float* __restrict__ dZ3,
@@ -326,7 +327,7 @@ __global__ void color_loss_kernel(const float* __restrict__ rgb_sel, const float
     for (int c = 0; c < 3; ++c) acc[c] = warp_sum(acc[c]);
     const float p_last = __ldg(p_last_in + r);
     const float wsum = __ldg(wsum_in + r);
-    const float unbias = (1.0f - p_last + 1e-8f) / (wsum + 1e-8f);
+    const float unbias = (__ldg(q_last_in + r) + 1e-8f) / (wsum + 1e-8f);  // q_last = 1 - p_last
     float col[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) col[c] = acc[c] * unbias + p_last * 1.0f;
@@ -436,7 +437,7 @@ int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t
 int launch_composite_select(const float* sigma, const float* origins, const float* dirs, int64_t R,
                             const SamplerArgs& s, int mode, int k, const float* gumbel,
                             int gumbel_per_ray, int32_t* sel_idx, float* w_sel, float* p_last,
-                            float* wsum, float* dist_out, float* w_dense, cudaStream_t st) {
+                            float* q_last, float* wsum, float* dist_out, float* w_dense, cudaStream_t st) {
   if (R == 0) return TVM_OK;
   const int P = (mode == TVM_MODE_RGB) ? next_pow2(k) : 1;
   const size_t per_warp = (size_t)s.N * 8 + (size_t)P * 8;
@@ -444,16 +445,16 @@ int launch_composite_select(const float* sigma, const float* origins, const floa
   const size_t smem = per_warp * warps;
   TVM_TRY(set_smem((const void*)composite_select_kernel, smem));
   composite_select_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(
-      sigma, origins, dirs, R, s, mode, k, P, gumbel, gumbel_per_ray, sel_idx, w_sel, p_last, wsum,
+      sigma, origins, dirs, R, s, mode, k, P, gumbel, gumbel_per_ray, sel_idx, w_sel, p_last, q_last, wsum,
       dist_out, w_dense);
   return check_launch("composite_select");
 }
 
-int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last,
+int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last, const float* q_last,
                       const float* wsum, int64_t R, int k, const float* target, float* color_out,
                       float* loss, float* dZ3, float* gw_sel, float* gP, cudaStream_t st) {
   if (R == 0) return TVM_OK;
-  color_loss_kernel<<<(unsigned)ceil_div(R, 8), 256, 0, st>>>(rgb_sel, w_sel, p_last, wsum, R, k,
+  color_loss_kernel<<<(unsigned)ceil_div(R, 8), 256, 0, st>>>(rgb_sel, w_sel, p_last, q_last, wsum, R, k,
                                                                target, color_out, loss, dZ3, gw_sel,
                                                                gP);
   return check_launch("color_loss");

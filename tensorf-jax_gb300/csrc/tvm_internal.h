@@ -55,16 +55,17 @@ int launch_segment_bwd(const float* sigmas, const float* steps, int64_t R, int N
                        const float* g_pt, float* g_sigma, cudaStream_t st);
 int launch_topk(const float* p, const float* gumbel, int gumbel_per_ray, int64_t R, int N, int k,
                 int32_t* idx, cudaStream_t st);
-// Fused: sigma (R,N) -> selection (RGB) or distance (DIST modes).
+// Fused: sigma (R,N) -> selection (RGB) or distance (DIST modes). p_last = the exit
+// probability of the last sample, q_last = 1 - p_last computed without cancellation.
 int launch_composite_select(const float* sigma, const float* origins, const float* dirs, int64_t R,
                             const SamplerArgs& s, int mode, int k, const float* gumbel,
                             int gumbel_per_ray, int32_t* sel_idx, float* w_sel, float* p_last,
-                            float* wsum, float* dist_out, float* w_dense, cudaStream_t st);
+                            float* q_last, float* wsum, float* dist_out, float* w_dense, cudaStream_t st);
 // Dense backward with explicit step sizes into dL/d(pre-softplus sum).
 int launch_segment_bwd_sum(const float* sigmas, const float* steps, int64_t R, int N, const float* g_pt,
                            float* g_sum, cudaStream_t st);
 // Fused: per-ray colour, loss and the gradients entering the MLP and the compositing.
-int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last,
+int launch_color_loss(const float* rgb_sel, const float* w_sel, const float* p_last, const float* q_last,
                       const float* wsum, int64_t R, int k, const float* target, float* color_out,
                       float* loss, float* dZ3, float* gw_sel, float* gP, cudaStream_t st);
 int launch_composite_bwd(const float* sigma, const float* origins, const float* dirs, int64_t R,
@@ -130,10 +131,14 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
                          const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
                          cudaStream_t st);
 // Fused proposal backward from dz = dL/d(pre-softplus): field scatter and MLP weight
-// gradients (all accumulate).
+// gradients (all accumulate). dx_buf (R * Np * 12 floats, 16-byte aligned, or NULL):
+// scratch for the per-sample feature gradients, which lets a field that fits shared
+// memory (prop_scatter_supported) be scattered without global contention.
+bool prop_scatter_supported(int G);
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
-                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st);
+                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, float* dx_buf,
+                    cudaStream_t st);
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                     const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
                     cudaStream_t st);

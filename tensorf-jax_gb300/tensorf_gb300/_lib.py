@@ -113,6 +113,7 @@ _SIGNATURES = {
     "tvm_adam_step": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, POINTER(AdamDesc),
                                 c_void_p, c_void_p]),
     "tvm_refresh_shadow": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p]),
+    "tvm_l2_probe": (c_int32, [c_int32, c_void_p, c_size_t, c_int32, c_void_p]),
     "tvm_noise_fill": (c_int32, [c_void_p, c_int64, c_uint64, c_uint64, c_int32, c_void_p]),
     "tvm_camera_rays": (c_int32, [POINTER(c_double), POINTER(c_double), POINTER(c_double), c_int32, c_int32,
                                   c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),

@@ -165,18 +165,7 @@ class LearnableParams:
         """TrainState.initialize's parameter init (training.py:35-99): N(0, 0.1^2)
         field tensors, flax-style MLP init."""
         require_cuda()
-        gen = torch.Generator().manual_seed(seed)
-        g = spec.grid_dim
-        ref = {
-            "density": (torch.randn((3, spec.density_feat_dim, g), generator=gen) * 0.1,
-                        torch.randn((3, spec.density_feat_dim, g, g), generator=gen) * 0.1),
-            "appearance": (torch.randn((3, spec.appearance_feat_dim, g), generator=gen) * 0.1,
-                           torch.randn((3, spec.appearance_feat_dim, g, g), generator=gen) * 0.1),
-            "mlp": spec.mlp().init_params(3 * spec.appearance_feat_dim, gen),
-        }
-        if spec.proposal_grid:
-            ref["proposal"] = init_proposal(spec.proposal_grid, spec.proposal_units, gen)
-        return LearnableParams.from_reference(spec, ref, scene_contraction, device)
+        return LearnableParams.from_reference(spec, initial_reference_params(spec, seed), scene_contraction, device)
 
     @staticmethod
     def from_reference(spec: ModelSpec, ref: dict, scene_contraction: bool = False,
@@ -276,6 +265,25 @@ class ProposalConfig:
     samples: int = 64
     shift: float = 0.0
     loss_weight: float = 1.0
+
+
+def initial_reference_params(spec: ModelSpec, seed: int = 94709) -> dict:
+    """The initial parameters of LearnableParams.initialize in the reference's layout,
+    on the CPU (float32): N(0, 0.1^2) vector / matrix of both VM tensors
+    (training.py:44-56), flax-style FeatureMlp init, and the proposal network when the
+    spec has one. Needs no GPU."""
+    gen = torch.Generator().manual_seed(seed)
+    g = spec.grid_dim
+    ref = {
+        "density": (torch.randn((3, spec.density_feat_dim, g), generator=gen) * 0.1,
+                    torch.randn((3, spec.density_feat_dim, g, g), generator=gen) * 0.1),
+        "appearance": (torch.randn((3, spec.appearance_feat_dim, g), generator=gen) * 0.1,
+                       torch.randn((3, spec.appearance_feat_dim, g, g), generator=gen) * 0.1),
+        "mlp": spec.mlp().init_params(3 * spec.appearance_feat_dim, gen),
+    }
+    if spec.proposal_grid:
+        ref["proposal"] = init_proposal(spec.proposal_grid, spec.proposal_units, gen)
+    return ref
 
 
 def init_proposal(grid: int, units: int, gen: torch.Generator) -> Dict[str, torch.Tensor]:

@@ -107,20 +107,35 @@ class SphereScene:
                   ptr(aabb), ctypes.byref(rs), n_samples, ptr(out), stream_handle())
         return out
 
+    @staticmethod
+    def training_pixels(cams: List[cameras.Camera], total: int, seed: int) -> Tuple[onp.ndarray, onp.ndarray]:
+        """The (camera index, flat pixel index) of each of ``total`` training rays, in
+        batch order: an equal share of random pixels per camera, then shuffled. Host
+        only, so a CPU run can rebuild the same rays."""
+        rng = onp.random.default_rng(seed)
+        per = [total // len(cams) + (1 if i < total % len(cams) else 0) for i in range(len(cams))]
+        cam_idx, pix = [], []
+        for i, (cam, n) in enumerate(zip(cams, per)):
+            if n == 0:
+                continue
+            pix.append(rng.integers(0, cam.image_width * cam.image_height, size=n))
+            cam_idx.append(onp.full(n, i))
+        perm = rng.permutation(total)
+        return onp.concatenate(cam_idx)[perm], onp.concatenate(pix)[perm]
+
     def training_rays(self, cams: List[cameras.Camera], total: int, seed: int,
                       n_samples: int = 4096) -> Tuple[cameras.Rays3D, torch.Tensor]:
         """``total`` random pixels over the cameras with their FP64 target colours."""
-        rng = onp.random.default_rng(seed)
-        per = [total // len(cams) + (1 if i < total % len(cams) else 0) for i in range(len(cams))]
-        os_, ds_ = [], []
-        for cam, n in zip(cams, per):
-            if n == 0:
+        cam_idx, pix = self.training_pixels(cams, total, seed)
+        o = torch.empty((total, 3), dtype=torch.float32, device="cuda")
+        d = torch.empty((total, 3), dtype=torch.float32, device="cuda")
+        for i, cam in enumerate(cams):
+            sel = onp.nonzero(cam_idx == i)[0]
+            if sel.size == 0:
                 continue
-            pix = torch.as_tensor(rng.integers(0, cam.image_width * cam.image_height, size=n), dtype=torch.int64)
-            rr = cam.pixel_rays_wrt_world(pix)
-            os_.append(rr.origins)
-            ds_.append(rr.directions)
-        rays = cameras.Rays3D(origins=torch.cat(os_), directions=torch.cat(ds_))
-        perm = torch.as_tensor(rng.permutation(total), device="cuda")
-        rays = cameras.Rays3D(origins=rays.origins[perm].contiguous(), directions=rays.directions[perm].contiguous())
+            rr = cam.pixel_rays_wrt_world(torch.as_tensor(pix[sel], dtype=torch.int64))
+            at = torch.as_tensor(sel, device="cuda")
+            o[at] = rr.origins
+            d[at] = rr.directions
+        rays = cameras.Rays3D(origins=o, directions=d)
         return rays, self.render(rays, n_samples)

@@ -1,0 +1,254 @@
+"""GPU parity at the benchmarked shapes, against the float64 CPU oracle.
+
+* The FP32 train step of the headline workload: G = 300, 16 / 48 components,
+  N = 512 uniform samples, top-64 appearance samples, density shift 0, rays and
+  targets of the 32-sphere scene. This is the shape at which the pair-merging scatter
+  kernels and the pipelined split-tf32 FeatureMlp run.
+* The CPU-runnable workload: G = 128, N = 256, k = 256 (every sample reaches the
+  appearance path), density shift -10, bbox [-1.5, 1.5]^3, rays from a sphere of
+  radius 4 aimed at the origin, uniform targets.
+
+Both compare the render, the loss and every gradient segment (density and appearance
+lines and planes, every FeatureMlp kernel and bias) with the oracle, at 1e-4 relative
+to the largest magnitude of each tensor (reference: render.py:105-279 forward,
+training.py:121-156 loss and value_and_grad).
+
+Two kinds of rays are left out of the comparison, and counted:
+  - near-ties of the top-k selection (k-th and (k+1)-th keys within 1e-5): float32
+    rounding may pick a different sample there;
+  - rays with a FeatureMlp pre-activation within 1e-5 of the layer's RMS of zero: at a
+    ReLU kink a pre-activation of either sign is correct to rounding, but the sign
+    decides whether the unit's gradient passes.
+
+Also here: Adam with bias correction over five consecutive updates and the
+exponential learning-rate decay with its reset after an upsampling iteration
+(training.py:158-243), through tvm_adam_step and through TrainState.training_step.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import tensorf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4        # render, loss and every gradient tensor (FP32 mode)
+KINK_REL = 1e-5    # |pre-activation| below this fraction of the layer's RMS: excluded
+TIE_MARGIN = 1e-5  # top-k near-tie margin
+
+
+def _rel_err(a, b):
+    a = torch.as_tensor(a.detach() if torch.is_tensor(a) else a, dtype=torch.float64).cpu()
+    b = torch.as_tensor(b.detach() if torch.is_tensor(b) else b, dtype=torch.float64).cpu()
+    assert a.numel() > 0 and a.shape == b.shape
+    return float((a - b).abs().max() / (b.abs().max() + 1e-30))
+
+
+def _ref_params(G, seed):
+    gen = torch.Generator().manual_seed(seed)
+    ref = {"density": O.vm_init(G, 16, gen, torch.float32), "appearance": O.vm_init(G, 48, gen, torch.float32),
+           "mlp": O.mlp_init(144, 2, 2, gen, dtype=torch.float32)}
+    for lay in ("Dense_1", "Dense_2", "Dense_3"):
+        ref["mlp"][lay]["bias"] = torch.randn(ref["mlp"][lay]["bias"].shape, generator=gen) * 0.05
+    return ref
+
+
+def _to64(p, grad=False):
+    t = lambda x: x.double().requires_grad_(grad)  # noqa: E731
+    return {"density": tuple(t(x) for x in p["density"]), "appearance": tuple(t(x) for x in p["appearance"]),
+            "mlp": {k: {n: t(x) for n, x in d.items()} for k, d in p["mlp"].items()}}
+
+
+def _keep_rays(ref64, aabb, o, d, N, k, jit, gum, shift):
+    """Rays free of top-k near-ties and of ReLU kinks, from an oracle forward pass."""
+    with torch.no_grad():
+        _, aux = O.render_rays(ref64, aabb, o, d, N, k, jit, gum, density_shift=shift, return_aux=True)
+    R = o.shape[0]
+    keys = O.gumbel_topk_keys(aux["p_terminates"], gum)
+    if k < N:
+        srt = torch.sort(keys, dim=-1, descending=True).values
+        margin = srt[:, k - 1] - srt[:, k]
+        tie_free = (margin > TIE_MARGIN) | ~torch.isfinite(margin)
+    else:
+        tie_free = torch.ones(R, dtype=torch.bool)
+    mlp = ref64["mlp"]
+    with torch.no_grad():
+        f = aux["appearance_features"] @ mlp["Dense_0"]["kernel"]
+        vd = d[:, None, :].expand(R, k, 3).reshape(-1, 3)
+        x = torch.cat([f, vd, O.fourier_encode(f, 2), O.fourier_encode(vd, 2)], dim=-1)
+        z1 = x @ mlp["Dense_1"]["kernel"] + mlp["Dense_1"]["bias"]
+        z2 = torch.relu(z1) @ mlp["Dense_2"]["kernel"] + mlp["Dense_2"]["bias"]
+    kink = torch.zeros(R * k, dtype=torch.bool)
+    for z in (z1, z2):
+        kink |= (z.abs() < KINK_REL * float(z.pow(2).mean().sqrt())).any(dim=-1)
+    kink_free = ~kink.reshape(R, k).any(dim=-1)
+    return tie_free & kink_free, int((~tie_free).sum()), int((~kink_free).sum())
+
+
+def _check_parity(G, o, d, c, N, k, shift, seed, min_keep):
+    from tensorf_gb300 import cameras, render
+    ref = _ref_params(G, seed)
+    rng = np.random.default_rng(seed)
+    jit = torch.tensor(rng.uniform(size=N), dtype=torch.float32)
+    gum = torch.tensor(-np.log(-np.log(rng.uniform(1e-7, 1, size=N))), dtype=torch.float32)
+    aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
+    keep, n_ties, n_kinks = _keep_rays(_to64(ref), aabb.double(), o.double(), d.double(), N, k, jit.double(),
+                                       gum.double(), shift)
+    print(f"G={G} N={N} k={k}: {len(o)} rays, {n_ties} near-ties, {n_kinks} with a ReLU kink")
+    assert float(keep.float().mean()) >= min_keep, (n_ties, n_kinks)
+    o, d, c = o[keep].contiguous(), d[keep].contiguous(), c[keep].contiguous()
+
+    spec = render.ModelSpec(grid_dim=G)
+    lp = render.LearnableParams.from_reference(spec, ref)
+    rays = cameras.Rays3D(o.cuda(), d.cuda())
+    noise = render.RenderNoise(jit.cuda(), gum.cuda())
+    cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, N, k)
+    img = render.render_rays(spec.mlp(), lp, aabb, rays, noise, cfg, density_shift=shift).cpu()
+    grads = torch.zeros_like(lp.params)
+    loss = float(render.loss_and_grad(lp, grads, aabb, rays, c.cuda(), noise, cfg, density_shift=shift).item())
+
+    ref64 = _to64(ref, grad=True)
+    out = O.render_rays(ref64, aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
+                        density_shift=shift)
+    L = O.mse(out, c.double())
+    L.backward()
+    assert _rel_err(img, out) < RTOL, _rel_err(img, out)
+    assert abs(loss - float(L)) <= RTOL * float(L), (loss, float(L))
+    g = lp.to_reference(grads)
+    pairs = {"density.vector": (g["density"][0], ref64["density"][0].grad),
+             "density.matrix": (g["density"][1], ref64["density"][1].grad),
+             "appearance.vector": (g["appearance"][0], ref64["appearance"][0].grad),
+             "appearance.matrix": (g["appearance"][1], ref64["appearance"][1].grad)}
+    for layer in ref64["mlp"]:
+        for nm in ref64["mlp"][layer]:
+            pairs[f"{layer}.{nm}"] = (g["mlp"][layer][nm], ref64["mlp"][layer][nm].grad)
+    errs = {name: _rel_err(got, want) for name, (got, want) in pairs.items()}
+    print({k_: f"{v:.1e}" for k_, v in errs.items()})
+    assert max(errs.values()) < RTOL, errs
+
+
+def test_headline_train_step_parity_g300_n512_k64():
+    """Config of the headline bench line: FP32, G=300, N=512, top-64, sphere scene."""
+    from tensorf_gb300 import scene
+    sc = scene.SphereScene.random(0, count=32)
+    rays, colors = sc.training_rays(sc.cameras(4, seed=1), 192, seed=2)
+    o, d, c = rays.origins.cpu(), rays.directions.cpu(), colors.cpu()
+    _check_parity(300, o, d, c, N=512, k=64, shift=0.0, seed=5, min_keep=0.8)
+
+
+def test_cpu_workload_parity_g128_n256_k256_shift_minus10():
+    """The CPU-runnable workload: G=128, N=k=256, softplus(sum - 10), uniform targets."""
+    from tensorf_gb300 import scene
+    # k = 256 rows of 256 hidden units per ray: about a third of the rays hold a
+    # pre-activation within the kink margin, so 384 rays leave more than 200.
+    o, d, c = (torch.tensor(a) for a in scene.sphere_rays(384, 7))
+    _check_parity(128, o, d, c, N=256, k=256, shift=-10.0, seed=6, min_keep=0.5)
+
+
+# ---------------------------------------------------------------------------------
+# Adam and the learning-rate schedule over several steps.
+# ---------------------------------------------------------------------------------
+def _schedule_config(**kw):
+    from tensorf_gb300 import training
+    d = dict(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
+             appearance_samples_per_ray=16, n_iters=10, upsamp_iters=(3,), density_shift=-1.0)
+    d.update(kw)
+    return training.TrainConfig(**d)
+
+
+def test_lr_schedule_matches_oracle():
+    from tensorf_gb300 import training
+    cfg = _schedule_config()
+    for step in range(0, 14):
+        want = O.lr_decay_coeff(step, cfg.n_iters, cfg.upsamp_iters)
+        assert training.lr_decay_coeff(step, cfg) == pytest.approx(want, rel=1e-6), step
+    assert training.lr_decay_coeff(2, cfg) < 1.0 and training.lr_decay_coeff(3, cfg) == 1.0  # reset at 3
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_adam_five_steps_with_decay_and_reset(precision):
+    """tvm_adam_step, counts 1..5, decay coefficients of steps 0..4 with a reset at 3,
+    fresh gradients each step: params, mu and nu against optax's Adam in FP64 at 1e-5;
+    the BF16 shadow is the rounded master copy of the field segments."""
+    from tensorf_gb300 import _lib, render
+    from tensorf_gb300._util import ptr, stream_handle
+    spec = render.ModelSpec(grid_dim=12, precision=precision)
+    lp = render.LearnableParams.initialize(spec, seed=3)
+    lay = lp.layout
+    md = lp.model_desc()
+    n = lay.total
+    mu = torch.zeros(n, device="cuda")
+    nu = torch.zeros(n, device="cuda")
+    p64, mu64, nu64 = lp.params.double().cpu(), torch.zeros(n, dtype=torch.float64), torch.zeros(n, dtype=torch.float64)
+    cfg = _schedule_config()
+    gen = torch.Generator().manual_seed(4)
+    for step in range(5):
+        g = torch.randn(n, generator=gen) * torch.exp(torch.randn(n, generator=gen) * 2.0)  # wide magnitude range
+        g[::97] = 0.0
+        grads = g.float().cuda()
+        decay = O.lr_decay_coeff(step, cfg.n_iters, cfg.upsamp_iters)
+        desc = _lib.AdamDesc(lr_tensor=0.02, lr_mlp=1e-3, b1=0.9, b2=0.99, eps=1e-8, lr_decay=decay, count=step + 1,
+                             _pad=0)
+        _lib.call("tvm_adam_step", ctypes.byref(md), ptr(lp.params), ptr(grads), ptr(mu), ptr(nu), ctypes.byref(desc),
+                  ptr(lp.shadow) if lp.shadow is not None else None, stream_handle())
+        assert float(grads.abs().max()) == 0.0  # zeroed for the next step
+        gd = g.float().double()
+        pt, mt, vt = O.adam_update(p64[:lay.mlp_begin], gd[:lay.mlp_begin], mu64[:lay.mlp_begin],
+                                   nu64[:lay.mlp_begin], step + 1, lr=0.02, lr_decay=decay)
+        pm, mm, vm = O.adam_update(p64[lay.mlp_begin:], gd[lay.mlp_begin:], mu64[lay.mlp_begin:],
+                                   nu64[lay.mlp_begin:], step + 1, lr=1e-3, lr_decay=decay)
+        p_prev = p64
+        p64, mu64, nu64 = torch.cat([pt, pm]), torch.cat([mt, mm]), torch.cat([vt, vm])
+        got = lp.params.double().cpu()
+        assert _rel_err(got - p_prev, p64 - p_prev) < 1e-5, step  # the update itself
+        assert _rel_err(mu.cpu(), mu64) < 1e-5 and _rel_err(nu.cpu(), nu64) < 1e-5, step
+        p64 = got  # follow the device's float32 parameters
+        if lp.shadow is not None:
+            want = lp.params[:lay.shadow_total].to(torch.bfloat16)
+            assert torch.equal(lp.shadow.view(torch.int16), want.view(torch.int16))
+
+
+def test_train_step_five_updates_follow_adam_on_device_gradients():
+    """Five TrainState.training_step calls with a reset of the decay at step 3: each
+    update equals optax's Adam applied to the gradient tvm_loss_and_grad returns at the
+    same parameters, and the logged learning rates follow the schedule."""
+    from tensorf_gb300 import cameras, render, scene, training
+    cfg = _schedule_config()
+    spec = render.ModelSpec(grid_dim=16)
+    lp = render.LearnableParams.initialize(spec, seed=8)
+    ts = training.TrainState(cfg, lp)
+    o, d, c = scene.sphere_rays(128, 8)
+    rays = cameras.Rays3D(torch.tensor(o).cuda(), torch.tensor(d).cuda())
+    colors = torch.tensor(c).cuda()
+    rng = np.random.default_rng(8)
+    noise = render.RenderNoise(torch.tensor(rng.uniform(size=64), dtype=torch.float32).cuda(),
+                               torch.tensor(-np.log(-np.log(rng.uniform(1e-7, 1, size=64))),
+                                            dtype=torch.float32).cuda())
+    lay = lp.layout
+    mu64 = torch.zeros(lay.total, dtype=torch.float64)
+    nu64 = torch.zeros(lay.total, dtype=torch.float64)
+    for step in range(5):
+        p0 = lp.params.double().cpu()
+        grads = torch.zeros_like(lp.params)
+        render.loss_and_grad(lp, grads, ts.aabb, rays, colors, noise, ts.render_config(), density_shift=-1.0)
+        g = grads.double().cpu()
+        _, log = ts.training_step(rays, colors, noise=noise)
+        decay = O.lr_decay_coeff(step, cfg.n_iters, cfg.upsamp_iters)
+        assert log["train/lr_tensor"] == pytest.approx(0.02 * decay, rel=1e-6)
+        assert log["train/lr_mlp"] == pytest.approx(1e-3 * decay, rel=1e-6)
+        pt, mt, vt = O.adam_update(p0[:lay.mlp_begin], g[:lay.mlp_begin], mu64[:lay.mlp_begin], nu64[:lay.mlp_begin],
+                                   step + 1, lr=0.02, lr_decay=decay)
+        pm, mm, vm = O.adam_update(p0[lay.mlp_begin:], g[lay.mlp_begin:], mu64[lay.mlp_begin:], nu64[lay.mlp_begin:],
+                                   step + 1, lr=1e-3, lr_decay=decay)
+        want = torch.cat([pt, pm])
+        mu64, nu64 = torch.cat([mt, mm]), torch.cat([vt, vm])
+        got = lp.params.double().cpu()
+        # The step's own gradient is the one measured above up to the order of its
+        # atomic reductions, so elements whose gradient is at rounding level may take
+        # a different Adam direction; compare the update where the gradient is clear.
+        clear = g.abs() > 1e-6 * float(g.abs().max())
+        assert _rel_err((got - p0)[clear], (want - p0)[clear]) < 1e-4, step
+        assert _rel_err(ts.mu.double().cpu()[clear], mu64[clear]) < 1e-4, step
+    assert ts.step == 5

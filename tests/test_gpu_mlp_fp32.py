@@ -28,19 +28,20 @@ def _rel(a, b):
     return float((a - b).abs().max() / (b.abs().max() + 1e-30))
 
 
-def _model(seed, ca=48):
+def _model(seed, ca=48, nf=2, nv=2):
     from tensorf_gb300 import render
-    spec = render.ModelSpec(grid_dim=8, appearance_feat_dim=ca, precision="fp32")
+    spec = render.ModelSpec(grid_dim=8, appearance_feat_dim=ca, feature_n_freqs=nf, viewdir_n_freqs=nv,
+                            precision="fp32")
     gen = torch.Generator().manual_seed(seed)
     ref = {"density": O.vm_init(8, 16, gen, torch.float32), "appearance": O.vm_init(8, ca, gen, torch.float32),
-           "mlp": O.mlp_init(3 * ca, 2, 2, gen, dtype=torch.float32)}
+           "mlp": O.mlp_init(3 * ca, nf, nv, gen, dtype=torch.float32)}
     for layer in ("Dense_1", "Dense_2", "Dense_3"):  # non-zero biases, so their gradients matter
         b = ref["mlp"][layer]["bias"]
         b.copy_(torch.randn(b.shape, generator=gen) * 0.1)
     return spec, ref, render.LearnableParams.from_reference(spec, ref)
 
 
-def _inputs(n, seed, ref):
+def _inputs(n, seed, ref, nf=2, nv=2):
     """n rows whose hidden pre-activations all lie at least KINK from zero in the
     float64 oracle: at a ReLU kink an FP32 pre-activation of either sign is correct to
     rounding, but it decides whether that unit's gradient passes, so such rows are
@@ -53,7 +54,7 @@ def _inputs(n, seed, ref):
         feats = torch.randn((2 * n + 8, feat), generator=gen) * 0.3
         dirs = torch.nn.functional.normalize(torch.randn((2 * n + 8, 3), generator=gen), dim=-1)
         f = feats.double() @ W["Dense_0"]["kernel"]
-        x1 = torch.cat([f, dirs.double(), O.fourier_encode(f, 2), O.fourier_encode(dirs.double(), 2)], dim=-1)
+        x1 = torch.cat([f, dirs.double(), O.fourier_encode(f, nf), O.fourier_encode(dirs.double(), nv)], dim=-1)
         z1 = x1 @ W["Dense_1"]["kernel"] + W["Dense_1"]["bias"]
         z2 = torch.relu(z1) @ W["Dense_2"]["kernel"] + W["Dense_2"]["bias"]
         ok = (z1.abs().min(dim=1).values > KINK) & (z2.abs().min(dim=1).values > KINK)
@@ -94,13 +95,13 @@ def _run(lp, feats, dirs, grad_rgb, out_offset=False):
     return rgb, gfeat, lp.mlp_views(grads)
 
 
-def _check_against_oracle(ref, lp, n, seed):
-    feats, dirs, grad_rgb = _inputs(n, seed, ref)
+def _check_against_oracle(ref, lp, n, seed, nf=2, nv=2):
+    feats, dirs, grad_rgb = _inputs(n, seed, ref, nf, nv)
     rgb, gfeat, got = _run(lp, feats.cuda(), dirs.cuda(), grad_rgb.cuda())
 
     mlp64 = {k: {nm: t.double().requires_grad_(True) for nm, t in d.items()} for k, d in ref["mlp"].items()}
     f64 = feats.double().requires_grad_(True)
-    r64 = O.feature_mlp(mlp64, f64, dirs.double(), 2, 2)
+    r64 = O.feature_mlp(mlp64, f64, dirs.double(), nf, nv)
     (r64 * grad_rgb.double()).sum().backward()
     assert _rel(rgb, r64) < RTOL
     assert _rel(gfeat, f64.grad) < GRAD_RTOL
@@ -122,6 +123,15 @@ def test_fp32_mlp_other_appearance_widths(ca):
     (train_config.py:44-45), with a narrower first product and a padded dX0 tile."""
     _, ref, lp = _model(9, ca)
     _check_against_oracle(ref, lp, 1000, 77 + ca)
+
+
+@pytest.mark.parametrize("n", [1, 129, 5000])
+def test_fp32_mlp_six_frequency_encodings(n):
+    """feature_n_freqs = viewdir_n_freqs = 6, the nerfstudio preset
+    (train_nerfstudio.py:33-34): a 390-wide encoding, which runs the layered split-tf32
+    GEMMs with a separate encoding pass rather than the fused pipelined kernel."""
+    _, ref, lp = _model(10, nf=6, nv=6)
+    _check_against_oracle(ref, lp, n, 500 + n, nf=6, nv=6)
 
 
 def test_fp32_mlp_unaligned_buffers_match_aligned():
