@@ -80,5 +80,36 @@ def build(verbose: bool = False, extra_flags=()) -> pathlib.Path:
     return LIB_PATH
 
 
+def jax_ffi_available() -> bool:
+    """True where jax with the FFI headers is importable (jaxlib >= 0.4.31)."""
+    try:
+        import jax.ffi  # noqa: F401
+
+        return bool(jax.ffi.include_dir())
+    except Exception:
+        return False
+
+
+def build_jax_shim(verbose: bool = False) -> pathlib.Path:
+    """libtvm_jax_ffi.so: the XLA FFI handlers of csrc/jax/tvm_jax_ffi.cc, linked against
+    the kernels' library. Needs jax.ffi."""
+    import jax.ffi
+
+    lib = build(verbose)
+    src = SRC_DIR / "jax" / "tvm_jax_ffi.cc"
+    out = PKG_DIR / "libtvm_jax_ffi.so"
+    cmd = ["g++", "-std=c++17", "-O2", "-shared", "-fPIC", f"-I{jax.ffi.include_dir()}", f"-I{INCLUDE_DIR}",
+           "-I/usr/local/cuda/include", str(src), str(lib), f"-Wl,-rpath,{PKG_DIR}", "-L/usr/local/cuda/lib64",
+           "-lcudart", "-o", str(out)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"building {out.name} failed:\n{res.stderr}")
+    if verbose:
+        print(f"built {out}", file=sys.stderr)
+    return out
+
+
 if __name__ == "__main__":
     build(verbose=True)
+    if jax_ffi_available():
+        build_jax_shim(verbose=True)

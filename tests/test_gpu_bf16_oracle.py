@@ -13,14 +13,17 @@ kernels actually use, rounded to bf16 at the points where those kernels round.
   their gradient dh and the loss gradient dz feed the products; b1, w2 and the scatter
   stay FP32.
 
-Error bound. A mirror value and a device value differ by FP32 rounding (2^-24
-relative) until one of them is rounded to bf16. Where the two straddle a bf16
-rounding boundary they round to neighbouring bf16 values, one ulp (at most 2^-7
-relative) apart. That happens with probability about 2^-24 / 2^-8 = 2^-16 per
-rounding. A norm over many independent contributions then moves by about
-2^-7 * sqrt(2^-16) = 3e-5 relative. The tests require a norm-relative error below 1e-3,
-more than 30 times that. A wrong rounding point, a wrong operand or a wrong index moves
-it by 1e-2 or more.
+Error bound. A mirror value and a device value differ by the device's FP32 (and
+tensor-core) accumulation error until one of them is rounded to bf16. Where the two
+straddle a bf16 rounding boundary they round to neighbouring bf16 values, one ulp
+(2^-8 to 2^-7 relative) apart, and in the FeatureMlp such a flip in an early layer
+perturbs every later value of that row by a fraction of an ulp, which flips more of
+them. So the device can sit up to about one bf16 ulp from the mirror, and no closer
+bound holds for the chained MLP: the tests allow 2^-8 = 3.9e-3 in norm. The proposal
+backward has one rounded product per operand and no chain: there the bound is 1e-4.
+A missing or extra rounding point shows as an error of the size of the rounding
+itself against the mirror, so each main-path tensor must also sit closer to the
+mirror than to the unrounded FP64 oracle.
 
 Rays are left out where the oracle's ReLU pre-activations lie within 1e-5 of the
 layer's RMS of zero, or the top-k selection has a near-tie (as in the FP32 tests).
@@ -40,7 +43,8 @@ from test_gpu_bf16 import _mirror_mlp, _mirror_mlp_backward
 
 pytestmark = pytest.mark.gpu
 
-NORM_RTOL = 1e-3
+NORM_RTOL = 2.0 ** -8       # main BF16 path: one bf16 ulp, in norm
+NORM_RTOL_PROPOSAL = 1e-4    # proposal backward: no chained rounding
 KINK_REL = 1e-5
 
 
@@ -74,6 +78,9 @@ class _MirrorMlp(torch.autograd.Function):
             dx0, g = _mirror_mlp_backward(mlp, feats.detach(), dirs.detach(), grad_rgb.detach())
         return (dx0, None, g["Dense_0"]["kernel"], g["Dense_1"]["kernel"], g["Dense_1"]["bias"],
                 g["Dense_2"]["kernel"], g["Dense_2"]["bias"], g["Dense_3"]["kernel"], g["Dense_3"]["bias"])
+
+
+_plain_feature_mlp = O.feature_mlp
 
 
 def _mirror_feature_mlp(params, features, viewdirs, nf, nv):
@@ -159,21 +166,32 @@ def test_bf16_render_and_gradients_match_rounding_mirror(monkeypatch):
     grads = torch.zeros_like(lp.params)
     loss = float(render.loss_and_grad(lp, grads, aabb, rays, c.cuda(), noise, cfg, density_shift=shift).item())
 
-    ref64 = _oracle_bf16(ref, grad=True)
-    out = O.render_rays(ref64, aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
-                        density_shift=shift)
-    L = O.mse(out, c.double())
-    L.backward()
-    errs = {"render": _nrel(img, out), "loss": abs(loss - float(L)) / float(L)}
+    def oracle_grads():
+        ref64 = _oracle_bf16(ref, grad=True)
+        out = O.render_rays(ref64, aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(),
+                            density_shift=shift)
+        L = O.mse(out, c.double())
+        L.backward()
+        gr = {f"{grp}.{nm}": ref64[grp][i].grad for grp in ("density", "appearance")
+              for i, nm in enumerate(("vector", "matrix"))}
+        gr.update({f"{layer}.{nm}": ref64["mlp"][layer][nm].grad for layer in ref64["mlp"] for nm in ref64["mlp"][layer]})
+        return out, L, gr
+
+    out, L, want = oracle_grads()
+    with monkeypatch.context() as mp:  # the same oracle with an unrounded FP64 FeatureMlp
+        mp.setattr(O, "feature_mlp", _plain_feature_mlp)
+        _, _, want_plain = oracle_grads()
     g = lp.to_reference(grads)
-    for grp in ("density", "appearance"):
-        for i, nm in enumerate(("vector", "matrix")):
-            errs[f"{grp}.{nm}"] = _nrel(g[grp][i], ref64[grp][i].grad)
-    for layer in ref64["mlp"]:
-        for nm in ref64["mlp"][layer]:
-            errs[f"{layer}.{nm}"] = _nrel(g["mlp"][layer][nm], ref64["mlp"][layer][nm].grad)
-    print({k_: f"{v:.1e}" for k_, v in errs.items()})
+    got = {f"{grp}.{nm}": g[grp][i] for grp in ("density", "appearance") for i, nm in enumerate(("vector", "matrix"))}
+    got.update({f"{layer}.{nm}": g["mlp"][layer][nm] for layer in g["mlp"] for nm in g["mlp"][layer]})
+    errs = {"render": _nrel(img, out), "loss": abs(loss - float(L)) / float(L)}
+    errs.update({name: _nrel(got[name], want[name]) for name in want})
+    plain = {name: _nrel(got[name], want_plain[name]) for name in want}
+    print("vs mirror", {k_: f"{v:.1e}" for k_, v in errs.items()})
+    print("vs unrounded MLP", {k_: f"{v:.1e}" for k_, v in plain.items()})
     assert max(errs.values()) < NORM_RTOL, errs
+    mlp_side = [n for n in want if n.startswith("Dense") or n.startswith("appearance")]
+    assert all(errs[n] < plain[n] for n in mlp_side), (errs, plain)
 
 
 def _proposal_mirror_grads(prop, o, d, aabb, Np, pj, shift_p, w_main, bins, loss_w):
@@ -259,7 +277,7 @@ def test_bf16_proposal_backward_matches_rounding_mirror(monkeypatch):
     got = lp.to_reference(grads)["proposal"]
     errs = {nm: _nrel(got[nm], want[nm]) for nm in ("vector", "matrix", "w1", "b1", "w2", "b2")}
     print({k_: f"{v:.1e}" for k_, v in errs.items()})
-    assert max(errs.values()) < NORM_RTOL, errs
+    assert max(errs.values()) < NORM_RTOL_PROPOSAL, errs
 
 
 def test_bf16_gradients_against_fp64_finite_differences():
