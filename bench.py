@@ -338,6 +338,39 @@ def time_render(state, w, data, views, chunk=65536):
     return total / (e0.elapsed_time(e1) / 1e3), img
 
 
+def scene_truth_comparison(states, data, views, per_view=4096, seed=5):
+    """Full-frame render scored against the FP64 scene itself, on a seeded subset of
+    `per_view` pixels of each of the `views` rendered views: PSNR of each path against
+    the FP64 quadrature colours (4096 samples per ray) and the mean absolute error of its
+    DIST_MEDIAN depth against the analytic median depth (SphereScene.median_depth), over
+    rays where both are finite, plus how often both agree on whether the ray
+    terminates."""
+    from tensorf_gb300 import cameras, render
+
+    cams = (data.test_cams * (1 + views // len(data.test_cams)))[:views]
+    rng = np.random.default_rng(seed)
+    os_, ds_ = [], []
+    for cam in cams:
+        pix = torch.as_tensor(rng.integers(0, cam.image_width * cam.image_height, size=per_view))
+        rr = cam.pixel_rays_wrt_world(pix)
+        os_.append(rr.origins)
+        ds_.append(rr.directions)
+    rays = cameras.Rays3D(torch.cat(os_), torch.cat(ds_))
+    target = data.sc.render(rays, 4096)
+    truth = torch.as_tensor(data.sc.median_depth(rays.origins.cpu().numpy(), rays.directions.cpu().numpy()))
+    out = {"pixels": views * per_view, "views": views}
+    for name in ("plain_fp32", "proposal_bf16"):
+        w, st, _ = states[name]
+        img = eval_rays(st, w, rays)
+        dep = eval_rays(st, w, rays, render.RenderMode.DIST_MEDIAN).cpu().double()
+        both = torch.isfinite(dep) & torch.isfinite(truth)
+        out[name] = {"psnr_vs_fp64_db": round(psnr(img, target), 3),
+                     "median_depth_abs_err_vs_fp64": round(float((dep[both] - truth[both]).abs().mean()), 5),
+                     "termination_agree_vs_fp64": round(float((torch.isfinite(dep) == torch.isfinite(truth))
+                                                              .float().mean()), 4)}
+    return out
+
+
 def algorithmic_bytes(w, phase):
     """Algorithmic bytes of one launch of each gather/scatter phase."""
     R, N, k = w["R"], w["N"], w["k"]
@@ -548,6 +581,7 @@ def run_ours(args):
             variants[name] = {"train_rays_per_s": round(w["R"] * args.steps / (vms / 1e3), 1),
                               "ms_per_step": round(vms / args.steps, 4),
                               "phase_ms": {p: round(v, 4) for p, v in vph.items()},
+                              "kernels": kernel_rooflines(w, vph, l2),
                               "density_samples": w["N"], "appearance_samples": w["k"],
                               "proposal_samples": w["proposal"]}
             states[name] = (w, st, vdone)
@@ -581,6 +615,7 @@ def run_ours(args):
             "median_depth_abs_diff_mean": round(float((d0[both] - d1[both]).abs().mean()), 5) if both.any() else None,
             "median_depth_terminated_agree": round(float((torch.isfinite(d0) == torch.isfinite(d1)).float().mean()), 4),
             "render_views": args.render_views, "render_chunk": 65536,
+            "against_fp64_scene": scene_truth_comparison(states, data, args.render_views),
         }
     if not args.headline_only and world == 1:
         line["unbounded"] = run_unbounded(args)

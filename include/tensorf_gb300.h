@@ -182,8 +182,10 @@ TVM_API uint64_t tvm_kernel_launches(void);
  * events[i] on their stream at the boundary before phase i and events[n_phases] after
  * the last one (phases: 0 proposal network forward + resampling, 1 density fwd,
  * 2 composite+select, 3 appearance gather, 4 MLP fwd, 5 colour+loss, 6 MLP bwd,
- * 7 appearance scatter, 8 composite bwd, 9 density scatter, 10 proposal loss +
- * backward, 11 Adam). Unused trailing phases record nothing. NULL disables. */
+ * 7 appearance scatter, 8 composite bwd, 9 density scatter, 10 the wait for the
+ * proposal backward on its side stream, 11 Adam: in tvm_train_step, the density
+ * field's update and the wait for the other segments' updates on their side stream).
+ * Unused trailing phases record nothing. NULL disables. */
 TVM_API int tvm_set_phase_events(void* const* events, int32_t n);
 
 /* ---- parameter layout ---------------------------------------------------------- */
@@ -329,6 +331,17 @@ TVM_API int tvm_train_step(const tvm_model_desc* model, void* params, void* shad
                    void* adam_mu, void* adam_nu, const tvm_adam_desc* adam, const tvm_rays* rays,
                    const float* colors, const tvm_render_desc* cfg, float* loss_out,
                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Side streams. With a proposal network (TVM_SAMPLER_PROPOSAL), tvm_train_step and
+ * tvm_loss_and_grad run the proposal's bound loss and backward on a second stream,
+ * forked from `stream` after the forward compositing. tvm_train_step also applies Adam
+ * segment by segment as each segment's gradient becomes final: the appearance field and
+ * the FeatureMlp on a third stream while `stream` runs the density backward, the
+ * proposal network on the second, the density field on `stream`. Both side streams
+ * belong to the calling thread and device, run at the lowest priority and are created
+ * on first use (with four events); all their work is joined back into `stream` before
+ * the call's work there ends, so work a caller orders after the call on `stream` sees
+ * every gradient and every update. */
 
 /* Loss and gradients only (no Adam): used by gradient checks. grads ACCUMULATE. */
 TVM_API int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, const void* shadow,

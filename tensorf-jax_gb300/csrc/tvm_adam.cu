@@ -93,6 +93,16 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
   return check_launch("adam");
 }
 
+int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
+                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st) {
+  if (hi <= lo) return TVM_OK;
+  // lo is a segment start (a multiple of 64 elements), so the offset buffers keep their
+  // 16-byte alignment and the kernel's float4 lanes stay whole.
+  const bool sh = shadow != nullptr && lo < shadow_n;
+  return launch_adam(params + lo, grads + lo, mu + lo, nu + lo, hi - lo, mlp_begin - lo, d, sh ? shadow + lo : nullptr,
+                     sh ? shadow_n - lo : 0, st);
+}
+
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st) {
   if (n == 0) return TVM_OK;
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 8);

@@ -76,6 +76,37 @@ int ensure_smem_limit(const void* fn, int bytes, const char* what) {
   return TVM_OK;
 }
 
+// Two more streams per calling thread and device, each with a fork and a join event,
+// both at the lowest priority (the main stream holds the longer chain):
+//  - `stream`: the proposal network's backward, which depends only on the forward's
+//    proposal and main-field weights, runs there concurrently with the main field's
+//    latency-bound backward kernels;
+//  - `stream2`: in a training step, Adam over the appearance field and the FeatureMlp
+//    (HBM-bound) runs there as soon as their gradients are final, concurrently with the
+//    density scatter (L2-bound).
+struct SideStream {
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
+};
+
+static int side_stream(SideStream*& out) {
+  static thread_local std::vector<SideStream> per_device;
+  const int dev = current_device();
+  if ((int)per_device.size() <= dev) per_device.resize(dev + 1);
+  SideStream& s = per_device[dev];
+  if (s.stream == nullptr) {
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, least);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream2, cudaStreamNonBlocking, least);
+    for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2})
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "side stream: %s", cudaGetErrorString(e));
+  }
+  out = &s;
+  return TVM_OK;
+}
+
 static int64_t seg(int64_t& off, int64_t n) {
   const int64_t at = off;
   off = round_up(off + n, 64);
@@ -263,7 +294,7 @@ struct PassBufs {
   int32_t* sel;
   float *w_sel, *p_last, *q_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
   // proposal-guided sampling
-  float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p, *dx_p;
+  float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p;
   int32_t* bins;
 };
 
@@ -302,7 +333,6 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
       b.g_wp = ws.take<float>(S);
       b.dz_p = ws.take<float>(S);
       b.loss_p = ws.take<float>(1);
-      b.dx_p = prop_scatter_supported(m.proposal_grid) ? ws.take<float>(S * 12) : nullptr;
     }
   }
   return b;
@@ -336,10 +366,21 @@ static SamplerArgs proposal_sampler(const tvm_render_desc& c) {
   return s;
 }
 
-// render_rays forward, and (if grads != null) the loss and backward of training_step.
+// Adam of a training step, applied segment by segment inside run_pass as each
+// segment's gradient becomes final.
+struct AdamPlan {
+  float *params, *mu, *nu;
+  tvm_adam_desc desc;
+  __nv_bfloat16* shadow;  // BF16 models: the field shadow, refreshed with the update
+  int64_t shadow_n;
+};
+
+// render_rays forward, and (if grads != null) the loss and backward of training_step,
+// and (if adam != null) the step's Adam update.
 static int run_pass(const tvm_model_desc& m, const float* params, const void* shadow, float* grads,
                     const tvm_rays& rays, const float* colors, const tvm_render_desc& c,
-                    float* loss, float* out, void* workspace, size_t ws_bytes, cudaStream_t st) {
+                    float* loss, float* out, void* workspace, size_t ws_bytes, cudaStream_t st,
+                    const AdamPlan* adam = nullptr) {
   tvm_param_layout L;
   make_layout(m, L);
   const bool backward = grads != nullptr;
@@ -389,6 +430,41 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
                                   c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.q_last, b.wsum, nullptr,
                                   (proposal && backward) ? b.w_dense : nullptr, st));
+  SideStream* side = nullptr;
+  bool prop_forked = false, adam_forked = false;
+  // Segments of the flat layout updated by Adam at different points of the pass.
+  const bool has_prop = m.proposal_grid > 0;
+  auto adam_seg = [&](int64_t lo, int64_t hi, cudaStream_t s_) {
+    return launch_adam_range(adam->params, grads, adam->mu, adam->nu, lo, hi, L.mlp_begin, adam->desc, adam->shadow,
+                             adam->shadow_n, s_);
+  };
+  if (proposal && backward) {
+    // Proposal bound loss on the main weights, then the proposal network backward, on the
+    // side stream: they need only the forward's outputs and write only the proposal's
+    // own gradient segments.
+    TVM_TRY(side_stream(side));
+    cudaStream_t aux = side->stream;
+    cudaError_t e = cudaEventRecord(side->fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, side->fork, 0);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), aux);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal fork: %s", cudaGetErrorString(e));
+    TVM_TRY(launch_prop_loss(b.w_dense, b.w_p, b.bins, R, c.proposal_samples, c.density_samples,
+                             c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, aux));
+    TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, aux));
+    const FieldView fp = proposal_field(m, L, params, shadow);
+    const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
+                     params + L.proposal_b2, c.proposal_shift, nullptr, nullptr};
+    TVM_TRY(launch_prop_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins, rays.directions,
+                            R, sp, edges, c.proposal_jitter, b.dz_p, pm, grads + L.proposal_w1,
+                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, aux));
+    if (adam) {  // the proposal's own parameters: fields, then its MLP
+      TVM_TRY(adam_seg(L.proposal_lines, L.mlp_begin, aux));
+      TVM_TRY(adam_seg(L.proposal_w1, L.total, aux));
+    }
+    prop_forked = true;
+    e = cudaEventRecord(side->join, aux);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal join record: %s", cudaGetErrorString(e));
+  }
   phase_mark(3, st);
   TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(4, st);
@@ -410,6 +486,20 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
+  if (adam) {
+    // The appearance field's and the FeatureMlp's gradients are final here, and nothing
+    // later in the pass reads those parameters: update them on the second side stream
+    // while the main stream runs the density backward.
+    if (side == nullptr) TVM_TRY(side_stream(side));
+    cudaError_t e = cudaEventRecord(side->fork2, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream2, side->fork2, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam fork: %s", cudaGetErrorString(e));
+    TVM_TRY(adam_seg(L.appearance_lines, has_prop ? L.proposal_lines : L.mlp_begin, side->stream2));
+    TVM_TRY(adam_seg(L.mlp_begin, has_prop ? L.proposal_w1 : L.total, side->stream2));
+    e = cudaEventRecord(side->join2, side->stream2);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam join record: %s", cudaGetErrorString(e));
+    adam_forked = true;
+  }
   phase_mark(8, st);
   TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
                                b.gsum, st));
@@ -417,21 +507,18 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
                              rays.directions, R, s, b.gsum, st));
   phase_mark(10, st);
-  if (proposal) {
-    // Proposal bound loss on the main weights, then the proposal network backward.
-    cudaError_t e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), st);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
-    TVM_TRY(launch_prop_loss(b.w_dense, b.w_p, b.bins, R, c.proposal_samples, c.density_samples,
-                             c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, st));
-    TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, st));
-    const FieldView fp = proposal_field(m, L, params, shadow);
-    const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
-                     params + L.proposal_b2, c.proposal_shift, nullptr, nullptr};
-    TVM_TRY(launch_prop_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins, rays.directions,
-                            R, sp, edges, c.proposal_jitter, b.dz_p, pm, grads + L.proposal_w1,
-                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, b.dx_p, st));
+  if (prop_forked) {  // join: the proposal backward (and its Adam) on the side stream is done
+    cudaError_t e = cudaStreamWaitEvent(st, side->join, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal join: %s", cudaGetErrorString(e));
   }
   phase_mark(11, st);
+  if (adam) {
+    TVM_TRY(adam_seg(L.density_lines, L.appearance_lines, st));  // the density field, last to be final
+    if (adam_forked) {
+      cudaError_t e = cudaStreamWaitEvent(st, side->join2, 0);
+      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam join: %s", cudaGetErrorString(e));
+    }
+  }
   return TVM_OK;
 }
 
@@ -744,10 +831,36 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
                    void* adam_nu, const tvm_adam_desc* adam, const tvm_rays* rays, const float* colors,
                    const tvm_render_desc* cfg, float* loss_out, void* workspace, size_t workspace_bytes,
                    void* stream) {
-  TVM_TRY(tvm_loss_and_grad(model, params, shadow, grads, rays, colors, cfg, loss_out, workspace,
-                            workspace_bytes, stream));
-  TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
-  phase_mark(12, as_stream(stream));
+  // The checks of tvm_loss_and_grad and tvm_adam_step, then one pass that applies Adam
+  // segment by segment as the gradients become final (same result as the two calls).
+  TVM_TRY(validate_model(model));
+  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_render(cfg, rays->count, true, model));
+  TVM_TRY(validate_params(model, params, shadow));
+  TVM_REQUIRE(cfg->mode == TVM_MODE_RGB, TVM_ERR_INVALID, "training needs RGB mode");
+  TVM_REQUIRE(grads && aligned(grads, 16), TVM_ERR_ALIGN, "grads NULL or not 16-byte aligned");
+  TVM_REQUIRE(rays->count == 0 || (colors && loss_out && workspace), TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(adam_mu && adam_nu && adam, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(adam_mu, 16) && aligned(adam_nu, 16), TVM_ERR_ALIGN, "Adam buffers must be 16-byte aligned");
+  TVM_REQUIRE(adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  cudaStream_t st = as_stream(stream);
+  tvm_param_layout L;
+  make_layout(*model, L);
+  if (rays->count == 0) {  // no rays: a plain Adam step on zero gradients
+    TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
+    phase_mark(12, st);
+    return TVM_OK;
+  }
+  if (loss_out) {
+    cudaError_t e = cudaMemsetAsync(loss_out, 0, sizeof(float), st);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+  }
+  const bool bf16 = shadow && model->dtype == TVM_BF16;
+  const AdamPlan plan{static_cast<float*>(params), static_cast<float*>(adam_mu), static_cast<float*>(adam_nu), *adam,
+                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0};
+  TVM_TRY(run_pass(*model, static_cast<const float*>(params), shadow, static_cast<float*>(grads), *rays, colors, *cfg,
+                   loss_out, nullptr, workspace, workspace_bytes, st, &plan));
+  phase_mark(12, st);
   return TVM_OK;
 }
 

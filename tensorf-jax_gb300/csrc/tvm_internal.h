@@ -131,14 +131,10 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
                          const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
                          cudaStream_t st);
 // Fused proposal backward from dz = dL/d(pre-softplus): field scatter and MLP weight
-// gradients (all accumulate). dx_buf (R * Np * 12 floats, 16-byte aligned, or NULL):
-// scratch for the per-sample feature gradients, which lets a field that fits shared
-// memory (prop_scatter_supported) be scattered without global contention.
-bool prop_scatter_supported(int G);
+// gradients (all accumulate).
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
-                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, float* dx_buf,
-                    cudaStream_t st);
+                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st);
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                     const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
                     cudaStream_t st);
@@ -154,6 +150,10 @@ int launch_loss_f64(const tvm_param_layout& L, const tvm_model_desc& m, const fl
 // ---- Adam (tvm_adam.cu) ----
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
                 const tvm_adam_desc& a, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st);
+// Adam over the elements [lo, hi) of the flat buffers only (lo a segment start); the
+// learning-rate group and the shadow follow the element's place in the whole layout.
+int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
+                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st);
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
 
 }  // namespace tvm

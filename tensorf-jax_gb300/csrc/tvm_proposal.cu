@@ -173,7 +173,6 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
 // reduced over the block in shared memory, then added to global memory with one atomic
 // per weight per block.
 constexpr int PBWD_THREADS = 128;
-constexpr int PSC_THREADS = 512;  // prop_scatter_kernel
 
 template <typename T>
 __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
@@ -181,8 +180,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
     float* __restrict__ gplanes, const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
     SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter, const float* __restrict__ dz_in,
     int units, const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
-    float* __restrict__ gw1, float* __restrict__ gb1, float* __restrict__ gw2, float* __restrict__ gb2,
-    float* __restrict__ dx_out) {
+    float* __restrict__ gw1, float* __restrict__ gb1, float* __restrict__ gw2, float* __restrict__ gb2) {
   extern __shared__ __align__(16) float sm[];
   float* sw1 = sm;                          // transposed [U][16]
   float* sb1 = sw1 + 16 * units;            // [U]
@@ -266,16 +264,11 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
 #pragma unroll
   for (int i = 0; i < PROP_IN; ++i) sX[tid * 16 + i] = X[i];
   sdz[tid] = dz;
-  // Field gradient: the feature gradients go to dx_out for prop_scatter_kernel, or are
-  // scattered here.
+  // Field gradient scatter.
   bool any = false;
 #pragma unroll
   for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
-  if (valid && dx_out) {
-    float4* dst = reinterpret_cast<float4*>(dx_out + smp * 12);
-#pragma unroll
-    for (int q = 0; q < 3; ++q) dst[q] = make_float4(dX[4 * q], dX[4 * q + 1], dX[4 * q + 2], dX[4 * q + 3]);
-  } else if (valid && any) {
+  if (valid && any) {
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const PropPair& e = e3[m];
@@ -340,68 +333,6 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
       for (int q = 0; q < PBWD_THREADS; ++q) acc += sdz[q];
       if (acc != 0.f) atomicAdd(gb2, acc);
     }
-  }
-}
-
-// Proposal field gradient from the per-sample feature gradients dX (12 per sample,
-// pair-major), for fields small enough to privatise: CTA (part, m = blockIdx.y)
-// accumulates pair m's plane [G][G][4] and line [G][4] gradients over its share of the
-// rays in shared memory (no global contention: every sample of every ray lands in one
-// small field), then adds them to global memory once with float4 reductions. Thread
-// k of a CTA takes ray k % rays, bin k / rays, so a warp's 32 lanes sit on 32 different
-// rays and rarely hit one shared-memory word at once.
-template <typename T>
-__global__ void __launch_bounds__(PSC_THREADS) prop_scatter_kernel(
-    const T* __restrict__ lines, const T* __restrict__ planes, int G, float* __restrict__ glines,
-    float* __restrict__ gplanes, const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
-    SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter, const float* __restrict__ dX) {
-  extern __shared__ __align__(16) float sacc[];
-  const int m = blockIdx.y;
-  const int np4 = G * G, nl4 = G;  // float4 chunks of the plane and the line
-  float4* sP = reinterpret_cast<float4*>(sacc);
-  float4* sL = sP + np4;
-  for (int i = threadIdx.x; i < np4 + nl4; i += PSC_THREADS) sP[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  __syncthreads();
-  const int Np = s.N;
-  const int64_t r0 = R * blockIdx.x / gridDim.x, r1 = R * (blockIdx.x + 1) / gridDim.x;
-  const int64_t nr = r1 - r0;
-  int a, b, c;
-  mode_perm(m, a, b, c);
-  for (int64_t k = threadIdx.x; k < nr * Np; k += PSC_THREADS) {
-    const int64_t r = r0 + k % nr;
-    const int j = (int)(k / nr);
-    const int64_t smp = r * Np + j;
-    const float4 gx = __ldg(reinterpret_cast<const float4*>(dX + smp * 12) + m);
-    if (gx.x == 0.f && gx.y == 0.f && gx.z == 0.f && gx.w == 0.f) continue;
-    RayGeom g = load_ray(origins, dirs, r, s);
-    float t, len, x[3];
-    prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
-    PropPair e;
-    prop_pair<T>(lines, planes, G, m, grid_coord(x[a], G), grid_coord(x[b], G), grid_coord(x[c], G), e);
-    const float gv[4] = {gx.x, gx.y, gx.z, gx.w};
-    float* l0 = reinterpret_cast<float*>(sL + e.tl.i0);
-    float* l1 = reinterpret_cast<float*>(sL + e.tl.i1);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      atomicAdd(l0 + q, gv[q] * e.P[q] * e.tl.w0);
-      atomicAdd(l1 + q, gv[q] * e.P[q] * e.tl.w1);
-    }
-    const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
-    const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
-    const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
-#pragma unroll
-    for (int q4 = 0; q4 < 4; ++q4) {
-      float* pp = reinterpret_cast<float*>(sP + rows[q4] * G + cols[q4]);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) atomicAdd(pp + q, gv[q] * e.L[q] * w[q4]);
-    }
-  }
-  __syncthreads();
-  float4* gp = reinterpret_cast<float4*>(gplanes + (int64_t)m * G * G * PROP_C);
-  float4* gl = reinterpret_cast<float4*>(glines + (int64_t)m * G * PROP_C);
-  for (int i = threadIdx.x; i < np4 + nl4; i += PSC_THREADS) {
-    const float4 v = sP[i];
-    if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(i < np4 ? gp + i : gl + (i - np4), v);
   }
 }
 
@@ -608,7 +539,7 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
     const float* __restrict__ jitter, const float* __restrict__ dz_in, const float* __restrict__ w1,
     const float* __restrict__ b1, const float* __restrict__ w2, float* __restrict__ gw1, float* __restrict__ gb1,
-    float* __restrict__ gw2, float* __restrict__ gb2, float* __restrict__ dx_out) {
+    float* __restrict__ gw2, float* __restrict__ gb2) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + OFF_BAR + 8);
@@ -742,11 +673,7 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     bool any = false;
 #pragma unroll
     for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
-    if (valid && dx_out) {
-      float4* dst = reinterpret_cast<float4*>(dx_out + smp * 12);
-#pragma unroll
-      for (int q = 0; q < 3; ++q) dst[q] = make_float4(dX[4 * q], dX[4 * q + 1], dX[4 * q + 2], dX[4 * q + 3]);
-    } else if (valid && any) {
+    if (valid && any) {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         const PropPair& e = e3[m];
@@ -820,39 +747,12 @@ int prop_status(int32_t* out, cudaStream_t st) {
   return TVM_OK;
 }
 
-// Shared memory of prop_scatter_kernel: one pair's plane and line gradients.
-static size_t prop_scatter_smem(int G) { return ((size_t)G * G + G) * PROP_C * sizeof(float); }
-constexpr size_t kPropScatterMaxSmem = 200 * 1024;
-
-bool prop_scatter_supported(int G) { return prop_scatter_smem(G) <= kPropScatterMaxSmem; }
-
-template <typename T>
-static int launch_prop_scatter(const FieldView& f, float* glines, float* gplanes, const float* origins,
-                               const float* dirs, int64_t R, const SamplerArgs& s, const float* edges,
-                               const float* jitter, const float* dX, cudaStream_t st) {
-  const size_t smem = prop_scatter_smem(f.G);
-  auto fn = prop_scatter_kernel<T>;
-  TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal scatter"));
-  // At least 4096 samples per CTA, so that the one flush of the private field (G*G*4
-  // floats) stays small against the samples' reductions it replaces.
-  const int64_t parts = std::max<int64_t>(1, std::min<int64_t>({ceil_div(R * s.N, 4096), (int64_t)device_sms(), R}));
-  fn<<<dim3((unsigned)parts, 3), PSC_THREADS, smem, st>>>(static_cast<const T*>(f.lines),
-                                                          static_cast<const T*>(f.planes), f.G, glines, gplanes,
-                                                          origins, dirs, R, s, edges, jitter, dX);
-  return check_launch("prop_scatter");
-}
-
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
-                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, float* dx_buf,
-                    cudaStream_t st) {
+                    const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
   const int U = mlp.units;
-  // With a dX buffer and a field that fits shared memory, the MLP backward writes the
-  // feature gradients and prop_scatter_kernel scatters them; otherwise the MLP backward
-  // scatters into global memory directly.
-  float* dx_out = (dx_buf && prop_scatter_supported(f.G)) ? dx_buf : nullptr;
   if (f.dtype == TVM_BF16 && U == ptc::U) {
     TVM_TRY(ensure_smem_limit((const void*)ptc::prop_bwd_tc_kernel, ptc::SMEM, "proposal backward"));
     const int sms = device_sms();
@@ -860,10 +760,8 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * std::max(sms, 1));  // 2 CTAs fit an SM
     ptc::prop_bwd_tc_kernel<<<grid, ptc::THREADS, ptc::SMEM, st>>>(
         (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines, gplanes, origins, dirs, R, s, edges,
-        jitter, dz, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2, dx_out);
-    TVM_TRY(check_launch("prop_bwd_tc"));
-    if (!dx_out) return TVM_OK;
-    return launch_prop_scatter<__nv_bfloat16>(f, glines, gplanes, origins, dirs, R, s, edges, jitter, dx_out, st);
+        jitter, dz, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2);
+    return check_launch("prop_bwd_tc");
   }
   const size_t smem = ((size_t)18 * U + PBWD_THREADS * 16 + 2 * PBWD_THREADS * (U + 4) + PBWD_THREADS) * sizeof(float);
   const unsigned blocks = (unsigned)ceil_div(n, PBWD_THREADS);
@@ -872,20 +770,15 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
     TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines,
                                            gplanes, origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2,
-                                           gw1, gb1, gw2, gb2, dx_out);
-    TVM_TRY(check_launch("prop_bwd"));
-    if (!dx_out) return TVM_OK;
-    return launch_prop_scatter<__nv_bfloat16>(f, glines, gplanes, origins, dirs, R, s, edges, jitter, dx_out, st);
+                                           gw1, gb1, gw2, gb2);
   } else {
     auto fn = prop_bwd_kernel<float>;
     TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines, gplanes,
                                            origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2, gw1, gb1,
-                                           gw2, gb2, dx_out);
-    TVM_TRY(check_launch("prop_bwd"));
-    if (!dx_out) return TVM_OK;
-    return launch_prop_scatter<float>(f, glines, gplanes, origins, dirs, R, s, edges, jitter, dx_out, st);
+                                           gw2, gb2);
   }
+  return check_launch("prop_bwd");
 }
 
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,

@@ -107,6 +107,48 @@ class SphereScene:
                   ptr(aabb), ctypes.byref(rs), n_samples, ptr(out), stream_handle())
         return out
 
+    def median_depth(self, origins: onp.ndarray, directions: onp.ndarray) -> onp.ndarray:
+        """Exact median depth of each ray in FP64: the distance t at which the optical
+        depth from the ray origin reaches ln 2 (transmittance 1/2), from the ray-sphere
+        intersections (overlapping spheres add their densities), clipped to the aabb
+        segment; +inf where the ray keeps more than half its transmittance. This is
+        the analytic counterpart of RenderMode.DIST_MEDIAN, whose rendered value is
+        quantised to the sample grid."""
+        o = onp.asarray(origins, dtype=onp.float64)
+        d = onp.asarray(directions, dtype=onp.float64)
+        d = d / onp.linalg.norm(d, axis=1, keepdims=True)
+        lo_b, hi_b = onp.asarray(self.aabb[0]), onp.asarray(self.aabb[1])
+        with onp.errstate(divide="ignore", invalid="ignore"):
+            t1, t2 = (lo_b - o) / d, (hi_b - o) / d
+        t_near = onp.maximum(onp.nanmax(onp.minimum(t1, t2), axis=1), 0.0)
+        t_far = onp.nanmin(onp.maximum(t1, t2), axis=1)
+        oc = o[:, None, :] - self.centers[None, :, :]  # (n, S, 3)
+        b = onp.einsum("nsk,nk->ns", oc, d)
+        disc = b * b - (onp.einsum("nsk,nsk->ns", oc, oc) - self.radii[None, :] ** 2)
+        hit = disc > 0
+        root = onp.sqrt(onp.where(hit, disc, 0.0))
+        enter = onp.clip(onp.where(hit, -b - root, onp.inf), t_near[:, None], t_far[:, None])
+        leave = onp.clip(onp.where(hit, -b + root, onp.inf), t_near[:, None], t_far[:, None])
+        S = self.radii.shape[0]
+        t_ev = onp.concatenate([enter, leave], axis=1)
+        step = onp.concatenate([onp.ones((o.shape[0], S)), -onp.ones((o.shape[0], S))], axis=1)
+        step[~onp.isfinite(t_ev)] = 0.0
+        t_ev = onp.where(onp.isfinite(t_ev), t_ev, onp.inf)
+        order = onp.argsort(t_ev, axis=1, kind="stable")
+        t_ev = onp.take_along_axis(t_ev, order, axis=1)
+        count = onp.cumsum(onp.take_along_axis(step, order, axis=1), axis=1)  # spheres covering [t_k, t_k+1)
+        seg = onp.diff(t_ev, axis=1)
+        seg = onp.where(onp.isfinite(seg), seg, 0.0)
+        sig = self.density * count[:, :-1]
+        tau = onp.concatenate([onp.zeros((o.shape[0], 1)), onp.cumsum(sig * seg, axis=1)], axis=1)
+        target = onp.log(2.0)
+        reached = tau >= target
+        out = onp.full(o.shape[0], onp.inf)
+        rows = onp.nonzero(reached.any(axis=1))[0]
+        k = onp.argmax(reached[rows], axis=1)  # first event with tau >= ln 2; tau[:, 0] = 0
+        out[rows] = t_ev[rows, k - 1] + (target - tau[rows, k - 1]) / sig[rows, k - 1]
+        return out
+
     @staticmethod
     def training_pixels(cams: List[cameras.Camera], total: int, seed: int) -> Tuple[onp.ndarray, onp.ndarray]:
         """The (camera index, flat pixel index) of each of ``total`` training rays, in
@@ -127,15 +169,19 @@ class SphereScene:
                       n_samples: int = 4096) -> Tuple[cameras.Rays3D, torch.Tensor]:
         """``total`` random pixels over the cameras with their FP64 target colours."""
         cam_idx, pix = self.training_pixels(cams, total, seed)
+        order = onp.argsort(cam_idx, kind="stable")  # batch positions grouped by camera
+        bounds = onp.searchsorted(cam_idx[order], onp.arange(len(cams) + 1))
+        os_, ds_ = [], []
+        for i, cam in enumerate(cams):
+            sel = order[bounds[i]:bounds[i + 1]]
+            if sel.size:
+                rr = cam.pixel_rays_wrt_world(torch.as_tensor(pix[sel], dtype=torch.int64))
+                os_.append(rr.origins)
+                ds_.append(rr.directions)
+        at = torch.as_tensor(order, device="cuda")
         o = torch.empty((total, 3), dtype=torch.float32, device="cuda")
         d = torch.empty((total, 3), dtype=torch.float32, device="cuda")
-        for i, cam in enumerate(cams):
-            sel = onp.nonzero(cam_idx == i)[0]
-            if sel.size == 0:
-                continue
-            rr = cam.pixel_rays_wrt_world(torch.as_tensor(pix[sel], dtype=torch.int64))
-            at = torch.as_tensor(sel, device="cuda")
-            o[at] = rr.origins
-            d[at] = rr.directions
+        o[at] = torch.cat(os_)
+        d[at] = torch.cat(ds_)
         rays = cameras.Rays3D(origins=o, directions=d)
         return rays, self.render(rays, n_samples)
