@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define TVM_ABI_VERSION 1
+#define TVM_ABI_VERSION 2
 
 /* Symbols of this library are exported with default visibility. */
 #ifndef TVM_API
@@ -97,7 +97,8 @@ typedef struct {
   int32_t proposal_grid;       /* proposal VM grid (e.g. 64); 0 = no proposal network */
   int32_t proposal_rank;       /* proposal components per pair: 4 */
   int32_t proposal_units;      /* proposal MLP hidden width (16 -> units -> 1): 64 */
-  int32_t _pad;
+  int32_t num_cameras;         /* FeatureMlp.num_cameras: FiLM camera embeddings (networks.py:103-111);
+                                  0 = none. Needs an even `units`. */
 } tvm_model_desc;
 
 /* MLP arithmetic. DEFAULT: TVM_F32 models run the dense layers on tcgen05 tensor
@@ -127,6 +128,8 @@ typedef struct {
   int64_t shadow_total;
   int32_t encoded_dim; /* MLP input width after the fourier encoding (150 for n=2) */
   int32_t _pad;
+  int64_t mlp_embed;   /* camera embedding table (num_cameras, units) of the FeatureMlp's
+                          nn.Embed (MLP lr group); 0 when num_cameras == 0 */
 } tvm_param_layout;
 
 /* A batch of rays (cameras.Rays3D, cameras.py:10-20), device pointers. */
@@ -134,6 +137,8 @@ typedef struct {
   int64_t count;          /* R */
   const float* origins;   /* (R, 3) */
   const float* directions;/* (R, 3) */
+  const int32_t* camera_indices; /* (R,) camera of each ray, for models with num_cameras > 0
+                                    (indices are clamped into [0, num_cameras)); else unused */
 } tvm_rays;
 
 /* Per-call render configuration (render.RenderConfig, render.py:26-36, plus the
@@ -170,6 +175,9 @@ typedef struct {
   float lr_decay;   /* multiplier from the exponential decay (training.py:158-181) */
   int32_t count;    /* step count after increment: 1 on the first update */
   int32_t _pad;
+  float* grad_sq;   /* optional device float, or NULL: overwritten with the sum of the squared
+                       gradients the update consumed, the square of optax.global_norm(grads)
+                       that training_step logs as grad_norm (training.py:190-196) */
 } tvm_adam_desc;
 
 /* ---- library ---------------------------------------------------------------------- */
@@ -251,16 +259,19 @@ TVM_API int tvm_topk_select(const float* p, const float* gumbel, int32_t gumbel_
 /* ---- (d) FeatureMlp (networks.py:45-121) --------------------------------------------- */
 /* features (n, 3*C_a), viewdirs (n, 3) -> rgb (n, 3). params: flat buffer in the
  * tvm_param_layout layout (master dtype float32; TVM_BF16 models use bf16 tensor
- * cores, TVM_F32 models float32 arithmetic). workspace: tvm_mlp_workspace_size(). */
+ * cores, TVM_F32 models float32 arithmetic). camera_indices (n,): camera of each row
+ * for models with num_cameras > 0 (networks.py:103-111), else NULL. workspace:
+ * tvm_mlp_workspace_size(). Models with camera embeddings run the layered GEMMs with a
+ * separate FiLM pass (the fused and pipelined kernels take models without them). */
 TVM_API size_t tvm_mlp_workspace_size(const tvm_model_desc* model, int64_t n);
 TVM_API int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* features,
-                const float* viewdirs, int64_t n, float* rgb, void* workspace,
+                const float* viewdirs, const int32_t* camera_indices, int64_t n, float* rgb, void* workspace,
                 size_t workspace_bytes, void* stream);
 /* grad_rgb (n, 3) -> grad_features (n, 3*C_a) (overwritten, may be NULL) and
  * ACCUMULATES the MLP weight gradients into grads (flat layout). */
 TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
-                const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
-                void* grads, void* workspace, size_t workspace_bytes, void* stream);
+                const float* viewdirs, const int32_t* camera_indices, int64_t n, const float* grad_rgb,
+                float* grad_features, void* grads, void* workspace, size_t workspace_bytes, void* stream);
 
 /* FeatureMlp forward without a caller workspace. This function has no counterpart in
  * the reference. It computes the same rgb as tvm_mlp_fwd, with the same kernels, but
@@ -280,7 +291,8 @@ TVM_API int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const f
  * model (144 features, 27 squash, 2/2 frequencies, 128 units) that is 20,164 rows. A
  * TVM_BF16 model with those dimensions runs the fused kernel: it needs only the
  * 87,040-byte packed weights, so n is not limited. Larger n returns TVM_ERR_SHAPE
- * before any launch, and the message gives the maximum for the model.
+ * before any launch, and the message gives the maximum for the model. It takes no
+ * camera indices: models with camera embeddings return TVM_ERR_UNSUPPORTED.
  *
  * Alignment: params must be 16-byte aligned (TVM_ERR_ALIGN otherwise). TVM_F32
  * models accept any features pointer; TVM_BF16 models read features with 16-byte
@@ -353,7 +365,7 @@ TVM_API int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, c
  * gradients, done on the device. It follows render_rays (render.py:105-279, RGB mode)
  * and the MSE of training_step (training.py:121-134) in double precision. Optionally
  * params[perturb_index] + perturb_delta replaces one parameter (-1: none). It supports
- * TVM_F32 models, the bounded sampler, and k == N <= 1024: every sample reaches the
+ * TVM_F32 models without camera embeddings, the bounded sampler, and k == N <= 1024: every sample reaches the
  * appearance path, so the loss has no selection discontinuity. *loss_out (device
  * double) is overwritten. This is a check path, not tuned for speed. */
 TVM_API size_t tvm_loss_f64_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg,

@@ -303,11 +303,14 @@ def fourier_encode(coords: torch.Tensor, n_freqs: int) -> torch.Tensor:
 
 
 def mlp_init(feat_dim: int, n_freqs_feat: int, n_freqs_view: int, gen: torch.Generator,
-             squash: int = 27, units: int = 128, dtype=torch.float64) -> Dict[str, Dict[str, torch.Tensor]]:
+             squash: int = 27, units: int = 128, dtype=torch.float64,
+             num_cameras: Optional[int] = None) -> Dict[str, Dict[str, torch.Tensor]]:
     """FeatureMlp parameters in flax's tree layout (networks.py:9-10, 57-117): kernels
     are (in, out); lecun_normal / kaiming_normal variances 1/fan_in and 2/fan_in
     (flax draws truncated normals; a plain normal of the same variance is used here,
-    which only changes initial values, never the forward function); biases zero."""
+    which only changes initial values, never the forward function); biases zero. With
+    num_cameras, the camera embedding table of nn.Embed (networks.py:104-106) as
+    "Embed_0": {"embedding": (num_cameras, units)}, variance 1 / num_cameras."""
     enc = squash + 3 + 2 * n_freqs_feat * squash + 2 * n_freqs_view * 3
 
     def normal(fan_in, fan_out, var):
@@ -318,15 +321,23 @@ def mlp_init(feat_dim: int, n_freqs_feat: int, n_freqs_view: int, gen: torch.Gen
         "Dense_1": {"kernel": normal(enc, units, 2.0), "bias": torch.zeros(units, dtype=dtype)},
         "Dense_2": {"kernel": normal(units, units, 2.0), "bias": torch.zeros(units, dtype=dtype)},
         "Dense_3": {"kernel": normal(units, 3, 1.0), "bias": torch.zeros(3, dtype=dtype)},
+        **({"Embed_0": {"embedding": normal(num_cameras, units, 1.0)}} if num_cameras else {}),
     }
 
 
-def feature_mlp(params, features: torch.Tensor, viewdirs: torch.Tensor, n_freqs_feat: int, n_freqs_view: int) -> torch.Tensor:
-    """``FeatureMlp.__call__`` without camera embeddings (networks.py:45-121)."""
+def feature_mlp(params, features: torch.Tensor, viewdirs: torch.Tensor, n_freqs_feat: int, n_freqs_view: int,
+                camera_indices: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """``FeatureMlp.__call__`` (networks.py:45-121). With an "Embed_0" table, the FiLM
+    step of networks.py:103-111 after layer 2: the upper half of the units becomes
+    cond[:U/2] * x[U/2:] + cond[U/2:] with cond the row's camera embedding."""
     f = features @ params["Dense_0"]["kernel"]
     x = torch.cat([f, viewdirs, fourier_encode(f, n_freqs_feat), fourier_encode(viewdirs, n_freqs_view)], dim=-1)
     x = torch.relu(x @ params["Dense_1"]["kernel"] + params["Dense_1"]["bias"])
     x = torch.relu(x @ params["Dense_2"]["kernel"] + params["Dense_2"]["bias"])
+    if "Embed_0" in params:
+        cond = params["Embed_0"]["embedding"][camera_indices.long()]
+        h = x.shape[-1] // 2
+        x = torch.cat([x[..., :h], cond[..., :h] * x[..., h:] + cond[..., h:]], dim=-1)
     x = x @ params["Dense_3"]["kernel"] + params["Dense_3"]["bias"]
     return torch.sigmoid(x)
 
@@ -338,7 +349,8 @@ def render_rays(params, aabb: torch.Tensor, origins: torch.Tensor, directions: t
                 density_samples: int, appearance_samples: int, jitter: Optional[torch.Tensor],
                 gumbel: torch.Tensor, n_freqs_feat: int = 2, n_freqs_view: int = 2,
                 density_shift: float = 10.0, mode: str = "rgb", scene_contraction: bool = False,
-                schedule: Optional[torch.Tensor] = None, return_aux: bool = False):
+                schedule: Optional[torch.Tensor] = None, return_aux: bool = False,
+                camera_indices: Optional[torch.Tensor] = None):
     """``render_rays`` (render.py:105-279) with explicit noise.
 
     params: dict with 'density' (vector, matrix), 'appearance' (vector, matrix) in the
@@ -374,7 +386,12 @@ def render_rays(params, aabb: torch.Tensor, origins: torch.Tensor, directions: t
         afeat = vm_interpolate(avec, amat, vis)
         afeat = afeat.permute(1, 2, 0).reshape(r * k, -1)
         viewdirs = directions[:, None, :].expand(r, k, 3).reshape(-1, 3)
-        vis_rgb = feature_mlp(params["mlp"], afeat, viewdirs, n_freqs_feat, n_freqs_view).reshape(r, k, 3)
+        if camera_indices is None:
+            vis_rgb = feature_mlp(params["mlp"], afeat, viewdirs, n_freqs_feat, n_freqs_view)
+        else:  # each ray's camera for its k appearance samples (render.py:492-497)
+            cams = camera_indices[:, None].expand(r, k).reshape(-1)
+            vis_rgb = feature_mlp(params["mlp"], afeat, viewdirs, n_freqs_feat, n_freqs_view, camera_indices=cams)
+        vis_rgb = vis_rgb.reshape(r, k, 3)
         rgb = torch.zeros((r, n, 3), dtype=origins.dtype)
         rgb = rgb.index_put((ar.expand(r, k), idx), vis_rgb)
         sampled = p_term[ar, idx]

@@ -112,8 +112,8 @@ ffi::Error MlpFwd(cudaStream_t s, ffi::Buffer<ffi::F32> params, ffi::Buffer<ffi:
   const tvm_model_desc m =
       model_desc(grid, density_channels, appearance_channels, feature_n_freqs, viewdir_n_freqs, dtype);
   const int64_t n = static_cast<int64_t>(viewdirs.element_count() / 3);
-  return status_error(tvm_mlp_fwd(&m, params.typed_data(), features.typed_data(), viewdirs.typed_data(), n,
-                                  rgb->typed_data(), workspace->typed_data(), workspace->size_bytes(), s),
+  return status_error(tvm_mlp_fwd(&m, params.typed_data(), features.typed_data(), viewdirs.typed_data(), nullptr,
+                                  n, rgb->typed_data(), workspace->typed_data(), workspace->size_bytes(), s),
                       "tvm_mlp_fwd");
 }
 
@@ -141,8 +141,8 @@ ffi::Error MlpBwd(cudaStream_t s, ffi::Buffer<ffi::F32> params, ffi::Buffer<ffi:
   const int64_t n = static_cast<int64_t>(viewdirs.element_count() / 3);
   ffi::Error e = zero(s, grad_params->typed_data(), grad_params->size_bytes(), "grad_params");
   if (e.failure()) return e;
-  return status_error(tvm_mlp_bwd(&m, params.typed_data(), features.typed_data(), viewdirs.typed_data(), n,
-                                  grad_rgb.typed_data(), grad_features->typed_data(), grad_params->typed_data(),
+  return status_error(tvm_mlp_bwd(&m, params.typed_data(), features.typed_data(), viewdirs.typed_data(), nullptr,
+                                  n, grad_rgb.typed_data(), grad_features->typed_data(), grad_params->typed_data(),
                                   workspace->typed_data(), workspace->size_bytes(), s),
                       "tvm_mlp_bwd");
 }

@@ -14,6 +14,7 @@ namespace tvm {
 
 struct AdamScalars {
   float b1, b2, omb1, omb2, rbc1, rbc2, eps, lr_t, lr_m, decay;
+  float* grad_sq;  // accumulates the sum of g^2 when non-null
 };
 
 // mu_hat = mu / (1 - b1^t) and nu_hat = nu / (1 - b2^t) as products with the
@@ -28,16 +29,19 @@ __device__ __forceinline__ float adam_one(float p, float g, float& m, float& v, 
   return p + a.decay * (-lr * u);
 }
 
-// shadow (may be null): bf16 copy of the updated elements [0, shadow_n).
+// shadow (may be null): bf16 copy of the updated elements [0, shadow_n). With
+// a.grad_sq, every warp adds the squares of the gradients it consumed to it.
 __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float* __restrict__ g,
                                                    float* __restrict__ m, float* __restrict__ v, int64_t n,
                                                    int64_t mlp_begin, __nv_bfloat16* __restrict__ shadow,
                                                    int64_t shadow_n, AdamScalars a) {
   const int64_t n4 = n / 4;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float sq = 0.f;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
     float4 pp = reinterpret_cast<float4*>(p)[q];
     const float4 gg = reinterpret_cast<float4*>(g)[q];
+    sq += (gg.x * gg.x + gg.y * gg.y) + (gg.z * gg.z + gg.w * gg.w);
     float4 mm = reinterpret_cast<float4*>(m)[q];
     float4 vv = reinterpret_cast<float4*>(v)[q];
     const int64_t e = q * 4;
@@ -58,11 +62,16 @@ __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float*
   }
   for (int64_t e = n4 * 4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {
     float mm = m[e], vv = v[e];
+    sq += g[e] * g[e];
     p[e] = adam_one(p[e], g[e], mm, vv, (e < mlp_begin) ? a.lr_t : a.lr_m, a);
     m[e] = mm;
     v[e] = vv;
     g[e] = 0.f;
     if (shadow != nullptr && e < shadow_n) shadow[e] = __float2bfloat16_rn(p[e]);
+  }
+  if (a.grad_sq != nullptr) {  // every thread of the block reaches this point
+    sq = warp_sum(sq);
+    if ((threadIdx.x & 31) == 0 && sq != 0.f) atomicAdd(a.grad_sq, sq);
   }
 }
 
@@ -74,7 +83,7 @@ __global__ void shadow_kernel(const float* __restrict__ src, __nv_bfloat16* __re
 }
 
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
-                const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st) {
+                const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st, int blocks_per_sm) {
   if (n == 0) return TVM_OK;
   AdamScalars a;
   a.b1 = d.b1;
@@ -88,19 +97,21 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
   a.lr_t = d.lr_tensor;
   a.lr_m = d.lr_mlp;
   a.decay = d.lr_decay;
-  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n / 4 + 1, 256), 152 * 8);
+  a.grad_sq = d.grad_sq;
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n / 4 + 1, 256), (int64_t)blocks_per_sm * device_sms());
   adam_kernel<<<blocks, 256, 0, st>>>(params, grads, mu, nu, n, mlp_begin, shadow, shadow_n, a);
   return check_launch("adam");
 }
 
 int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
-                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st) {
+                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
+                      int blocks_per_sm) {
   if (hi <= lo) return TVM_OK;
   // lo is a segment start (a multiple of 64 elements), so the offset buffers keep their
   // 16-byte alignment and the kernel's float4 lanes stay whole.
   const bool sh = shadow != nullptr && lo < shadow_n;
   return launch_adam(params + lo, grads + lo, mu + lo, nu + lo, hi - lo, mlp_begin - lo, d, sh ? shadow + lo : nullptr,
-                     sh ? shadow_n - lo : 0, st);
+                     sh ? shadow_n - lo : 0, st, blocks_per_sm);
 }
 
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st) {

@@ -136,6 +136,10 @@ static int validate_model(const tvm_model_desc* m) {
               "model dtype %d not supported (TVM_F32, TVM_BF16)", m->dtype);
   TVM_REQUIRE(m->mlp_math == TVM_MLP_DEFAULT || (m->mlp_math == TVM_MLP_SIMT_F32 && m->dtype == TVM_F32),
               TVM_ERR_INVALID, "mlp_math=%d invalid for dtype %d", m->mlp_math, m->dtype);
+  TVM_REQUIRE(m->num_cameras >= 0 && m->num_cameras <= (1 << 24), TVM_ERR_SHAPE, "num_cameras=%d outside [0, 2^24]",
+              m->num_cameras);
+  TVM_REQUIRE(m->num_cameras == 0 || m->units % 2 == 0, TVM_ERR_SHAPE,
+              "camera embeddings condition half of the units: units=%d must be even", m->units);
   if (m->proposal_grid != 0) {
     TVM_REQUIRE(m->proposal_grid >= 2 && m->proposal_grid <= 1024, TVM_ERR_SHAPE, "proposal_grid=%d outside [2, 1024]",
                 m->proposal_grid);
@@ -169,6 +173,7 @@ static void make_layout(const tvm_model_desc& m, tvm_param_layout& L) {
   L.mlp_b2 = seg(off, m.units);
   L.mlp_w3 = seg(off, (int64_t)m.units * 3);
   L.mlp_b3 = seg(off, 3);
+  if (m.num_cameras > 0) L.mlp_embed = seg(off, (int64_t)m.num_cameras * m.units);
   if (Gp > 0) {
     L.proposal_w1 = seg(off, 16LL * m.proposal_units);
     L.proposal_b1 = seg(off, m.proposal_units);
@@ -188,8 +193,10 @@ static void make_layout(const tvm_model_desc& m, tvm_param_layout& L) {
   L.encoded_dim = enc;
 }
 
-static int validate_rays(const tvm_rays* rays) {
+static int validate_rays(const tvm_rays* rays, const tvm_model_desc* m = nullptr) {
   TVM_REQUIRE(rays != nullptr, TVM_ERR_INVALID, "rays is NULL");
+  TVM_REQUIRE(m == nullptr || m->num_cameras == 0 || rays->count == 0 || rays->camera_indices != nullptr,
+              TVM_ERR_INVALID, "a model with camera embeddings needs the rays' camera_indices");
   TVM_REQUIRE(rays->count >= 0 && rays->count <= (1LL << 31), TVM_ERR_SHAPE, "ray count %lld out of range",
               (long long)rays->count);
   TVM_REQUIRE(rays->count == 0 || (rays->origins && rays->directions), TVM_ERR_INVALID,
@@ -255,16 +262,17 @@ static MlpDims mlp_dims(const tvm_model_desc& m) {
   d.nf = m.feature_n_freqs;
   d.nv = m.viewdir_n_freqs;
   d.math = (m.dtype == TVM_BF16) ? 0 : (m.mlp_math == TVM_MLP_SIMT_F32 ? 2 : 1);
+  d.cams = m.num_cameras;
   return d;
 }
 
 static MlpWeights mlp_weights(const tvm_param_layout& L, const float* p) {
   return MlpWeights{p + L.mlp_w0, p + L.mlp_w1, p + L.mlp_b1, p + L.mlp_w2,
-                    p + L.mlp_b2, p + L.mlp_w3, p + L.mlp_b3};
+                    p + L.mlp_b2, p + L.mlp_w3, p + L.mlp_b3, L.mlp_embed ? p + L.mlp_embed : nullptr};
 }
 static MlpGrads mlp_grads(const tvm_param_layout& L, float* g) {
   return MlpGrads{g + L.mlp_w0, g + L.mlp_w1, g + L.mlp_b1, g + L.mlp_w2,
-                  g + L.mlp_b2, g + L.mlp_w3, g + L.mlp_b3};
+                  g + L.mlp_b2, g + L.mlp_w3, g + L.mlp_b3, L.mlp_embed ? g + L.mlp_embed : nullptr};
 }
 
 // Fields read by the gathers: bf16 shadow in BF16 mode, the FP32 master otherwise.
@@ -434,9 +442,11 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   bool prop_forked = false, adam_forked = false;
   // Segments of the flat layout updated by Adam at different points of the pass.
   const bool has_prop = m.proposal_grid > 0;
+  // Updates on a side stream run beside the main stream's kernels: a persistent grid of
+  // two blocks per SM keeps HBM busy and leaves the SMs room for them.
   auto adam_seg = [&](int64_t lo, int64_t hi, cudaStream_t s_) {
     return launch_adam_range(adam->params, grads, adam->mu, adam->nu, lo, hi, L.mlp_begin, adam->desc, adam->shadow,
-                             adam->shadow_n, s_);
+                             adam->shadow_n, s_, s_ == st ? 8 : 2);
   };
   if (proposal && backward) {
     // Proposal bound loss on the main weights, then the proposal network backward, on the
@@ -470,7 +480,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
-  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, k, R * k, b.rgb, ws, st));
+  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, rays.camera_indices, k, R * k, b.rgb, ws, st));
   phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
@@ -482,7 +492,8 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
                             b.gP, st));
   phase_mark(6, st);
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
-  TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, k, R * k, b.dZ3, b.dX0, ws2, st));
+  TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, rays.camera_indices, k, R * k, b.dZ3,
+                       b.dX0, ws2, st));
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
@@ -643,26 +654,30 @@ size_t tvm_mlp_workspace_size(const tvm_model_desc* model, int64_t n) {
 }
 
 int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* features,
-                const float* viewdirs, int64_t n, float* rgb, void* workspace, size_t workspace_bytes,
-                void* stream) {
+                const float* viewdirs, const int32_t* camera_indices, int64_t n, float* rgb, void* workspace,
+                size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
   TVM_REQUIRE(n == 0 || (params && features && viewdirs && rgb && workspace), TVM_ERR_INVALID,
               "NULL pointer");
+  TVM_REQUIRE(n == 0 || model->num_cameras == 0 || camera_indices, TVM_ERR_INVALID,
+              "a model with camera embeddings needs camera_indices");
   tvm_param_layout L;
   make_layout(*model, L);
   Workspace ws{static_cast<char*>(workspace), workspace_bytes, 0, false};
   return mlp_forward(mlp_dims(*model), mlp_weights(L, static_cast<const float*>(params)), features,
-                     viewdirs, 1, n, rgb, ws, as_stream(stream));
+                     viewdirs, camera_indices, 1, n, rgb, ws, as_stream(stream));
 }
 
 int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* features,
-                const float* viewdirs, int64_t n, const float* grad_rgb, float* grad_features,
-                void* grads, void* workspace, size_t workspace_bytes, void* stream) {
+                const float* viewdirs, const int32_t* camera_indices, int64_t n, const float* grad_rgb,
+                float* grad_features, void* grads, void* workspace, size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
   TVM_REQUIRE(n == 0 || (params && features && viewdirs && grad_rgb && grads && workspace),
               TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(n == 0 || model->num_cameras == 0 || camera_indices, TVM_ERR_INVALID,
+              "a model with camera embeddings needs camera_indices");
   if (n == 0) return TVM_OK;
   tvm_param_layout L;
   make_layout(*model, L);
@@ -675,11 +690,11 @@ int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* fe
   float* dz = ws.take<float>(n * 3);
   const size_t off = ws.used;
   TVM_REQUIRE(ws.ok(), TVM_ERR_WORKSPACE, "workspace too small");
-  TVM_TRY(mlp_forward(d, w, features, viewdirs, 1, n, rgb, ws, st));
+  TVM_TRY(mlp_forward(d, w, features, viewdirs, camera_indices, 1, n, rgb, ws, st));
   TVM_TRY(launch_sigmoid_bwd(rgb, grad_rgb, n, dz, st));
   Workspace ws2{static_cast<char*>(workspace), workspace_bytes, off, false};
-  return mlp_backward(d, w, mlp_grads(L, static_cast<float*>(grads)), features, viewdirs, 1, n, dz, grad_features,
-                      ws2, st);
+  return mlp_backward(d, w, mlp_grads(L, static_cast<float*>(grads)), features, viewdirs, camera_indices, 1, n, dz,
+                      grad_features, ws2, st);
 }
 
 size_t tvm_render_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t rays) {
@@ -706,7 +721,7 @@ int tvm_render_fwd(const tvm_model_desc* model, const void* params, const void* 
                    const tvm_rays* rays, const tvm_render_desc* cfg, float* out, void* workspace,
                    size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
-  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_rays(rays, model));
   TVM_TRY(validate_render(cfg, rays->count, true, model));
   TVM_TRY(validate_params(model, params, shadow));
   TVM_REQUIRE(rays->count == 0 || (out && workspace), TVM_ERR_INVALID, "out/workspace NULL");
@@ -718,7 +733,7 @@ int tvm_loss_and_grad(const tvm_model_desc* model, const void* params, const voi
                       const tvm_rays* rays, const float* colors, const tvm_render_desc* cfg,
                       float* loss_out, void* workspace, size_t workspace_bytes, void* stream) {
   TVM_TRY(validate_model(model));
-  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_rays(rays, model));
   TVM_TRY(validate_render(cfg, rays->count, true, model));
   TVM_TRY(validate_params(model, params, shadow));
   TVM_REQUIRE(cfg->mode == TVM_MODE_RGB, TVM_ERR_INVALID, "training needs RGB mode");
@@ -745,6 +760,10 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
   cudaStream_t st = as_stream(stream);
   const bool bf16 = shadow && model->dtype == TVM_BF16;
   TVM_REQUIRE(!bf16 || aligned(shadow, 8), TVM_ERR_ALIGN, "shadow must be 8-byte aligned");
+  if (adam->grad_sq) {
+    cudaError_t e = cudaMemsetAsync(adam->grad_sq, 0, sizeof(float), st);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+  }
   return launch_adam(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
                      static_cast<float*>(nu), L.total, L.mlp_begin, *adam,
                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0, st);
@@ -779,6 +798,7 @@ int tvm_gemm(int32_t math, int32_t a_trans, int32_t b_trans, int64_t M, int32_t 
 static int validate_loss_f64(const tvm_model_desc* model, const tvm_render_desc* cfg, int64_t R) {
   TVM_TRY(validate_model(model));
   TVM_REQUIRE(model->dtype == TVM_F32, TVM_ERR_DTYPE, "the FP64 loss checks TVM_F32 models");
+  TVM_REQUIRE(model->num_cameras == 0, TVM_ERR_UNSUPPORTED, "the FP64 loss covers models without camera embeddings");
   TVM_TRY(validate_render(cfg, R, false, model));
   TVM_REQUIRE(cfg->sampler == TVM_SAMPLER_BBOX && cfg->mode == TVM_MODE_RGB, TVM_ERR_UNSUPPORTED,
               "the FP64 loss supports the bounded sampler in RGB mode");
@@ -797,7 +817,7 @@ size_t tvm_loss_f64_workspace_size(const tvm_model_desc* model, const tvm_render
 int tvm_loss_f64(const tvm_model_desc* model, const void* params, const tvm_rays* rays, const float* colors,
                  const tvm_render_desc* cfg, int64_t perturb_index, double perturb_delta, double* loss_out,
                  void* workspace, size_t workspace_bytes, void* stream) {
-  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_rays(rays, model));
   TVM_TRY(validate_loss_f64(model, cfg, rays->count));
   TVM_REQUIRE(params && loss_out && (rays->count == 0 || colors), TVM_ERR_INVALID, "NULL pointer");
   tvm_param_layout L;
@@ -834,7 +854,7 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
   // The checks of tvm_loss_and_grad and tvm_adam_step, then one pass that applies Adam
   // segment by segment as the gradients become final (same result as the two calls).
   TVM_TRY(validate_model(model));
-  TVM_TRY(validate_rays(rays));
+  TVM_TRY(validate_rays(rays, model));
   TVM_TRY(validate_render(cfg, rays->count, true, model));
   TVM_TRY(validate_params(model, params, shadow));
   TVM_REQUIRE(cfg->mode == TVM_MODE_RGB, TVM_ERR_INVALID, "training needs RGB mode");
@@ -851,8 +871,9 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
     phase_mark(12, st);
     return TVM_OK;
   }
-  if (loss_out) {
-    cudaError_t e = cudaMemsetAsync(loss_out, 0, sizeof(float), st);
+  for (float* z : {loss_out, adam->grad_sq}) {
+    if (!z) continue;
+    cudaError_t e = cudaMemsetAsync(z, 0, sizeof(float), st);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
   }
   const bool bf16 = shadow && model->dtype == TVM_BF16;
@@ -940,6 +961,8 @@ int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params, 
                                const float* viewdirs, int64_t n, float* rgb, void* stream) {
   TVM_TRY(validate_model(model));
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(model->num_cameras == 0, TVM_ERR_UNSUPPORTED,
+              "the static-scratch forward takes models without camera embeddings");
   const MlpDims d = mlp_dims(*model);
   const size_t need = mlp_fwd_workspace_bytes(d, n);
   TVM_REQUIRE(need <= kMlpStaticScratchBytes, TVM_ERR_SHAPE,
@@ -954,7 +977,7 @@ int tvm_mlp_fwd_static_scratch(const tvm_model_desc* model, const void* params, 
   tvm_param_layout L;
   make_layout(*model, L);
   Workspace ws{static_cast<char*>(scratch), kMlpStaticScratchBytes, 0, false};
-  return mlp_forward(d, mlp_weights(L, static_cast<const float*>(params)), features, viewdirs, 1, n, rgb, ws,
+  return mlp_forward(d, mlp_weights(L, static_cast<const float*>(params)), features, viewdirs, nullptr, 1, n, rgb, ws,
                      as_stream(stream));
 }
 

@@ -80,24 +80,29 @@ struct MlpDims {
   int units;   // 128
   int nf, nv;  // fourier frequencies
   int math;    // 0: tcgen05 bf16, 1: tcgen05 split-tf32 (FP32-accurate), 2: FP32 SIMT
+  int cams;    // camera embeddings (FiLM after layer 2); 0 = none
 };
 struct MlpWeights {
   const float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
+  const float* embed;  // (cams, units) or null
 };
 struct MlpGrads {
   float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
+  float* embed;
 };
 size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);      // forward + backward
 size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M);  // forward only (a prefix of the above)
-// rgb = FeatureMlp(X0, viewdir). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...].
-int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
+// rgb = FeatureMlp(X0, viewdir, camera). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...],
+// its camera cams[m / rows_per_dir] (cams is read only when d.cams > 0).
+int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st);
 // Needs the preceding mlp_forward on the same workspace: its kept row-major activations
 // (layered path), or its packed bf16 weights (fused path, which recomputes the forward
 // from X0 and the view directions).
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
-                 int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st);
+                 const int32_t* cams, int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws,
+                 cudaStream_t st);
 int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
@@ -148,12 +153,16 @@ int launch_loss_f64(const tvm_param_layout& L, const tvm_model_desc& m, const fl
                     double* scratch, double* loss, cudaStream_t st);
 
 // ---- Adam (tvm_adam.cu) ----
+// blocks_per_sm caps the grid-stride grid: a full 8 when Adam has the GPU to itself,
+// fewer when it runs beside other kernels on a side stream and must leave them room.
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
-                const tvm_adam_desc& a, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st);
+                const tvm_adam_desc& a, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
+                int blocks_per_sm = 8);
 // Adam over the elements [lo, hi) of the flat buffers only (lo a segment start); the
 // learning-rate group and the shadow follow the element's place in the whole layout.
 int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
-                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st);
+                      const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
+                      int blocks_per_sm = 8);
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
 
 }  // namespace tvm

@@ -334,7 +334,7 @@ static int ld_x1(const MlpDims& d) { return (int)round_up(d.enc, 4); }
 //             dW2 = H1^T dH2, dW1 = X1^T dH1, dW0 = X0^T dH0     (split-K tc_gemm)
 // ---------------------------------------------------------------------------------
 static bool pmlp_supported(const MlpDims& d) {
-  return d.math == 1 && d.squash == pg::SQ && d.enc == pg::ENC && d.nf == 2 && d.nv == 2 && d.units == 128 &&
+  return d.math == 1 && d.cams == 0 && d.squash == pg::SQ && d.enc == pg::ENC && d.nf == 2 && d.nv == 2 && d.units == 128 &&
          d.feat % 4 == 0 && d.feat >= 4 && d.feat <= 160;
 }
 static int pmlp_nt_dx0(const MlpDims& d) { return d.feat <= 64 ? 64 : d.feat <= 144 ? 144 : 160; }
@@ -525,6 +525,74 @@ __global__ void __launch_bounds__(L3_THREADS) l3_bwd_kernel(int64_t M, const flo
   if (tid < 3) atomicAdd(gb3 + tid, sB3[tid]);
 }
 
+// FiLM camera conditioning after layer 2 (networks.py:103-111): with the row's embedding
+// e = embed[camera], units j >= U/2 become e[j - U/2] * h_j + e[j]; the lower half passes
+// through. H2f = FiLM(H2), one thread per (row, unit). Camera indices are clamped into
+// [0, cams).
+__device__ __forceinline__ int film_camera(const int32_t* cams, int64_t row, int rows_per_dir, int ncam) {
+  return min(max(__ldg(cams + row / rows_per_dir), 0), ncam - 1);
+}
+
+__global__ void film_fwd_kernel(int64_t M, int U, const float* __restrict__ H2, const float* __restrict__ emb,
+                                const int32_t* __restrict__ cams, int rows_per_dir, int ncam,
+                                float* __restrict__ H2f) {
+  const int64_t n = M * U;
+  const int half = U / 2;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = e / U;
+    const int j = (int)(e - row * U);
+    const float h = H2[e];
+    if (j < half) {
+      H2f[e] = h;
+    } else {
+      const float* c = emb + (int64_t)film_camera(cams, row, rows_per_dir, ncam) * U;
+      H2f[e] = __ldg(c + j - half) * h + __ldg(c + j);
+    }
+  }
+}
+
+// FiLM backward, in place on dH: dH2f (gradient of the conditioned units) -> dH2, the
+// gradient of layer 2's pre-activation (the ReLU mask from H2 applied), and the embedding
+// gradient d e[j - U/2] += dH2f_j * h_j, d e[j] += dH2f_j. A block walks FILM_ROWS
+// consecutive rows per unit; rows of one ray share its camera, so each thread adds its
+// sums to the embedding gradient only when the camera changes.
+constexpr int FILM_ROWS = 64;
+
+__global__ void film_bwd_kernel(int64_t M, int U, const float* __restrict__ H2, const float* __restrict__ emb,
+                                const int32_t* __restrict__ cams, int rows_per_dir, int ncam, float* __restrict__ dH,
+                                float* __restrict__ gemb) {
+  const int64_t r0 = (int64_t)blockIdx.x * FILM_ROWS;
+  const int64_t r1 = min(M, r0 + FILM_ROWS);
+  const int half = U / 2;
+  for (int j = threadIdx.x; j < U; j += blockDim.x) {
+    int cur = -1;
+    float acc_scale = 0.f, acc_shift = 0.f;
+    for (int64_t r = r0; r < r1; ++r) {
+      const float h = H2[r * U + j];
+      float g = dH[r * U + j];
+      if (j >= half) {
+        const int cam = film_camera(cams, r, rows_per_dir, ncam);
+        if (cam != cur) {
+          if (cur >= 0) {
+            atomicAdd(gemb + (int64_t)cur * U + j - half, acc_scale);
+            atomicAdd(gemb + (int64_t)cur * U + j, acc_shift);
+          }
+          cur = cam;
+          acc_scale = acc_shift = 0.f;
+        }
+        acc_scale += g * h;
+        acc_shift += g;
+        g *= __ldg(emb + (int64_t)cam * U + j - half);
+      }
+      dH[r * U + j] = h > 0.f ? g : 0.f;
+    }
+    if (cur >= 0) {
+      atomicAdd(gemb + (int64_t)cur * U + j - half, acc_scale);
+      atomicAdd(gemb + (int64_t)cur * U + j, acc_shift);
+    }
+  }
+}
+
 // Workspace carve-out shared by forward and backward. The buffers the forward writes
 // come first, so a forward-only carve is a prefix of the full one and a forward
 // followed by a backward on the same workspace sees the same addresses.
@@ -533,6 +601,7 @@ struct MlpBufs {
   uint8_t* wpack;
   uint8_t* img[6];
   uint32_t* mask1;  // ReLU bits of H1 (4 words per row), for the dH1 product
+  float* H2f;       // FiLM-conditioned H2 (models with camera embeddings)
 };
 static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws, bool fwd_only) {
   MlpBufs b{};
@@ -557,6 +626,7 @@ static MlpBufs carve(const MlpDims& d, int64_t M, Workspace& ws, bool fwd_only) 
   b.X1 = ws.take<float>(M * ld_x1(d));
   b.H1 = ws.take<float>(M * d.units);
   b.H2 = ws.take<float>(M * d.units);
+  if (d.cams > 0) b.H2f = ws.take<float>(M * d.units);
   if (fwd_only) return b;
   b.dH2 = ws.take<float>(M * d.units);
   b.dH1 = ws.take<float>(M * d.units);
@@ -577,7 +647,7 @@ size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M) {
   return ws.used + 256;
 }
 
-int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs,
+int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st) {
   MlpBufs b = carve(d, M, ws, true);
   if (!ws.ok()) {
@@ -632,12 +702,20 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
                               EpiBiasAct{b.H1, d.units, w.b1, 1}, st)));
   TVM_TRY((mm<false, false>(d.math, M, d.units, d.units, b.H1, d.units, w.w2, d.units,
                               EpiBiasAct{b.H2, d.units, w.b2, 1}, st)));
-  TVM_TRY((mm<false, false>(d.math, M, 3, d.units, b.H2, d.units, w.w3, 3, EpiBiasAct{rgb, 3, w.b3, 2}, st)));
+  const float* h2 = b.H2;
+  if (d.cams > 0) {
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(M * d.units, 256), 8 * device_sms());
+    film_fwd_kernel<<<blocks, 256, 0, st>>>(M, d.units, b.H2, w.embed, cams, rows_per_dir, d.cams, b.H2f);
+    TVM_TRY(check_launch("film_fwd"));
+    h2 = b.H2f;
+  }
+  TVM_TRY((mm<false, false>(d.math, M, 3, d.units, h2, d.units, w.w3, 3, EpiBiasAct{rgb, 3, w.b3, 2}, st)));
   return TVM_OK;
 }
 
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
-                 int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws, cudaStream_t st) {
+                 const int32_t* cams, int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws,
+                 cudaStream_t st) {
   MlpBufs b = carve(d, M, ws, false);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
@@ -691,9 +769,20 @@ int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const
     return TVM_OK;
   }
   {
-    // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3.
-    TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units}, st)));
-    TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+    // Layer 3: dH2 = (dZ3 @ W3^T) * [H2 > 0]; dW3 = H2^T dZ3; db3 = sum dZ3. With camera
+    // embeddings layer 3 reads the conditioned H2f, and the FiLM backward turns its
+    // gradient into dH2 (mask included) and the embedding gradient.
+    if (d.cams > 0) {
+      TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiStore{b.dH2, d.units}, st)));
+      TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2f, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+      film_bwd_kernel<<<(unsigned)ceil_div(M, FILM_ROWS), 128, 0, st>>>(M, d.units, b.H2, w.embed, cams, rows_per_dir,
+                                                                       d.cams, b.dH2, g.embed);
+      TVM_TRY(check_launch("film_bwd"));
+    } else {
+      TVM_TRY((mm<false, true>(d.math, M, d.units, 3, dZ3, 3, w.w3, 3, EpiReluMask{b.dH2, d.units, b.H2, d.units},
+                               st)));
+      TVM_TRY((mm<true, false>(d.math, d.units, 3, M, b.H2, d.units, dZ3, 3, EpiAtomic{g.w3, 3}, st, kc)));
+    }
     // Layer 2.
     TVM_TRY((mm<false, true>(d.math, M, d.units, d.units, b.dH2, d.units, w.w2, d.units,
                              EpiReluMask{b.dH1, d.units, b.H1, d.units}, st)));

@@ -767,7 +767,8 @@ int fused_status(int32_t* out, cudaStream_t st) {
 }
 
 bool mlp_fused_supported(const MlpDims& d) {
-  return d.math == 0 && d.feat == fmlp::F && d.squash == fmlp::SQ && d.enc == fmlp::ENC && d.units == fmlp::U;
+  return d.math == 0 && d.cams == 0 && d.feat == fmlp::F && d.squash == fmlp::SQ && d.enc == fmlp::ENC &&
+         d.units == fmlp::U;
 }
 
 size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }

@@ -13,6 +13,7 @@ from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_int64, c_siz
 PKG_DIR = pathlib.Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "libtensorf_gb300.so"
 
+ABI_VERSION = 2  # TVM_ABI_VERSION of include/tensorf_gb300.h
 TVM_OK = 0
 ERROR_NAMES = {
     -1: "TVM_ERR_INVALID",
@@ -40,7 +41,7 @@ class ModelDesc(ctypes.Structure):
     _fields_ = [("grid_dim", c_int32), ("density_channels", c_int32), ("appearance_channels", c_int32),
                 ("feature_n_freqs", c_int32), ("viewdir_n_freqs", c_int32), ("squash_dim", c_int32),
                 ("units", c_int32), ("dtype", c_int32), ("mlp_math", c_int32), ("proposal_grid", c_int32),
-                ("proposal_rank", c_int32), ("proposal_units", c_int32), ("_pad", c_int32)]
+                ("proposal_rank", c_int32), ("proposal_units", c_int32), ("num_cameras", c_int32)]
 
 
 class ParamLayout(ctypes.Structure):
@@ -51,11 +52,11 @@ class ParamLayout(ctypes.Structure):
         "mlp_begin", "total",
         "shadow_density_lines", "shadow_density_planes", "shadow_appearance_lines",
         "shadow_appearance_planes", "shadow_proposal_lines", "shadow_proposal_planes",
-        "shadow_total")] + [("encoded_dim", c_int32), ("_pad", c_int32)]
+        "shadow_total")] + [("encoded_dim", c_int32), ("_pad", c_int32), ("mlp_embed", c_int64)]
 
 
 class Rays(ctypes.Structure):
-    _fields_ = [("count", c_int64), ("origins", c_void_p), ("directions", c_void_p)]
+    _fields_ = [("count", c_int64), ("origins", c_void_p), ("directions", c_void_p), ("camera_indices", c_void_p)]
 
 
 class RenderDesc(ctypes.Structure):
@@ -69,7 +70,8 @@ class RenderDesc(ctypes.Structure):
 
 class AdamDesc(ctypes.Structure):
     _fields_ = [("lr_tensor", c_float), ("lr_mlp", c_float), ("b1", c_float), ("b2", c_float),
-                ("eps", c_float), ("lr_decay", c_float), ("count", c_int32), ("_pad", c_int32)]
+                ("eps", c_float), ("lr_decay", c_float), ("count", c_int32), ("_pad", c_int32),
+                ("grad_sq", c_void_p)]
 
 
 # name -> (restype, argtypes)
@@ -88,10 +90,10 @@ _SIGNATURES = {
     "tvm_composite_bwd": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tvm_topk_select": (c_int32, [c_void_p, c_void_p, c_int32, c_int64, c_int32, c_int32, c_void_p, c_void_p]),
     "tvm_mlp_workspace_size": (c_size_t, [POINTER(ModelDesc), c_int64]),
-    "tvm_mlp_fwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
-                              c_size_t, c_void_p]),
-    "tvm_mlp_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
-                              c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tvm_mlp_fwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                              c_void_p, c_size_t, c_void_p]),
+    "tvm_mlp_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_mlp_fwd_static_scratch": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
                                             c_void_p]),
     "tvm_loss_f64_workspace_size": (c_size_t, [POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
@@ -144,7 +146,7 @@ def load() -> ctypes.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.tvm_abi_version() != 1:
+    if lib.tvm_abi_version() != ABI_VERSION:
         raise RuntimeError("ABI version mismatch")
     _LIB = lib
     return lib

@@ -67,6 +67,7 @@ class ModelSpec:
     mlp_math: str = "tensor"  # "tensor" (tcgen05; split-tf32 in fp32 mode) or "simt" (fp32 only)
     proposal_grid: int = 0    # proposal VM grid; 0 = no proposal network
     proposal_units: int = 64
+    num_cameras: int = 0      # FeatureMlp camera embeddings (FiLM, networks.py:103-111); 0 = none
 
     def desc(self) -> _lib.ModelDesc:
         return _lib.ModelDesc(grid_dim=self.grid_dim, density_channels=self.density_feat_dim,
@@ -76,11 +77,12 @@ class ModelSpec:
                               dtype=_lib.TVM_BF16 if self.precision == "bf16" else _lib.TVM_F32,
                               mlp_math=_lib.TVM_MLP_SIMT_F32 if self.mlp_math == "simt" else _lib.TVM_MLP_DEFAULT,
                               proposal_grid=self.proposal_grid, proposal_rank=4 if self.proposal_grid else 0,
-                              proposal_units=self.proposal_units)
+                              proposal_units=self.proposal_units, num_cameras=self.num_cameras)
 
     def mlp(self) -> networks.FeatureMlp:
         return networks.FeatureMlp(feature_squash_dim=self.squash_dim, units=self.units,
-                                   feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs)
+                                   feature_n_freqs=self.feature_n_freqs, viewdir_n_freqs=self.viewdir_n_freqs,
+                                   num_cameras=self.num_cameras or None)
 
 
 def param_layout(spec: ModelSpec) -> _lib.ParamLayout:
@@ -142,6 +144,8 @@ class LearnableParams:
             "Dense_1": {"kernel": self._seg(L.mlp_w1, (enc, s.units), buf), "bias": self._seg(L.mlp_b1, (s.units,), buf)},
             "Dense_2": {"kernel": self._seg(L.mlp_w2, (s.units, s.units), buf), "bias": self._seg(L.mlp_b2, (s.units,), buf)},
             "Dense_3": {"kernel": self._seg(L.mlp_w3, (s.units, 3), buf), "bias": self._seg(L.mlp_b3, (3,), buf)},
+            **({"Embed_0": {"embedding": self._seg(L.mlp_embed, (s.num_cameras, s.units), buf)}}
+               if s.num_cameras else {}),
         }
 
     @property
@@ -371,10 +375,14 @@ def make_render_desc(config: RenderConfig, aabb, noise: RenderNoise, rays: int, 
 
 
 def rays_struct(rays: "cameras.Rays3D") -> _lib.Rays:
+    """The C view of a ray batch. Camera indices, when present, must be a contiguous
+    int32 CUDA tensor of one index per ray (the struct keeps only its address)."""
     o = rays.origins.reshape(-1, 3)
     dvec = rays.directions.reshape(-1, 3)
+    ci = rays.camera_indices
     return _lib.Rays(count=o.shape[0], origins=ptr(o, torch.float32, "origins"),
-                     directions=ptr(dvec, torch.float32, "directions"))
+                     directions=ptr(dvec, torch.float32, "directions"),
+                     camera_indices=ptr(ci, torch.int32, "camera_indices") if ci is not None else None)
 
 
 def _schedule_for(config: RenderConfig, scene_contraction: bool, schedule,

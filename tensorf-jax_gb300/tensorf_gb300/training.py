@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import dataclasses
+import math
 from typing import Optional, Tuple
 
 import numpy as onp
@@ -100,7 +101,10 @@ class TrainState:
         self.aabb = torch.tensor([config.initial_aabb_min, config.initial_aabb_max], dtype=torch.float32)
         self.prng_key = render.NoiseKey(seed)
         self.step = 0
-        self.loss = torch.zeros(1, dtype=torch.float32, device=p.device)
+        # The step's MSE and the sum of its squared gradients, written on the device and
+        # read back together when the step logs.
+        self._stats = torch.zeros(2, dtype=torch.float32, device=p.device)
+        self.loss = self._stats[0:1]
         self._ws = None
         self._ws_key = None
 
@@ -194,7 +198,8 @@ class TrainState:
     def adam_desc(self, count: int) -> _lib.AdamDesc:
         o = self.config.optimizer
         return _lib.AdamDesc(lr_tensor=o.lr_init_tensor, lr_mlp=o.lr_init_mlp, b1=0.9, b2=0.99, eps=1e-8,
-                             lr_decay=lr_decay_coeff(self.step, self.config), count=count, _pad=0)
+                             lr_decay=lr_decay_coeff(self.step, self.config), count=count, _pad=0,
+                             grad_sq=self._stats[1:].data_ptr())
 
     def training_step(self, rays: cameras.Rays3D, colors: torch.Tensor,
                       noise: Optional[render.RenderNoise] = None, log: bool = True):
@@ -222,9 +227,10 @@ class TrainState:
                   ctypes.byref(desc), ptr(self.loss), ptr(self._ws), self._ws.numel(), stream_handle())
         self.step += 1
         log_data = {}
-        if log:
-            mse = float(self.loss.item())
+        if log:  # training.py:143-196: mse, psnr, both learning rates, the gradient's global norm
+            mse, grad_sq = self._stats.tolist()
             log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
                         "train/lr_tensor": adam.lr_decay * self.config.optimizer.lr_init_tensor,
-                        "train/lr_mlp": adam.lr_decay * self.config.optimizer.lr_init_mlp}
+                        "train/lr_mlp": adam.lr_decay * self.config.optimizer.lr_init_mlp,
+                        "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
         return self, log_data

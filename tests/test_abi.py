@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.tvm_abi_version() == 1
+    assert lib.tvm_abi_version() == _lib.ABI_VERSION == 2
 
 
 def _model(**kw):
@@ -166,3 +166,17 @@ def test_static_scratch_limit_matches_workspace_size(dtype, ca):
     assert lib.tvm_mlp_fwd_static_scratch(ctypes.byref(md), None, None, None, n + 1, None, None) == -2
     assert lib.tvm_mlp_workspace_size(ctypes.byref(md), n) > (32 << 20)
     assert 0 < n
+
+
+def test_param_layout_camera_embeddings():
+    """FeatureMlp camera embeddings (networks.py:103-111): a (num_cameras, units) segment
+    inside the MLP learning-rate group; none without cameras; odd units rejected."""
+    lay = _lib.ParamLayout()
+    _lib.call("tvm_get_param_layout", ctypes.byref(_model(num_cameras=5)), ctypes.byref(lay))
+    assert lay.mlp_embed >= lay.mlp_b3 + 3 and lay.mlp_embed >= lay.mlp_begin and lay.mlp_embed % 64 == 0
+    assert lay.total >= lay.mlp_embed + 5 * 128
+    plain = _lib.ParamLayout()
+    _lib.call("tvm_get_param_layout", ctypes.byref(_model()), ctypes.byref(plain))
+    assert plain.mlp_embed == 0 and lay.total == plain.total + 5 * 128
+    st = _lib.load().tvm_get_param_layout(ctypes.byref(_model(num_cameras=5, units=127)), ctypes.byref(lay))
+    assert st == -2

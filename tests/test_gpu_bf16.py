@@ -155,7 +155,7 @@ def test_fused_bf16_mlp_backward_matches_mirror(n):
     f_c, d_c, g_c = feats.cuda().contiguous(), dirs.cuda().contiguous(), grad_rgb.cuda().contiguous()
     gfeat = torch.empty_like(f_c)
     grads = torch.zeros_like(lp.params)
-    _lib.call("tvm_mlp_bwd", ctypes.byref(md), ptr(lp.params), ptr(f_c), ptr(d_c), n, ptr(g_c), ptr(gfeat),
+    _lib.call("tvm_mlp_bwd", ctypes.byref(md), ptr(lp.params), ptr(f_c), ptr(d_c), None, n, ptr(g_c), ptr(gfeat),
               ptr(grads), ptr(ws), ws.numel(), stream_handle())
     st = ctypes.c_int32(-1)
     _lib.call("tvm_device_status", ctypes.byref(st), None)

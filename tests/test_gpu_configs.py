@@ -238,6 +238,8 @@ def test_train_step_five_updates_follow_adam_on_device_gradients():
         decay = O.lr_decay_coeff(step, cfg.n_iters, cfg.upsamp_iters)
         assert log["train/lr_tensor"] == pytest.approx(0.02 * decay, rel=1e-6)
         assert log["train/lr_mlp"] == pytest.approx(1e-3 * decay, rel=1e-6)
+        # optax.global_norm of the step's gradient (training.py:190-196)
+        assert log["train/grad_norm"] == pytest.approx(float(g.norm()), rel=1e-4)
         pt, mt, vt = O.adam_update(p0[:lay.mlp_begin], g[:lay.mlp_begin], mu64[:lay.mlp_begin], nu64[:lay.mlp_begin],
                                    step + 1, lr=0.02, lr_decay=decay)
         pm, mm, vm = O.adam_update(p0[lay.mlp_begin:], g[lay.mlp_begin:], mu64[lay.mlp_begin:], nu64[lay.mlp_begin:],

@@ -81,12 +81,12 @@ def _run(lp, feats, dirs, grad_rgb, out_offset=False):
     n = feats.shape[0]
     ws = torch.empty(max(1, lib.tvm_mlp_workspace_size(ctypes.byref(md), n)), dtype=torch.uint8, device="cuda")
     rgb = torch.empty((n, 3), dtype=torch.float32, device="cuda")
-    _lib.call("tvm_mlp_fwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(rgb), ptr(ws),
+    _lib.call("tvm_mlp_fwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), None, n, ptr(rgb), ptr(ws),
               ws.numel(), stream_handle())
     feat = feats.shape[1]
     gfeat = _offset(torch.zeros((n, feat))) if out_offset else torch.zeros((n, feat), device="cuda")
     grads = torch.zeros_like(lp.params)
-    _lib.call("tvm_mlp_bwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(grad_rgb), ptr(gfeat),
+    _lib.call("tvm_mlp_bwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), None, n, ptr(grad_rgb), ptr(gfeat),
               ptr(grads), ptr(ws), ws.numel(), stream_handle())
     st = ctypes.c_int32(-1)
     _lib.call("tvm_device_status", ctypes.byref(st), None)

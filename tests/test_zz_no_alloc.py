@@ -61,7 +61,7 @@ def _with_workspace(lp, feats, dirs):
     n = feats.shape[0]
     ws = torch.empty(_lib.load().tvm_mlp_workspace_size(ctypes.byref(md), n), dtype=torch.uint8, device="cuda")
     rgb = torch.empty((n, 3), dtype=torch.float32, device="cuda")
-    _lib.call("tvm_mlp_fwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), n, ptr(rgb), ptr(ws),
+    _lib.call("tvm_mlp_fwd", ctypes.byref(md), ptr(lp.params), ptr(feats), ptr(dirs), None, n, ptr(rgb), ptr(ws),
               ws.numel(), stream_handle())
     return rgb
 
