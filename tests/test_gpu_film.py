@@ -95,7 +95,11 @@ def test_film_render_and_gradients_match_oracle():
     jit = torch.tensor(rng.uniform(size=N), dtype=torch.float32)
     gum = torch.tensor(-np.log(-np.log(rng.uniform(1e-7, 1, size=N))), dtype=torch.float32)
     aabb = torch.tensor([[-1.5] * 3, [1.5] * 3])
-    keep, _, _ = TC._keep_rays(TC._to64(ref), aabb.double(), o.double(), d.double(), N, k, jit.double(), gum.double(), shift)
+    # Near-ties depend on the density only and the ReLU kinks lie before the FiLM step,
+    # so the filter runs the model without the embedding.
+    plain = dict(ref, mlp={n: v for n, v in ref["mlp"].items() if n != "Embed_0"})
+    keep, _, _ = TC._keep_rays(TC._to64(plain), aabb.double(), o.double(), d.double(), N, k, jit.double(),
+                               gum.double(), shift)
     assert float(keep.float().mean()) > 0.8
     o, d, c, cams = o[keep].contiguous(), d[keep].contiguous(), c[keep].contiguous(), cams[keep].contiguous()
 

@@ -279,7 +279,7 @@ def test_loss_and_grad_matches_oracle_autograd(tg):
         for nm in ref64["mlp"][layer]:
             pairs.append((g["mlp"][layer][nm], ref64["mlp"][layer][nm].grad))
     for got, want in pairs:
-        assert _rel_err(got, want) < 2e-4, (_rel_err(got, want))
+        assert _rel_err(got, want) < RTOL, (_rel_err(got, want))
 
 
 def test_train_step_adam_update(tg):

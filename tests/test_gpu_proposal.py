@@ -127,7 +127,7 @@ def test_proposal_gradients_match_oracle():
     for nm in ("vector", "matrix", "w1", "b1", "w2", "b2"):
         pairs.append((g["proposal"][nm], ref64["proposal"][nm].grad))
     errs = [_rel(got, want) for got, want in pairs]
-    assert max(errs) < 2e-4, errs
+    assert max(errs) < RTOL, errs
 
 
 def _psnr(a, b):
