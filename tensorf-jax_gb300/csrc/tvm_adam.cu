@@ -6,6 +6,9 @@
 // decay multiplier and apply_updates. One pass streams param, grad, mu, nu (4 reads,
 // 3 writes + the zeroed grad): 32 B per parameter, HBM-bound, plus 2 B for the bf16
 // shadow of the field segments in BF16 mode. float4 lanes, grid sized to the 152 SMs.
+// Every value is touched once per step, so loads and stores carry the evict-first
+// (streaming) cache hint: in a training step Adam runs beside the density scatter, whose
+// field must stay in L2, and its half gigabyte would otherwise push that field out.
 #include <algorithm>
 
 #include "tvm_internal.h"
@@ -39,25 +42,25 @@ __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float*
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   float sq = 0.f;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += stride) {
-    float4 pp = reinterpret_cast<float4*>(p)[q];
-    const float4 gg = reinterpret_cast<float4*>(g)[q];
+    float4 pp = __ldcs(reinterpret_cast<const float4*>(p) + q);
+    const float4 gg = __ldcs(reinterpret_cast<const float4*>(g) + q);
     sq += (gg.x * gg.x + gg.y * gg.y) + (gg.z * gg.z + gg.w * gg.w);
-    float4 mm = reinterpret_cast<float4*>(m)[q];
-    float4 vv = reinterpret_cast<float4*>(v)[q];
+    float4 mm = __ldcs(reinterpret_cast<const float4*>(m) + q);
+    float4 vv = __ldcs(reinterpret_cast<const float4*>(v) + q);
     const int64_t e = q * 4;
     const float lr = (e < mlp_begin) ? a.lr_t : a.lr_m;  // mlp_begin is a multiple of 64
     pp.x = adam_one(pp.x, gg.x, mm.x, vv.x, lr, a);
     pp.y = adam_one(pp.y, gg.y, mm.y, vv.y, lr, a);
     pp.z = adam_one(pp.z, gg.z, mm.z, vv.z, lr, a);
     pp.w = adam_one(pp.w, gg.w, mm.w, vv.w, lr, a);
-    reinterpret_cast<float4*>(p)[q] = pp;
-    reinterpret_cast<float4*>(m)[q] = mm;
-    reinterpret_cast<float4*>(v)[q] = vv;
-    reinterpret_cast<float4*>(g)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __stcs(reinterpret_cast<float4*>(p) + q, pp);
+    __stcs(reinterpret_cast<float4*>(m) + q, mm);
+    __stcs(reinterpret_cast<float4*>(v) + q, vv);
+    __stcs(reinterpret_cast<float4*>(g) + q, make_float4(0.f, 0.f, 0.f, 0.f));
     if (shadow != nullptr && e < shadow_n) {
       __nv_bfloat162 lo = __floats2bfloat162_rn(pp.x, pp.y), hi = __floats2bfloat162_rn(pp.z, pp.w);
-      reinterpret_cast<uint2*>(shadow)[q] =
-          make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi));
+      __stcs(reinterpret_cast<uint2*>(shadow) + q,
+             make_uint2(*reinterpret_cast<uint32_t*>(&lo), *reinterpret_cast<uint32_t*>(&hi)));
     }
   }
   for (int64_t e = n4 * 4 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += stride) {

@@ -497,15 +497,12 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
-  phase_mark(8, st);
-  TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
-                               b.gsum, st));
   if (adam) {
     // The appearance field's and the FeatureMlp's gradients are final here, and nothing
     // later in the pass reads those parameters: update them on the second side stream
-    // while the main stream runs the density scatter. Adam is HBM-bound and the scatter
-    // L2-bound, so they share the GPU well; the short, memory-latency-bound compositing
-    // backward before it would only be starved.
+    // while the main stream runs the compositing and density backward. Adam is
+    // HBM-bound and streams with evict-first hints, so the density field those kernels
+    // gather from stays in L2.
     if (side == nullptr) TVM_TRY(side_stream(side));
     cudaError_t e = cudaEventRecord(side->fork2, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream2, side->fork2, 0);
@@ -516,6 +513,9 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam join record: %s", cudaGetErrorString(e));
     adam_forked = true;
   }
+  phase_mark(8, st);
+  TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
+                               b.gsum, st));
   phase_mark(9, st);
   TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
                              rays.directions, R, s, b.gsum, st));
