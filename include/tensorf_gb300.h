@@ -76,7 +76,7 @@ extern "C" {
 /* One VM-decomposed tensor (TensorVM, tensor_vm.py:14-40). */
 typedef struct {
   int32_t grid_dim; /* G */
-  int32_t channels; /* C per vector-matrix pair; multiple of 4 */
+  int32_t channels; /* C per vector-matrix pair: 8, 16, 24, 32 or 48 */
   int32_t dtype;    /* TVM_F32 / TVM_BF16 / TVM_F64 */
   int32_t _pad;
   const void* lines;  /* [3][G][C] */

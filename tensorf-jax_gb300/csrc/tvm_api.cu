@@ -76,16 +76,14 @@ int ensure_smem_limit(const void* fn, int bytes, const char* what) {
   return TVM_OK;
 }
 
-// Two more streams per calling thread and device, each with a fork and a join event,
-// both at the lowest priority (the main stream holds the longer chain):
-//  - `stream`: the proposal network's backward, which depends only on the forward's
-//    proposal and main-field weights, runs there concurrently with the main field's
-//    latency-bound backward kernels;
-//  - `stream2`: in a training step, Adam over the appearance field and the FeatureMlp
-//    (HBM-bound) runs there as soon as their gradients are final, concurrently with the
-//    density scatter (L2-bound).
+// Two more streams per calling thread and device, each with a fork and a join event:
+//  - `stream` (lowest priority): the proposal network's backward and update, which
+//    depend only on the forward, run there beside the main field's backward;
+//  - `branch` (highest priority): the appearance branch of the backward (FeatureMlp
+//    backward, appearance scatter, their update), the longer of the two chains that
+//    follow the loss, runs there while the caller's stream runs the density branch.
 struct SideStream {
-  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaStream_t stream = nullptr, branch = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
 };
 
@@ -98,7 +96,7 @@ static int side_stream(SideStream*& out) {
     int least = 0, greatest = 0;
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, least);
-    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream2, cudaStreamNonBlocking, least);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.branch, cudaStreamNonBlocking, greatest);
     for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2})
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "side stream: %s", cudaGetErrorString(e));
@@ -117,16 +115,16 @@ static int encoded_dim(const tvm_model_desc& m) {
   return m.squash_dim + 3 + 2 * m.feature_n_freqs * m.squash_dim + 2 * m.viewdir_n_freqs * 3;
 }
 
-static bool channels_ok(int c) { return c == 8 || c == 16 || c == 24 || c == 48; }
+static bool channels_ok(int c) { return c == 8 || c == 16 || c == 24 || c == 32 || c == 48; }
 
 static int validate_model(const tvm_model_desc* m) {
   TVM_REQUIRE(m != nullptr, TVM_ERR_INVALID, "model descriptor is NULL");
   TVM_REQUIRE(m->grid_dim >= 2 && m->grid_dim <= 4096, TVM_ERR_SHAPE, "grid_dim=%d outside [2, 4096]",
               m->grid_dim);
   TVM_REQUIRE(channels_ok(m->density_channels), TVM_ERR_UNSUPPORTED,
-              "density_channels=%d not compiled (8, 16, 24, 48)", m->density_channels);
+              "density_channels=%d not compiled (8, 16, 24, 32, 48)", m->density_channels);
   TVM_REQUIRE(channels_ok(m->appearance_channels), TVM_ERR_UNSUPPORTED,
-              "appearance_channels=%d not compiled (8, 16, 24, 48)", m->appearance_channels);
+              "appearance_channels=%d not compiled (8, 16, 24, 32, 48)", m->appearance_channels);
   TVM_REQUIRE(m->feature_n_freqs >= 0 && m->feature_n_freqs <= 16 && m->viewdir_n_freqs >= 0 &&
                   m->viewdir_n_freqs <= 16,
               TVM_ERR_SHAPE, "fourier frequencies must be in [0, 16]");
@@ -438,42 +436,60 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_composite_select(b.sigma, rays.origins, rays.directions, R, s, c.mode, k, c.gumbel,
                                   c.gumbel_per_ray, b.sel, b.w_sel, b.p_last, b.q_last, b.wsum, nullptr,
                                   (proposal && backward) ? b.w_dense : nullptr, st));
+  // With phase events set, the whole pass runs on the caller's stream in phase order, so
+  // each phase is the span of its own kernels. Otherwise work that depends on neither
+  // branch of the main chain runs beside it on side streams.
+  const bool overlap = g_n_events == 0;
   SideStream* side = nullptr;
-  bool prop_forked = false, adam_forked = false;
-  // Segments of the flat layout updated by Adam at different points of the pass.
-  const bool has_prop = m.proposal_grid > 0;
-  // Updates on a side stream run beside the main stream's kernels: a persistent grid of
-  // two blocks per SM keeps HBM busy and leaves the SMs room for them.
+  if (overlap && backward) TVM_TRY(side_stream(side));
+  auto fork_to = [&](cudaStream_t to, cudaEvent_t ev) {
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(to, ev, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "stream fork: %s", cudaGetErrorString(e));
+    return TVM_OK;
+  };
+  auto branch_done = [&](cudaStream_t from, cudaEvent_t ev) {
+    cudaError_t e = cudaEventRecord(ev, from);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "stream join: %s", cudaGetErrorString(e));
+    return TVM_OK;
+  };
+  auto join = [&](cudaEvent_t ev) {
+    cudaError_t e = cudaStreamWaitEvent(st, ev, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "stream join: %s", cudaGetErrorString(e));
+    return TVM_OK;
+  };
+  // Updates beside other kernels use a grid of two blocks per SM: enough to keep HBM busy,
+  // and it leaves the SMs to the kernels they run beside.
   auto adam_seg = [&](int64_t lo, int64_t hi, cudaStream_t s_) {
     return launch_adam_range(adam->params, grads, adam->mu, adam->nu, lo, hi, L.mlp_begin, adam->desc, adam->shadow,
                              adam->shadow_n, s_, s_ == st ? 8 : 2);
   };
-  if (proposal && backward) {
-    // Proposal bound loss on the main weights, then the proposal network backward, on the
-    // side stream: they need only the forward's outputs and write only the proposal's
-    // own gradient segments.
-    TVM_TRY(side_stream(side));
-    cudaStream_t aux = side->stream;
-    cudaError_t e = cudaEventRecord(side->fork, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(aux, side->fork, 0);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), aux);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal fork: %s", cudaGetErrorString(e));
+  const bool has_prop = m.proposal_grid > 0;
+  // Proposal bound loss on the main weights, then the proposal network's backward and its
+  // update: they need only the forward's outputs and touch only the proposal's segments.
+  auto proposal_backward = [&](cudaStream_t s_) {
+    cudaError_t e = cudaMemsetAsync(b.loss_p, 0, sizeof(float), s_);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal loss: %s", cudaGetErrorString(e));
     TVM_TRY(launch_prop_loss(b.w_dense, b.w_p, b.bins, R, c.proposal_samples, c.density_samples,
-                             c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, aux));
-    TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, aux));
+                             c.proposal_loss_weight / (float)R, b.loss_p, b.g_wp, s_));
+    TVM_TRY(launch_segment_bwd_sum(b.sig_p, b.delta_p, R, c.proposal_samples, b.g_wp, b.dz_p, s_));
     const FieldView fp = proposal_field(m, L, params, shadow);
     const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
                      params + L.proposal_b2, c.proposal_shift, nullptr, nullptr};
     TVM_TRY(launch_prop_bwd(fp, grads + L.proposal_lines, grads + L.proposal_planes, rays.origins, rays.directions,
                             R, sp, edges, c.proposal_jitter, b.dz_p, pm, grads + L.proposal_w1,
-                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, aux));
-    if (adam) {  // the proposal's own parameters: fields, then its MLP
-      TVM_TRY(adam_seg(L.proposal_lines, L.mlp_begin, aux));
-      TVM_TRY(adam_seg(L.proposal_w1, L.total, aux));
+                            grads + L.proposal_b1, grads + L.proposal_w2, grads + L.proposal_b2, s_));
+    if (adam && overlap) {  // the proposal's own parameters: fields, then its MLP
+      TVM_TRY(adam_seg(L.proposal_lines, L.mlp_begin, s_));
+      TVM_TRY(adam_seg(L.proposal_w1, L.total, s_));
     }
-    prop_forked = true;
-    e = cudaEventRecord(side->join, aux);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal join record: %s", cudaGetErrorString(e));
+    return TVM_OK;
+  };
+  const bool prop_forked = overlap && proposal && backward;
+  if (prop_forked) {
+    TVM_TRY(fork_to(side->stream, side->fork));
+    TVM_TRY(proposal_backward(side->stream));
+    TVM_TRY(branch_done(side->stream, side->join));
   }
   phase_mark(3, st);
   TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
@@ -491,27 +507,29 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, colors, out, loss, b.dZ3, b.gw,
                             b.gP, st));
   phase_mark(6, st);
+  // Two independent branches follow the loss. The appearance branch (FeatureMlp backward,
+  // appearance scatter, then the update of both) reads the rgb gradient dZ3; the density
+  // branch (compositing backward, density scatter, then the density field's update)
+  // reads the weight gradients gw / gP. They write disjoint gradient segments and
+  // workspace buffers, so the appearance branch, the longer one, runs on a high-priority
+  // side stream while the density branch runs on the caller's stream.
+  cudaStream_t ab = st;
+  if (overlap) {
+    TVM_TRY(fork_to(side->branch, side->fork2));
+    ab = side->branch;
+  }
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
   TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, rays.camera_indices, k, R * k, b.dZ3,
-                       b.dX0, ws2, st));
+                       b.dX0, ws2, ab));
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
-                                rays.origins, rays.directions, R, s, b.sel, k, b.dX0, st));
-  if (adam) {
-    // The appearance field's and the FeatureMlp's gradients are final here, and nothing
-    // later in the pass reads those parameters: update them on the second side stream
-    // while the main stream runs the compositing and density backward. Adam is
-    // HBM-bound and streams with evict-first hints, so the density field those kernels
-    // gather from stays in L2.
-    if (side == nullptr) TVM_TRY(side_stream(side));
-    cudaError_t e = cudaEventRecord(side->fork2, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(side->stream2, side->fork2, 0);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam fork: %s", cudaGetErrorString(e));
-    TVM_TRY(adam_seg(L.appearance_lines, has_prop ? L.proposal_lines : L.mlp_begin, side->stream2));
-    TVM_TRY(adam_seg(L.mlp_begin, has_prop ? L.proposal_w1 : L.total, side->stream2));
-    e = cudaEventRecord(side->join2, side->stream2);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam join record: %s", cudaGetErrorString(e));
-    adam_forked = true;
+                                rays.origins, rays.directions, R, s, b.sel, k, b.dX0, ab));
+  if (overlap) {
+    if (adam) {
+      TVM_TRY(adam_seg(L.appearance_lines, has_prop ? L.proposal_lines : L.mlp_begin, ab));
+      TVM_TRY(adam_seg(L.mlp_begin, has_prop ? L.proposal_w1 : L.total, ab));
+    }
+    TVM_TRY(branch_done(ab, side->join2));
   }
   phase_mark(8, st);
   TVM_TRY(launch_composite_bwd(b.sigma, rays.origins, rays.directions, R, s, k, b.sel, b.gw, b.gP,
@@ -520,17 +538,17 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   TVM_TRY(launch_density_bwd(fd, grads + L.density_lines, grads + L.density_planes, rays.origins,
                              rays.directions, R, s, b.gsum, st));
   phase_mark(10, st);
-  if (prop_forked) {  // join: the proposal backward (and its Adam) on the side stream is done
-    cudaError_t e = cudaStreamWaitEvent(st, side->join, 0);
-    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "proposal join: %s", cudaGetErrorString(e));
-  }
+  if (proposal && !overlap) TVM_TRY(proposal_backward(st));
   phase_mark(11, st);
   if (adam) {
-    TVM_TRY(adam_seg(L.density_lines, L.appearance_lines, st));  // the density field, last to be final
-    if (adam_forked) {
-      cudaError_t e = cudaStreamWaitEvent(st, side->join2, 0);
-      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "Adam join: %s", cudaGetErrorString(e));
-    }
+    if (overlap)  // the density field
+      TVM_TRY(adam_seg(L.density_lines, L.appearance_lines, st));
+    else
+      TVM_TRY(adam_seg(0, L.total, st));
+  }
+  if (overlap) {  // the caller's stream resumes once both side streams are done
+    TVM_TRY(join(side->join2));
+    if (prop_forked) TVM_TRY(join(side->join));
   }
   return TVM_OK;
 }
@@ -583,7 +601,7 @@ static int validate_field(const tvm_vm_field* f) {
   TVM_REQUIRE(f != nullptr, TVM_ERR_INVALID, "field is NULL");
   TVM_REQUIRE(f->grid_dim >= 2 && f->grid_dim <= 4096, TVM_ERR_SHAPE, "grid_dim=%d outside [2, 4096]",
               f->grid_dim);
-  TVM_REQUIRE(channels_ok(f->channels), TVM_ERR_UNSUPPORTED, "channels=%d not compiled (8, 16, 24, 48)",
+  TVM_REQUIRE(channels_ok(f->channels), TVM_ERR_UNSUPPORTED, "channels=%d not compiled (8, 16, 24, 32, 48)",
               f->channels);
   TVM_REQUIRE(f->dtype == TVM_F32 || f->dtype == TVM_BF16, TVM_ERR_DTYPE, "field dtype %d", f->dtype);
   TVM_REQUIRE(f->lines && f->planes, TVM_ERR_INVALID, "field lines/planes NULL");

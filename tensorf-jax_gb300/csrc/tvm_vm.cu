@@ -350,114 +350,6 @@ __global__ void __launch_bounds__(256, 3) density_bwd2_kernel(const T* __restric
 }
 
 // ---------------------------------------------------------------------------------
-// Density scatter along runs of consecutive samples. A quad walks RUN consecutive
-// samples of one ray (lane q owning channels [q*C/4, (q+1)*C/4), as everywhere here)
-// and keeps, per pair, the last sample's six tap texels with their running sums in
-// registers. A new sample's tap that lands on a kept texel is added to its sum; a kept
-// texel that no tap of the new sample lands on is left behind for good (along a straight
-// ray every tap index is monotone, so the run never returns to it) and gets its one
-// 16-byte reduction then. Each texel the run passes through is therefore reduced once,
-// also when it moves between tap slots (the upper line tap of one sample is the lower
-// one of the next).
-// ---------------------------------------------------------------------------------
-template <int K, int CPL>
-__device__ __forceinline__ void run_merge(int (&oidx)[K], float (&oval)[K][CPL], const int (&nidx)[K],
-                                          float (&nval)[K][CPL], float* __restrict__ base, int C) {
-#pragma unroll
-  for (int j = 0; j < K; ++j) {
-    if (oidx[j] < 0) continue;
-    bool used = false;
-#pragma unroll
-    for (int q = 0; q < K; ++q) {
-      if (!used && nidx[q] == oidx[j]) {
-#pragma unroll
-        for (int c = 0; c < CPL; ++c) nval[q][c] += oval[j][c];
-        used = true;
-      }
-    }
-    if (!used) red_chunk<CPL>(base + (int64_t)oidx[j] * C, oval[j]);
-  }
-#pragma unroll
-  for (int j = 0; j < K; ++j) {
-    oidx[j] = nidx[j];
-#pragma unroll
-    for (int c = 0; c < CPL; ++c) oval[j][c] = nval[j][c];
-  }
-}
-
-template <int K, int CPL>
-__device__ __forceinline__ void run_flush(const int (&oidx)[K], const float (&oval)[K][CPL], float* __restrict__ base,
-                                          int C) {
-#pragma unroll
-  for (int j = 0; j < K; ++j)
-    if (oidx[j] >= 0) red_chunk<CPL>(base + (int64_t)oidx[j] * C, oval[j]);
-}
-
-template <typename T, int C, int RUN>
-__global__ void __launch_bounds__(256) density_bwd_run_kernel(const T* __restrict__ lines,
-                                                             const T* __restrict__ planes, int G,
-                                                             float* __restrict__ glines,
-                                                             float* __restrict__ gplanes,
-                                                             const float* __restrict__ origins,
-                                                             const float* __restrict__ dirs,
-                                                             int64_t total, SamplerArgs s,
-                                                             const float* __restrict__ gsum) {
-  constexpr int CPL = C / 4;
-  const int64_t s0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2) * RUN;
-  const int sub = threadIdx.x & 3;
-  if (s0 >= total) return;
-  const int64_t r = s0 / s.N;  // RUN divides N: the run stays on one ray
-  const int i0 = (int)(s0 - r * s.N);
-  float gs[RUN];
-  bool any = false;
-#pragma unroll
-  for (int j = 0; j < RUN; ++j) {
-    gs[j] = __ldg(gsum + s0 + j);
-    any |= gs[j] != 0.0f;
-  }
-  if (!any) return;  // the whole quad agrees: nothing to scatter
-  const RayGeom g = load_ray(origins, dirs, r, s);
-#pragma unroll 1
-  for (int m = 0; m < 3; ++m) {
-    int a, b, c;
-    mode_perm(m, a, b, c);
-    float* lb = glines + (int64_t)m * G * C + sub * CPL;
-    float* pb = gplanes + (int64_t)m * G * G * C + sub * CPL;
-    int lidx[2] = {-1, -1}, pidx[4] = {-1, -1, -1, -1};
-    float lval[2][CPL], pval[4][CPL];
-#pragma unroll
-    for (int j = 0; j < RUN; ++j) {
-      if (gs[j] == 0.0f) continue;  // no contribution; the kept sums wait for the next one
-      float t, delta, x[3];
-      sample_t(g, s, r, i0 + j, t, delta);
-      sample_point(g, s, t, x);
-      PairEval<T, CPL> e;
-      vm_pair_eval<T, CPL>(lines, planes, G, C, m, grid_coord(x[a], G), grid_coord(x[b], G), grid_coord(x[c], G),
-                           sub * CPL, e);
-      const int nl[2] = {e.tl.i0, e.tl.i1};
-      float nlv[2][CPL];
-#pragma unroll
-      for (int q = 0; q < CPL; ++q) {
-        nlv[0][q] = gs[j] * e.P[q] * e.tl.w0;
-        nlv[1][q] = gs[j] * e.P[q] * e.tl.w1;
-      }
-      run_merge<2, CPL>(lidx, lval, nl, nlv, lb, C);
-      const int np[4] = {e.tr.i0 * G + e.tc.i0, e.tr.i0 * G + e.tc.i1, e.tr.i1 * G + e.tc.i0, e.tr.i1 * G + e.tc.i1};
-      const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
-      float npv[4][CPL];
-#pragma unroll
-      for (int k4 = 0; k4 < 4; ++k4) {
-#pragma unroll
-        for (int q = 0; q < CPL; ++q) npv[k4][q] = gs[j] * e.L[q] * w[k4];
-      }
-      run_merge<4, CPL>(pidx, pval, np, npv, pb, C);
-    }
-    run_flush<2, CPL>(lidx, lval, lb, C);
-    run_flush<4, CPL>(pidx, pval, pb, C);
-  }
-}
-
-// ---------------------------------------------------------------------------------
 // Fused appearance gather for the selected samples (render.py:472-486): row
 // m = r*k + j uses sample sel_idx[m] of ray r; X0[m] = 3C features, mode-major.
 // ---------------------------------------------------------------------------------
@@ -662,9 +554,10 @@ __global__ void to_channel_first_kernel(int G, int C, const float* __restrict__ 
     case 8: { constexpr int CC = 8; __VA_ARGS__; break; }                         \
     case 16: { constexpr int CC = 16; __VA_ARGS__; break; }                       \
     case 24: { constexpr int CC = 24; __VA_ARGS__; break; }                       \
+    case 32: { constexpr int CC = 32; __VA_ARGS__; break; }                       \
     case 48: { constexpr int CC = 48; __VA_ARGS__; break; }                       \
     default:                                                                      \
-      set_error("channels=%d not compiled (supported: 8, 16, 24, 48)", (int)(C_)); \
+      set_error("channels=%d not compiled (supported: 8, 16, 24, 32, 48)", (int)(C_)); \
       return TVM_ERR_UNSUPPORTED;                                                 \
   }
 
@@ -717,8 +610,6 @@ int launch_density_fwd(const FieldView& f, float shift, const float* origins, co
 // rays (512 uniform samples, 64 selected); with few samples per ray the single-sample
 // kernels keep more warps resident, which matters more.
 constexpr int kPairScatterMinSamples = 128;
-// Samples per run of density_bwd_run_kernel (when it divides the samples per ray).
-constexpr int kDensityRun = 8;
 constexpr int kPairScatterMinSelected = 32;
 
 int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
@@ -726,11 +617,7 @@ int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const 
                        cudaStream_t st) {
   const int64_t total = R * s.N;
   if (total == 0) return TVM_OK;
-  if (s.N % kDensityRun == 0 && f.C <= 24) {  // wider fields would not keep their sums in registers
-    TVM_DISPATCH_FIELD(f, (density_bwd_run_kernel<TT, CC, kDensityRun>
-                           <<<quad_blocks(total / kDensityRun), 256, 0, st>>>(L_, P_, f.G, glines, gplanes, origins,
-                                                                              dirs, total, s, gsum)));
-  } else if (s.N >= kPairScatterMinSamples) {
+  if (s.N >= kPairScatterMinSamples) {
     TVM_DISPATCH_FIELD(f, (density_bwd2_kernel<TT, CC><<<quad_blocks((total + 1) / 2), 256, 0, st>>>(
                                L_, P_, f.G, glines, gplanes, origins, dirs, total, s, gsum)));
   } else {

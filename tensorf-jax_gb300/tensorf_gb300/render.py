@@ -435,10 +435,14 @@ def render_rays_batched(appearance_mlp: networks.FeatureMlp, learnable_params: L
     batch_axes = rays_wrt_world.origins.shape[:-1]
     o = rays_wrt_world.origins.reshape(-1, 3).to("cuda", torch.float32)
     d = rays_wrt_world.directions.reshape(-1, 3).to("cuda", torch.float32)
+    ci = rays_wrt_world.camera_indices
+    if ci is not None:
+        ci = ci.reshape(-1).to("cuda", torch.int32).contiguous()
     total = o.shape[0]
     outs = []
     for start in range(0, total, batch_size):
-        chunk = cameras.Rays3D(origins=o[start:start + batch_size], directions=d[start:start + batch_size])
+        chunk = cameras.Rays3D(origins=o[start:start + batch_size], directions=d[start:start + batch_size],
+                               camera_indices=ci[start:start + batch_size] if ci is not None else None)
         outs.append(render_rays(appearance_mlp, learnable_params, aabb, chunk, prng_key, config,
                                 density_shift=density_shift, schedule=schedule, proposal=proposal))
     out = torch.cat(outs, dim=0)

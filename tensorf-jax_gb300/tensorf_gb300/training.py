@@ -54,6 +54,23 @@ class TrainConfig:
     proposal: Optional["render.ProposalConfig"] = None  # proposal-guided sampling
 
 
+def nerfstudio_preset(num_cameras: int) -> Tuple[TrainConfig, "render.ModelSpec"]:
+    """The defaults real scenes in the nerfstudio format train with (train_nerfstudio.py:23-44):
+    scene contraction, 2048 rays per step for 30000 steps, three times the sample-count
+    heuristic, near / far 0.05 / 200, a 32-component density field and a 48-component
+    appearance field grown from 128^3 to 300^3 at steps 2500, 5000 and 10000, six Fourier
+    frequencies for features and view directions, and camera embeddings (FiLM, one row per
+    training camera). Returns the training configuration and the model at its initial
+    grid."""
+    cfg = TrainConfig(minibatch_size=2048, n_iters=30000, initial_aabb_min=(-2.0, -2.0, -2.0),
+                      initial_aabb_max=(2.0, 2.0, 2.0), upsamp_iters=(2_500, 5_000, 10_000), grid_dim_init=128,
+                      grid_dim_final=300, scene_contraction=True, render_near=0.05, render_far=200.0,
+                      train_ray_sample_multiplier=3.0)
+    spec = render.ModelSpec(grid_dim=cfg.grid_dim_init, density_feat_dim=32, appearance_feat_dim=48,
+                            feature_n_freqs=6, viewdir_n_freqs=6, num_cameras=int(num_cameras))
+    return cfg, spec
+
+
 def lr_decay_coeff(step: int, cfg: TrainConfig) -> float:
     """training.py:158-181 (optax.exponential_decay with end_value)."""
     o = cfg.optimizer

@@ -180,3 +180,22 @@ def test_param_layout_camera_embeddings():
     assert plain.mlp_embed == 0 and lay.total == plain.total + 5 * 128
     st = _lib.load().tvm_get_param_layout(ctypes.byref(_model(num_cameras=5, units=127)), ctypes.byref(lay))
     assert st == -2
+
+
+def test_nerfstudio_preset_matches_reference_defaults():
+    """train_nerfstudio.py:23-44: contraction, 32 / 48 components, 6 / 6 frequencies,
+    camera embeddings, 128^3 -> 300^3, 2048 rays, three times the sample heuristic; its
+    model descriptor lays out."""
+    from tensorf_gb300 import render, training
+    cfg, spec = training.nerfstudio_preset(5)
+    assert (spec.density_feat_dim, spec.appearance_feat_dim) == (32, 48)
+    assert (spec.feature_n_freqs, spec.viewdir_n_freqs, spec.num_cameras) == (6, 6, 5)
+    assert cfg.scene_contraction and cfg.minibatch_size == 2048 and cfg.train_ray_sample_multiplier == 3.0
+    assert (cfg.initial_aabb_min, cfg.initial_aabb_max) == ((-2.0,) * 3, (2.0,) * 3)
+    assert (cfg.render_near, cfg.render_far) == (0.05, 200.0)
+    assert (cfg.grid_dim_init, cfg.grid_dim_final, cfg.upsamp_iters) == (128, 300, (2500, 5000, 10000))
+    assert training.sample_counts(cfg.grid_dim_init, cfg) == (665, 99)
+    lay = render.param_layout(spec)
+    G = spec.grid_dim
+    assert lay.appearance_lines - lay.density_lines >= 3 * 32 * G * (G + 1)
+

@@ -8,7 +8,7 @@ second half shifts the upper half of layer 2's output before layer 3.
   within 1e-4 of a ReLU kink redrawn;
 * render_rays and loss_and_grad with per-ray camera indices (each ray's camera repeated
   over its appearance samples, render.py:492-497) against the oracle, every gradient
-  segment including the embedding;
+  segment including the embedding, and render_rays_batched carrying each chunk's cameras;
 * a training step moves the embedding rows of the cameras it saw and no others."""
 import numpy as np
 import pytest
@@ -125,6 +125,10 @@ def test_film_render_and_gradients_match_oracle():
                  for layer in ref64["mlp"] for nm in ref64["mlp"][layer]})
     print({a: f"{b:.1e}" for a, b in errs.items()})
     assert max(errs.values()) < RTOL, errs
+    # Chunked rendering hands each chunk its own rays' cameras.
+    chunked = render.render_rays_batched(spec.mlp(), lp, aabb, rays, noise, cfg, batch_size=64,
+                                         density_shift=shift, to_host=False).cpu()
+    assert _rel(chunked, img) < 1e-6
 
 
 def test_film_training_step_moves_only_seen_cameras():

@@ -49,7 +49,7 @@ def _rays(R, seed):
     return torch.tensor(o), torch.tensor(d), torch.tensor(c)
 
 
-@pytest.mark.parametrize("C", [8, 16, 24, 48])
+@pytest.mark.parametrize("C", [8, 16, 24, 32, 48])
 def test_vm_features_fwd_bwd(tg, C):
     from tensorf_gb300.tensor_vm import TensorVM
     gen = torch.Generator().manual_seed(C)
