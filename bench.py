@@ -87,7 +87,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -399,24 +399,69 @@ def mlp_flops(w, phase):
     return {"mlp_fwd": 2 * rows * per_row, "mlp_bwd": 4 * rows * per_row}.get(phase)
 
 
-def roofline_for(w, phase_ms):
+# Phases that are one kernel launch in the single-stream pass, with the kernel the
+# headline workload runs (N >= 128 and k >= 32 select the pair-merging scatters).
+SINGLE_KERNEL_PHASES = {"density_fwd": "density_fwd_kernel", "appearance_fwd": "appearance_fwd_kernel",
+                        "density_bwd": "density_bwd2_kernel", "appearance_bwd": "appearance_bwd2_kernel",
+                        "adam": "adam_kernel"}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the headline
+# step's kernels, from one ncu capture of the full-size workload; the command and the
+# per-kernel figures are in profiles/dram_traffic_train_fp32_300grid_4096rays.md.
+NCU_DRAM_BYTES_PER_LAUNCH = {"density_bwd": 46.4e6}
+
+
+def roofline_for(w, phase_ms, l2):
+    """The dominant kernel of the headline step, the longest single-kernel phase.
+    The field gathers and scatters work on L2-resident fields, so their bound is L2:
+    for a scatter, the algorithmic reduction bytes (one 4-byte reduction per gathered
+    element) over the measured L2 float4-reduction bandwidth; its HBM figures are kept
+    beside it with the DRAM traffic ncu measured."""
     hbm, bf16, src = measured_peaks()
-    dom = max(phase_ms, key=lambda p: phase_ms[p])
-    if dom in ("mlp_fwd", "mlp_bwd"):
-        tflops = mlp_flops(w, dom) / (phase_ms[dom] / 1e3) / 1e12
-        if w["precision"] == "bf16":
-            peak, note = bf16, "bf16 tcgen05 against the measured bf16 peak"
-        else:
-            # FP32-accurate path: 3 tf32 MMAs per product at half the bf16 rate, so the
-            # algorithmic FLOP peak is the measured bf16 peak / 6.
-            peak, note = bf16 / 6.0, "split-tf32 (3 tf32 MMAs per product): peak = measured bf16 / 6"
-        return {"bound": "tensor", "kernel": dom, "achieved": round(tflops, 2), "peak": round(peak, 1),
-                "unit": "TFLOP/s", "frac": round(tflops / peak, 4), "traffic": None, "peak_source": src,
-                "note": note}
-    gb = algorithmic_bytes(w, dom) / (phase_ms[dom] / 1e3) / 1e9
-    return {"bound": "hbm", "kernel": dom, "achieved": round(gb, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(gb / hbm, 4), "traffic": None, "peak_source": src,
-            "note": "gathers/scatters are L2-resident: algorithmic bytes over the measured HBM copy peak"}
+    dom = max((p for p in SINGLE_KERNEL_PHASES if phase_ms.get(p)), key=lambda p: phase_ms[p])
+    ms = phase_ms[dom]
+    alg = algorithmic_bytes(w, dom)
+    hbm_part = {"achieved": round(alg / (ms / 1e3) / 1e9, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(alg / (ms / 1e3) / 1e9 / hbm, 4), "peak_source": src}
+    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(dom)
+    if dom in ("density_bwd", "appearance_bwd") and l2:
+        red = gather_scatter_bytes(w, dom)[1]
+        gbs = red / (ms / 1e3) / 1e9
+        return {"bound": "l2", "kernel": SINGLE_KERNEL_PHASES[dom], "achieved": round(gbs, 1),
+                "peak": l2["l2_red_gbs"], "unit": "GB/s", "frac": round(gbs / l2["l2_red_gbs"], 4),
+                "traffic": traffic, "algorithmic_bytes": alg, "reduction_bytes": red, "ms": round(ms, 4),
+                "hbm": hbm_part, "peak_source": "measured: tvm_l2_probe float4 reductions in this run",
+                "note": "L2-resident scatter: reductions over the measured L2 reduction bandwidth; traffic is "
+                        "the DRAM bytes ncu measured for one launch at this size"}
+    return {"bound": "hbm", "kernel": SINGLE_KERNEL_PHASES[dom], "achieved": hbm_part["achieved"], "peak": hbm,
+            "unit": "GB/s", "frac": hbm_part["frac"], "traffic": traffic, "algorithmic_bytes": alg,
+            "ms": round(ms, 4), "peak_source": src}
+
+
+def measure_tf32_peak(n=8192, launches=5):
+    """cuBLAS TF32 GEMM throughput on this GPU (fp32 n x n x n with TF32 tensor cores),
+    TFLOP/s, best of `launches`: the denominator of the split-tf32 FeatureMlp, which
+    issues three TF32 products per FP32 product."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        g = torch.Generator(device="cuda").manual_seed(0)
+        a = torch.randn(n, n, device="cuda", generator=g)
+        b = torch.randn(n, n, device="cuda", generator=g)
+        for _ in range(3):
+            a @ b
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(launches):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a @ b
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return {"tflops": round(2 * n ** 3 / (best / 1e3) / 1e12, 1), "n": n,
+            "how": "torch fp32 matmul with TF32 tensor cores (cuBLAS), best of 5"}
 
 
 def measure_l2_peaks(mb=48, passes=20, launches=5):
@@ -455,10 +500,11 @@ def gather_scatter_bytes(w, phase):
             "appearance_bwd": (R * k * app_el * s, R * k * app_el * 4)}.get(phase)
 
 
-def kernel_rooflines(w, phase_ms, l2):
+def kernel_rooflines(w, phase_ms, l2, tf32=None):
     """Per phase: achieved algorithmic GB/s (or TFLOP/s for the MLP) and its fraction of
     the peak that bounds it: HBM for Adam, L2 (read + reduction time) for the field
-    gathers and scatters, the tensor pipe for the MLP."""
+    gathers and scatters, the tensor pipe for the MLP (the measured bf16 peak, or for
+    split-tf32 one third of the measured TF32 peak)."""
     hbm, bf16, _ = measured_peaks()
     out = {}
     for ph in ("density_fwd", "appearance_fwd", "density_bwd", "appearance_bwd", "adam", "mlp_fwd", "mlp_bwd"):
@@ -467,7 +513,10 @@ def kernel_rooflines(w, phase_ms, l2):
             continue
         if ph in ("mlp_fwd", "mlp_bwd"):
             tf = mlp_flops(w, ph) / (ms / 1e3) / 1e12
-            peak = bf16 if w["precision"] == "bf16" else bf16 / 6.0
+            if w["precision"] == "bf16":
+                peak = bf16
+            else:
+                peak = tf32["tflops"] / 3.0 if tf32 else bf16 / 6.0
             out[ph] = {"ms": round(ms, 4), "tflops": round(tf, 1), "frac_tensor": round(tf / peak, 3)}
             continue
         b = algorithmic_bytes(w, ph)
@@ -526,6 +575,7 @@ def run_ours(args):
     _, phase_ms, _ = time_train(st_plain, data, nph, 0, phases=True, start_step=args.warmup + args.steps)
     done_plain = args.warmup + args.steps + nph
     l2 = measure_l2_peaks()
+    tf32 = measure_tf32_peak()
 
     # End to end through the public API: pinned host rays and colours copied in every
     # step, the loss read back every step.
@@ -565,9 +615,10 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 1), "unit": "rays/s", "h2d_bytes_per_step": R * 9 * 4,
                 "d2h_bytes_per_step": 4},
         "gpu_launches": launches,
-        "roofline": roofline_for(plain, phase_ms),
+        "roofline": roofline_for(plain, phase_ms, l2),
         "l2_peaks": l2,
-        "kernels": kernel_rooflines(plain, phase_ms, l2),
+        "tf32_peak": tf32,
+        "kernels": kernel_rooflines(plain, phase_ms, l2, tf32),
         "clocks": clk.summary(),
     }
 
@@ -581,7 +632,7 @@ def run_ours(args):
             variants[name] = {"train_rays_per_s": round(w["R"] * args.steps / (vms / 1e3), 1),
                               "ms_per_step": round(vms / args.steps, 4),
                               "phase_ms": {p: round(v, 4) for p, v in vph.items()},
-                              "kernels": kernel_rooflines(w, vph, l2),
+                              "kernels": kernel_rooflines(w, vph, l2, tf32),
                               "density_samples": w["N"], "appearance_samples": w["k"],
                               "proposal_samples": w["proposal"]}
             states[name] = (w, st, vdone)

@@ -148,6 +148,45 @@ __device__ __forceinline__ void red_chunk(float* p, const float (&v)[CPL]) {
   }
 }
 
+// A lane's CPL consecutive floats of a buffer that is written once and read once
+// (appearance features, their gradients), moved with the evict-first cache hint so the
+// stream does not push the fields out of L2. p is 16-byte aligned when CPL % 4 == 0, else
+// 8-byte aligned.
+template <int CPL>
+__device__ __forceinline__ void store_streaming(float* p, const float (&v)[CPL]) {
+  if constexpr (CPL % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < CPL / 4; ++j)
+      __stcs(reinterpret_cast<float4*>(p) + j, make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]));
+  } else {
+    static_assert(CPL % 2 == 0, "lanes hold an even number of channels");
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) __stcs(reinterpret_cast<float2*>(p) + j, make_float2(v[2 * j], v[2 * j + 1]));
+  }
+}
+
+template <int CPL>
+__device__ __forceinline__ void load_streaming(const float* p, float (&v)[CPL]) {
+  if constexpr (CPL % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < CPL / 4; ++j) {
+      const float4 q = __ldcs(reinterpret_cast<const float4*>(p) + j);
+      v[4 * j] = q.x;
+      v[4 * j + 1] = q.y;
+      v[4 * j + 2] = q.z;
+      v[4 * j + 3] = q.w;
+    }
+  } else {
+    static_assert(CPL % 2 == 0, "lanes hold an even number of channels");
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+      const float2 q = __ldcs(reinterpret_cast<const float2*>(p) + j);
+      v[2 * j] = q.x;
+      v[2 * j + 1] = q.y;
+    }
+  }
+}
+
 // Linear-interpolation taps of map_coordinates(order=1, mode="nearest")
 // (tensor_vm.py:226-250): weights from the unclamped coordinate, both corner indices
 // clamped into [0, G-1]. The float->int conversion is done on a clamped copy so

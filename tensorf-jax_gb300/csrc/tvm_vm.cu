@@ -380,8 +380,10 @@ __global__ void __launch_bounds__(256) appearance_fwd_kernel(const T* __restrict
     mode_perm(m, a, b, c);
     PairEval<T, CPL> e;
     vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+    float v[CPL];
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) dst[m * C + j] = e.L[j] * e.P[j];
+    for (int j = 0; j < CPL; ++j) v[j] = e.L[j] * e.P[j];
+    store_streaming<CPL>(dst + m * C, v);
   }
 }
 
@@ -415,8 +417,7 @@ __global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict
     PairEval<T, CPL> e;
     vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
     float gv[CPL];
-#pragma unroll
-    for (int j = 0; j < CPL; ++j) gv[j] = __ldg(src + m * C + j);
+    load_streaming<CPL>(src + m * C, gv);
     vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
   }
 }
@@ -469,10 +470,12 @@ __global__ void __launch_bounds__(256) appearance_bwd2_kernel(const T* __restric
     PairEval<T, CPL> ea, eb;
     vm_pair_eval<T, CPL>(lines, planes, G, C, m, ua[a], ua[b], ua[c], sub * CPL, ea);
     float ga[CPL], gb[CPL];
+    load_streaming<CPL>(srca + m * C, ga);
+    if (has_b) {
+      load_streaming<CPL>(srcb + m * C, gb);
+    } else {
 #pragma unroll
-    for (int j = 0; j < CPL; ++j) {
-      ga[j] = __ldg(srca + m * C + j);
-      gb[j] = has_b ? __ldg(srcb + m * C + j) : 0.0f;
+      for (int j = 0; j < CPL; ++j) gb[j] = 0.0f;
     }
     if (has_b) vm_pair_eval<T, CPL>(lines, planes, G, C, m, ub[a], ub[b], ub[c], sub * CPL, eb);
     vm_pair_scatter2<T, CPL>(glines, gplanes, G, C, m, sub * CPL, ea, ga, has_b, eb, gb);
