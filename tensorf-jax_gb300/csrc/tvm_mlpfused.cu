@@ -68,6 +68,34 @@ __device__ void stage_weight(uint8_t* dst, const float* __restrict__ W, int ld, 
   }
 }
 
+// One 128-row tile of X0 (fp32, global) into a bf16 A tile (K-major canonical, SBO
+// sbo) at dst; rows at or past M are zero. Each thread issues all of its loads before
+// its first shared-memory store, so the tile costs one L2 round trip, not nine.
+__device__ __forceinline__ void load_x0_tile(uint8_t* dst, int sbo, const float* X0, int64_t m0, int64_t M,
+                                             int tid) {
+  constexpr int PER_THREAD = BM * (F / 8) / THREADS;
+  static_assert(BM * (F / 8) % THREADS == 0, "whole chunks per thread");
+  float4 p[PER_THREAD], q[PER_THREAD];
+#pragma unroll
+  for (int i = 0; i < PER_THREAD; ++i) {
+    const int c = tid + i * THREADS;
+    const int64_t row = m0 + c / (F / 8);
+    p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    q[i] = p[i];
+    if (row < M) {
+      const float4* src = reinterpret_cast<const float4*>(X0 + row * F + (c % (F / 8)) * 8);
+      p[i] = __ldg(src);
+      q[i] = __ldg(src + 1);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < PER_THREAD; ++i) {
+    const int c = tid + i * THREADS;
+    *reinterpret_cast<uint4*>(dst + coff(c / (F / 8), c % (F / 8), sbo)) =
+        make_uint4(pack2(p[i].x, p[i].y), pack2(p[i].z, p[i].w), pack2(q[i].x, q[i].y), pack2(q[i].z, q[i].w));
+  }
+}
+
 __device__ __forceinline__ void issue(uint32_t tmem_d, uint32_t a, uint32_t b, int ksteps, uint32_t sbo_a,
                                       uint32_t sbo_b, uint32_t idesc) {
 #pragma unroll 1
@@ -149,19 +177,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   const int64_t ntiles = (a.M + BM - 1) / BM;
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int64_t m0 = tile * BM;
-    // X0 tile: 128 rows x 18 chunks of 8 features.
-    for (int c = tid; c < BM * (F / 8); c += THREADS) {
-      const int r = c / (F / 8), kc = c % (F / 8);
-      const int64_t row = m0 + r;
-      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), q = p;
-      if (row < a.M) {
-        const float4* src = reinterpret_cast<const float4*>(a.X0 + row * F + kc * 8);
-        p = __ldg(src);
-        q = __ldg(src + 1);
-      }
-      *reinterpret_cast<uint4*>(smem + OFF_A0 + coff(r, kc, SBO_F)) =
-          make_uint4(pack2(p.x, p.y), pack2(p.z, p.w), pack2(q.x, q.y), pack2(q.z, q.w));
-    }
+    load_x0_tile(smem + OFF_A0, SBO_F, a.X0, m0, a.M, tid);  // 128 rows x 18 chunks of 8 features
     {  // the next tile's features travel to L2 while this tile computes
       const int64_t nm0 = (tile + gridDim.x) * BM;
       if (nm0 < a.M) {
@@ -447,18 +463,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
     return all != 0;
   };
   auto load_x0 = [&](int64_t m0) {
-    for (int c = tid; c < BM * (F / 8); c += THREADS) {
-      const int rr = c / (F / 8), kc = c % (F / 8);
-      const int64_t row = m0 + rr;
-      float4 p = make_float4(0.f, 0.f, 0.f, 0.f), q = p;
-      if (row < a.M) {
-        const float4* src = reinterpret_cast<const float4*>(a.X0 + row * F + kc * 8);
-        p = __ldg(src);
-        q = __ldg(src + 1);
-      }
-      *reinterpret_cast<uint4*>(smem + RA + coff(rr, kc, SBO_A)) =
-          make_uint4(pack2(p.x, p.y), pack2(p.z, p.w), pack2(q.x, q.y), pack2(q.z, q.w));
-    }
+    load_x0_tile(smem + RA, SBO_A, a.X0, m0, a.M, tid);
   };
   // +bias, ReLU, bf16 into a natural tile.
   auto hidden = [&](const float* bias, int dst, int sbo) {

@@ -79,6 +79,59 @@ __device__ __forceinline__ void vm_pair_scatter(float* __restrict__ glines, floa
   }
 }
 
+// One tap slot's reductions for the 8 samples (quads) of a warp. Along a ray every tap
+// index is monotone, so quads of consecutive samples that land on the same texel form a
+// contiguous run: the run's values are summed in registers (a segmented reduction over
+// quads with shuffles of 4, 8 and 16 lanes) and its first quad issues one reduction.
+// key: the texel (>= 0), or -1 for a quad with nothing to add. All 32 lanes call this.
+template <int CPL>
+__device__ __forceinline__ void warp_red_chunk(float* __restrict__ base, int key, int C, float (&v)[CPL]) {
+  const unsigned lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(0xffffffffu, key, 4);  // the previous quad's key, same channels
+  const bool head = lane < 4 || prev != key;
+  const unsigned heads = __ballot_sync(0xffffffffu, head) & 0x11111111u;  // one bit per quad
+  if (heads != 0x11111111u) {  // some quad continues a run (the same for the whole warp)
+#pragma unroll
+    for (int o = 4; o < 32; o <<= 1) {
+      float u[CPL];
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) u[j] = __shfl_down_sync(0xffffffffu, v[j], o);
+      // lane + o belongs to this run when no quad in (lane, lane + o] starts a run
+      if (lane + o < 32 && ((heads >> (lane + 1)) & ((1u << o) - 1u)) == 0u) {
+#pragma unroll
+        for (int j = 0; j < CPL; ++j) v[j] += u[j];
+      }
+    }
+  }
+  if (head && key >= 0) red_chunk<CPL>(base + (int64_t)key * C, v);
+}
+
+// vm_pair_scatter for the consecutive samples of a warp, each tap slot merged over the
+// warp's quads (warp_red_chunk). active: this quad's sample has a gradient to add.
+template <typename T, int CPL>
+__device__ __forceinline__ void vm_pair_scatter_warp(float* __restrict__ glines, float* __restrict__ gplanes,
+                                                     int G, int C, int m, int ch0, bool active,
+                                                     const PairEval<T, CPL>& e, const float (&g)[CPL]) {
+  float* lb = glines + (int64_t)m * G * C + ch0;
+  float* pb = gplanes + (int64_t)m * G * G * C + ch0;
+  float v[CPL];
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) v[j] = g[j] * e.P[j] * e.tl.w0;
+  warp_red_chunk<CPL>(lb, active ? e.tl.i0 : -1, C, v);
+#pragma unroll
+  for (int j = 0; j < CPL; ++j) v[j] = g[j] * e.P[j] * e.tl.w1;
+  warp_red_chunk<CPL>(lb, active ? e.tl.i1 : -1, C, v);
+  const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
+  const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
+  const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int j = 0; j < CPL; ++j) v[j] = g[j] * e.L[j] * w[q];
+    warp_red_chunk<CPL>(pb, active ? rows[q] * G + cols[q] : -1, C, v);
+  }
+}
+
 // Scatter of two samples' gradients for pair m (sample b optional): b's taps that land
 // on one of a's taps are added into a's values first, so a texel shared by consecutive
 // samples of a ray gets one reduction instead of two. (Consecutive samples of a ray are
@@ -263,20 +316,25 @@ __global__ void __launch_bounds__(256) density_bwd_kernel(const T* __restrict__ 
                                                          const float* __restrict__ dirs,
                                                          int64_t total, SamplerArgs s,
                                                          const float* __restrict__ gsum) {
+  // The warp's 8 samples are consecutive along a ray: their reductions are merged per
+  // texel (vm_pair_scatter_warp), so every lane stays to the end.
   constexpr int CPL = C / 4;
   const int64_t smp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
   const int sub = threadIdx.x & 3;
-  if (smp >= total) return;
-  const float gs = __ldg(gsum + smp);
-  if (gs == 0.0f) return;  // the whole quad agrees: nothing to scatter
-  const int64_t r = smp / s.N;
-  const int i = (int)(smp - r * s.N);
-  RayGeom g = load_ray(origins, dirs, r, s);
-  float t, delta, x[3], u[3];
-  sample_t(g, s, r, i, t, delta);
-  sample_point(g, s, t, x);
+  const float gs = smp < total ? __ldg(gsum + smp) : 0.0f;
+  const bool active = gs != 0.0f;
+  if (__all_sync(0xffffffffu, !active)) return;  // nothing to scatter in this warp
+  float u[3] = {0.f, 0.f, 0.f};
+  if (active) {
+    const int64_t r = smp / s.N;
+    const int i = (int)(smp - r * s.N);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
 #pragma unroll
-  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+    for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  }
   float gv[CPL];
 #pragma unroll
   for (int j = 0; j < CPL; ++j) gv[j] = gs;
@@ -285,8 +343,12 @@ __global__ void __launch_bounds__(256) density_bwd_kernel(const T* __restrict__ 
     int a, b, c;
     mode_perm(m, a, b, c);
     PairEval<T, CPL> e;
-    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
-    vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
+    if (active) {
+      vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+    } else {
+      e = PairEval<T, CPL>{};
+    }
+    vm_pair_scatter_warp<T, CPL>(glines, gplanes, G, C, m, sub * CPL, active, e, gv);
   }
 }
 
@@ -397,28 +459,41 @@ __global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict
                                                             int64_t rows, int k, SamplerArgs s,
                                                             const int32_t* __restrict__ sel_idx,
                                                             const float* __restrict__ dX0) {
+  // A ray's selected samples are consecutive rows in sample order, so a warp's 8 rows
+  // are mostly neighbours along one ray: their reductions are merged per texel
+  // (vm_pair_scatter_warp), and every lane stays to the end.
   constexpr int CPL = C / 4;
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
   const int sub = threadIdx.x & 3;
-  if (row >= rows) return;
-  const int64_t r = row / k;
-  const int i = __ldg(sel_idx + row);
-  RayGeom g = load_ray(origins, dirs, r, s);
-  float t, delta, x[3], u[3];
-  sample_t(g, s, r, i, t, delta);
-  sample_point(g, s, t, x);
+  const bool active = row < rows;
+  if (__all_sync(0xffffffffu, !active)) return;
+  float u[3] = {0.f, 0.f, 0.f};
+  if (active) {
+    const int64_t r = row / k;
+    const int i = __ldg(sel_idx + row);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
 #pragma unroll
-  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+    for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+  }
   const float* src = dX0 + row * (3 * C) + sub * CPL;
 #pragma unroll
   for (int m = 0; m < 3; ++m) {
     int a, b, c;
     mode_perm(m, a, b, c);
     PairEval<T, CPL> e;
-    vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
     float gv[CPL];
-    load_streaming<CPL>(src + m * C, gv);
-    vm_pair_scatter<T, CPL>(glines, gplanes, G, C, m, sub * CPL, e, gv);
+    if (active) {
+      vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+      load_streaming<CPL>(src + m * C, gv);
+    } else {
+      e = PairEval<T, CPL>{};
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) gv[j] = 0.0f;
+    }
+    vm_pair_scatter_warp<T, CPL>(glines, gplanes, G, C, m, sub * CPL, active, e, gv);
   }
 }
 
