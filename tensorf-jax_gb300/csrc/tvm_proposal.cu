@@ -88,8 +88,39 @@ __device__ __forceinline__ void prop_sample(const RayGeom& g, const SamplerArgs&
 // Features X[s] = [12 VM features (pair-major), x, y, z, |x|_inf], bin length, and
 // (with weights) the whole MLP in registers: h = relu(X W1 + b1), sigma = softplus(h W2
 // + b2 + shift). The weights sit in shared memory and every thread reads the same
-// element at the same time (broadcast). X and h are written only when the backward
-// needs them.
+// element at the same time (broadcast); each thread carries two samples (blockDim
+// apart) through the MLP, so every weight it loads serves both. X and h are written only
+// when the backward needs them.
+template <typename T>
+__device__ __forceinline__ void prop_sample_features(const T* __restrict__ lines, const T* __restrict__ planes, int G,
+                                                     const float* __restrict__ origins, const float* __restrict__ dirs,
+                                                     const SamplerArgs& s, const float* __restrict__ edges,
+                                                     const float* __restrict__ jitter, int64_t smp,
+                                                     float (&out)[PROP_IN], float& len) {
+  const int Np = s.N;
+  const int64_t r = smp / Np;
+  const int j = (int)(smp - r * Np);
+  RayGeom g = load_ray(origins, dirs, r, s);
+  float t, x[3];
+  prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    int a, b, c;
+    mode_perm(m, a, b, c);
+    PropPair e;
+    prop_pair<T>(lines, planes, G, m, u[a], u[b], u[c], e);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) out[m * 4 + q] = e.L[q] * e.P[q];
+  }
+  out[12] = x[0];
+  out[13] = x[1];
+  out[14] = x[2];
+  out[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) prop_features_kernel(
     const T* __restrict__ lines, const T* __restrict__ planes, int G, const float* __restrict__ origins,
@@ -112,58 +143,57 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
     }
     __syncthreads();
   }
-  const int Np = s.N;
-  const int64_t smp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (smp >= R * Np) return;
-  const int64_t r = smp / Np;
-  const int j = (int)(smp - r * Np);
-  RayGeom g = load_ray(origins, dirs, r, s);
-  float t, len, x[3];
-  prop_sample(g, s, edges, Np, jitter, r, j, t, len, x);
-  float u[3];
+  const int64_t n = R * s.N;
+  const int64_t smp0 = (int64_t)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+  const int64_t smps[2] = {smp0, smp0 + blockDim.x};
+  if (smp0 >= n) return;
+  const bool two = smps[1] < n;
+  float out[2][PROP_IN];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
-  float out[PROP_IN];
+  for (int k = 0; k < 2; ++k) {
+    if (k == 1 && !two) {
 #pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    int a, b, c;
-    mode_perm(m, a, b, c);
-    PropPair e;
-    prop_pair<T>(lines, planes, G, m, u[a], u[b], u[c], e);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) out[m * 4 + q] = e.L[q] * e.P[q];
-  }
-  out[12] = x[0];
-  out[13] = x[1];
-  out[14] = x[2];
-  out[15] = fmaxf(fabsf(x[0]), fmaxf(fabsf(x[1]), fabsf(x[2])));
-  if (X) {
-    float4* dst = reinterpret_cast<float4*>(X + smp * PROP_IN);
-#pragma unroll
-    for (int q = 0; q < 4; ++q) dst[q] = make_float4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
-  }
-  delta[smp] = len;
-  if (mlp) {
-    const float4* sw1 = reinterpret_cast<const float4*>(sw);  // row u: 16 weights
-    const float* sb1 = sw + 16 * units;
-    const float* sw2 = sw + 17 * units;
-    float z = __ldg(b2);
-    for (int u = 0; u < units; ++u) {
-      float h = sb1[u];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 w = sw1[u * 4 + q];
-        h = fmaf(out[4 * q], w.x, h);
-        h = fmaf(out[4 * q + 1], w.y, h);
-        h = fmaf(out[4 * q + 2], w.z, h);
-        h = fmaf(out[4 * q + 3], w.w, h);
-      }
-      h = fmaxf(h, 0.0f);
-      if (H) H[smp * units + u] = h;
-      z = fmaf(h, sw2[u], z);
+      for (int i = 0; i < PROP_IN; ++i) out[1][i] = 0.f;
+      continue;
     }
-    sigma[smp] = softplus_f(z + shift);
+    float len;
+    prop_sample_features<T>(lines, planes, G, origins, dirs, s, edges, jitter, smps[k], out[k], len);
+    if (X) {
+      float4* dst = reinterpret_cast<float4*>(X + smps[k] * PROP_IN);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        dst[q] = make_float4(out[k][4 * q], out[k][4 * q + 1], out[k][4 * q + 2], out[k][4 * q + 3]);
+    }
+    delta[smps[k]] = len;
   }
+  if (!mlp) return;
+  const float4* sw1 = reinterpret_cast<const float4*>(sw);  // row u: 16 weights
+  const float* sb1 = sw + 16 * units;
+  const float* sw2 = sw + 17 * units;
+  float z[2] = {__ldg(b2), __ldg(b2)};
+  for (int u = 0; u < units; ++u) {
+    float h[2] = {sb1[u], sb1[u]};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 w = sw1[u * 4 + q];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        h[k] = fmaf(out[k][4 * q], w.x, h[k]);
+        h[k] = fmaf(out[k][4 * q + 1], w.y, h[k]);
+        h[k] = fmaf(out[k][4 * q + 2], w.z, h[k]);
+        h[k] = fmaf(out[k][4 * q + 3], w.w, h[k]);
+      }
+    }
+    const float w2u = sw2[u];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      h[k] = fmaxf(h[k], 0.0f);
+      if (H && (k == 0 || two)) H[smps[k] * units + u] = h[k];
+      z[k] = fmaf(h[k], w2u, z[k]);
+    }
+  }
+  sigma[smps[0]] = softplus_f(z[0] + shift);
+  if (two) sigma[smps[1]] = softplus_f(z[1] + shift);
 }
 
 // Fused proposal backward, one thread per sample, 128 samples per block: recompute the
@@ -456,7 +486,7 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
                          cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
-  const unsigned blocks = (unsigned)ceil_div(n, 128);
+  const unsigned blocks = (unsigned)ceil_div(n, 256);  // 128 threads, two samples each
   const int units = mlp ? mlp->units : 0;
   const size_t smem = mlp ? (size_t)18 * units * sizeof(float) : 0;
   const float *w1 = mlp ? mlp->w1 : nullptr, *b1 = mlp ? mlp->b1 : nullptr, *w2 = mlp ? mlp->w2 : nullptr,

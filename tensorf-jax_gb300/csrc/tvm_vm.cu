@@ -459,42 +459,41 @@ __global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict
                                                             int64_t rows, int k, SamplerArgs s,
                                                             const int32_t* __restrict__ sel_idx,
                                                             const float* __restrict__ dX0) {
-  // A ray's selected samples are consecutive rows in sample order, so a warp's 8 rows
-  // are mostly neighbours along one ray: their reductions are merged per texel
+  // One quad per (pair m, row), pair-major: with few selected samples (k < 32) there are
+  // few rows, and three quads per row keep three times as many warps in flight. A ray's
+  // selected samples are consecutive rows in sample order, so a warp's 8 quads are mostly
+  // neighbours along one ray for the same pair: their reductions are merged per texel
   // (vm_pair_scatter_warp), and every lane stays to the end.
   constexpr int CPL = C / 4;
-  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int64_t quad = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
   const int sub = threadIdx.x & 3;
-  const bool active = row < rows;
+  const int m = (int)(quad / rows < 3 ? quad / rows : 2);
+  const int64_t row = quad - (int64_t)m * rows;
+  const bool active = quad < 3 * rows;
   if (__all_sync(0xffffffffu, !active)) return;
-  float u[3] = {0.f, 0.f, 0.f};
+  int a, b, c;
+  mode_perm(m, a, b, c);
+  PairEval<T, CPL> e;
+  float gv[CPL];
   if (active) {
     const int64_t r = row / k;
     const int i = __ldg(sel_idx + row);
     RayGeom g = load_ray(origins, dirs, r, s);
-    float t, delta, x[3];
+    float t, delta, x[3], u[3];
     sample_t(g, s, r, i, t, delta);
     sample_point(g, s, t, x);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
-  }
-  const float* src = dX0 + row * (3 * C) + sub * CPL;
+    for (int q = 0; q < 3; ++q) u[q] = grid_coord(x[q], G);
+    // the pair's axes, selected without indexing the array by a runtime value
+    auto pick = [&](int q) { return q == 0 ? u[0] : (q == 1 ? u[1] : u[2]); };
+    vm_pair_eval<T, CPL>(lines, planes, G, C, m, pick(a), pick(b), pick(c), sub * CPL, e);
+    load_streaming<CPL>(dX0 + row * (3 * C) + m * C + sub * CPL, gv);
+  } else {
+    e = PairEval<T, CPL>{};
 #pragma unroll
-  for (int m = 0; m < 3; ++m) {
-    int a, b, c;
-    mode_perm(m, a, b, c);
-    PairEval<T, CPL> e;
-    float gv[CPL];
-    if (active) {
-      vm_pair_eval<T, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
-      load_streaming<CPL>(src + m * C, gv);
-    } else {
-      e = PairEval<T, CPL>{};
-#pragma unroll
-      for (int j = 0; j < CPL; ++j) gv[j] = 0.0f;
-    }
-    vm_pair_scatter_warp<T, CPL>(glines, gplanes, G, C, m, sub * CPL, active, e, gv);
+    for (int j = 0; j < CPL; ++j) gv[j] = 0.0f;
   }
+  vm_pair_scatter_warp<T, CPL>(glines, gplanes, G, C, m, sub * CPL, active, e, gv);
 }
 
 template <typename T, int C>
@@ -724,7 +723,7 @@ int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, con
     TVM_DISPATCH_FIELD(f, (appearance_bwd2_kernel<TT, CC><<<quad_blocks((rows + 1) / 2), 256, 0, st>>>(
                                L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx, dX0)));
   } else {
-    TVM_DISPATCH_FIELD(f, (appearance_bwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
+    TVM_DISPATCH_FIELD(f, (appearance_bwd_kernel<TT, CC><<<quad_blocks(3 * rows), 256, 0, st>>>(
                                L_, P_, f.G, glines, gplanes, origins, dirs, rows, k, s, sel_idx, dX0)));
   }
   return check_launch("appearance_bwd");
