@@ -283,10 +283,18 @@ def time_then_phases(state, data, steps, warmup):
 
 
 def train_more(state, data, steps, start_step):
+    """`steps` more training steps; returns their mean ms per step (CUDA events around
+    the whole loop, nothing synchronised inside), or None for no steps."""
+    if steps <= 0:
+        return None
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
     for i in range(steps):
         r, c = data.batch(start_step + i)
         state.training_step(r, c, log=False)
+    e1.record()
     torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
 
 
 def psnr(a, b):
@@ -636,12 +644,23 @@ def run_ours(args):
                               "density_samples": w["N"], "appearance_samples": w["k"],
                               "proposal_samples": w["proposal"]}
             states[name] = (w, st, vdone)
-        # The same number of training steps for every variant, then held-out PSNR.
+        # The same number of training steps for every variant, then held-out PSNR. The
+        # proposal path's step gets cheaper as its network learns where the surfaces are,
+        # so the step is also timed over the whole training run and once trained.
         for name, (w, st, done) in states.items():
-            train_more(st, data, max(0, args.train_steps - done), done)
+            n_more = max(0, args.train_steps - done)
+            run_ms = train_more(st, data, n_more, done)
             img = eval_rays(st, w, data.test_rays)
             variants[name]["psnr_db"] = round(psnr(img, data.test_colors), 3)
             variants[name]["train_steps"] = max(args.train_steps, done)
+            if run_ms is not None:
+                variants[name]["training_run"] = {"steps": n_more, "first_step": done,
+                                                  "ms_per_step": round(run_ms, 4),
+                                                  "rays_per_s": round(w["R"] / (run_ms / 1e3), 1)}
+            tms, _, _ = time_train(st, data, args.steps, args.warmup, phases=False, start_step=done + n_more)
+            variants[name]["trained"] = {"after_steps": done + n_more + args.warmup,
+                                         "ms_per_step": round(tms / args.steps, 4),
+                                         "rays_per_s": round(w["R"] * args.steps / (tms / 1e3), 1)}
         # Full-frame render: plain FP32 (512 samples) vs proposal BF16.
         imgs = {}
         for name in ("plain_fp32", "proposal_bf16"):
@@ -659,6 +678,13 @@ def run_ours(args):
         line["variants"] = variants
         line["comparison"] = {
             "train_speedup_proposal_bf16_vs_plain_fp32": round(variants["proposal_bf16"]["train_rays_per_s"] / value, 3),
+            "train_speedup_trained": round(variants["plain_fp32"]["trained"]["ms_per_step"] /
+                                           variants["proposal_bf16"]["trained"]["ms_per_step"], 3),
+            "train_speedup_over_training_run": (
+                round(variants["plain_fp32"]["training_run"]["ms_per_step"] /
+                      variants["proposal_bf16"]["training_run"]["ms_per_step"], 3)
+                if "training_run" in variants["plain_fp32"] and "training_run" in variants["proposal_bf16"]
+                else None),
             "render_speedup_proposal_bf16_vs_plain_fp32": round(rq / rp, 3),
             "psnr_gap_db_plain_minus_proposal_bf16": round(variants["plain_fp32"]["psnr_db"] -
                                                           variants["proposal_bf16"]["psnr_db"], 3),

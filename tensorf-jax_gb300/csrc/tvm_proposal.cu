@@ -236,11 +236,14 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
   const int64_t smp = (int64_t)blockIdx.x * PBWD_THREADS + tid;
   const bool valid = smp < R * Np;
   float dz = valid ? __ldg(dz_in + smp) : 0.f;
+  // A sample with dz = 0 adds nothing to any gradient (dh = 0, so dX, dW1, dW2 and db1
+  // rows are all zero): its gathers and scatter are skipped.
+  const bool live = valid && dz != 0.f;
   float X[PROP_IN];
 #pragma unroll
   for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
   PropPair e3[3];
-  if (valid) {
+  if (live) {
     const int64_t r = smp / Np;
     const int j = (int)(smp - r * Np);
     RayGeom g = load_ray(origins, dirs, r, s);
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
   bool any = false;
 #pragma unroll
   for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
-  if (valid && any) {
+  if (live && any) {
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const PropPair& e = e3[m];
@@ -658,11 +661,14 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     const bool valid = smp < nsmp;
     const float dz = valid ? __ldg(dz_in + smp) : 0.f;
     db2 += dz;
+    // A sample with dz = 0 adds nothing to any gradient (its dH row is zero): it keeps a
+    // zero row in the tile and skips its gathers and scatter.
+    const bool live = valid && dz != 0.f;
     float X[PROP_IN];
 #pragma unroll
     for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
-    PropPair e3[3] = {};  // zero for invalid samples, whose lanes still join the merged reductions
-    if (valid) {
+    PropPair e3[3] = {};  // zero for skipped samples, whose lanes still join the merged reductions
+    if (live) {
       const int64_t r = smp / Np;
       const int j = (int)(smp - r * Np);
       RayGeom g = load_ray(origins, dirs, r, s);
@@ -731,7 +737,7 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     bool any = false;
 #pragma unroll
     for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
-    const bool add = valid && any;
+    const bool add = live && any;
     if (__any_sync(0xffffffffu, add)) {  // every lane of the warp takes part in the merged reductions
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
