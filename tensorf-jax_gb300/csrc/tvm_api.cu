@@ -458,11 +458,14 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "stream join: %s", cudaGetErrorString(e));
     return TVM_OK;
   };
-  // Updates beside other kernels use a grid of two blocks per SM: enough to keep HBM busy,
-  // and it leaves the SMs to the kernels they run beside.
+  // Updates beside other kernels use a persistent grid of a few blocks per SM, which
+  // leaves the SMs to the kernels they run beside: two while a step's field scatters have
+  // a million or more density samples to work through, four below that, where those
+  // kernels are short and leave the SMs idle between them.
+  const int side_blocks_per_sm = R * (int64_t)c.density_samples >= (1 << 20) ? 2 : 4;
   auto adam_seg = [&](int64_t lo, int64_t hi, cudaStream_t s_) {
     return launch_adam_range(adam->params, grads, adam->mu, adam->nu, lo, hi, L.mlp_begin, adam->desc, adam->shadow,
-                             adam->shadow_n, s_, s_ == st ? 8 : 2);
+                             adam->shadow_n, s_, s_ == st ? 8 : side_blocks_per_sm);
   };
   const bool has_prop = m.proposal_grid > 0;
   // Proposal bound loss on the main weights, then the proposal network's backward and its

@@ -522,34 +522,6 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
 // ---------------------------------------------------------------------------------
 static __device__ int g_prop_status;  // sticky: bit 0 = a bounded tensor-core wait gave up
 
-// One tap slot's float4 reductions for the 32 samples (lanes) of a warp. The lanes hold
-// consecutive samples of a ray, and along a ray every tap index is monotone, so lanes
-// on the same texel form contiguous runs: a segmented reduction over lanes sums each
-// run in registers and its first lane issues one reduction. The small proposal field
-// takes every ray's taps, so this also takes most of the same-address traffic off L2.
-// key: the texel, or -1 for a lane with nothing to add. All 32 lanes call this.
-__device__ __forceinline__ void warp_red4(float* __restrict__ base, int key, float4 v) {
-  const unsigned lane = threadIdx.x & 31;
-  const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-  const bool head = lane == 0 || prev != key;
-  const unsigned heads = __ballot_sync(0xffffffffu, head);
-  if (heads != 0xffffffffu) {  // some lane continues a run (the same for the whole warp)
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float4 u = make_float4(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o),
-                                   __shfl_down_sync(0xffffffffu, v.z, o), __shfl_down_sync(0xffffffffu, v.w, o));
-      // lane + o belongs to this run when no lane in (lane, lane + o] starts a run
-      if (lane + o < 32 && ((heads >> (lane + 1)) & ((1u << o) - 1u)) == 0u) {
-        v.x += u.x;
-        v.y += u.y;
-        v.z += u.z;
-        v.w += u.w;
-      }
-    }
-  }
-  if (head && key >= 0) atomicAdd(reinterpret_cast<float4*>(base + (int64_t)key * PROP_C), v);
-}
-
 namespace ptc {
 
 constexpr int THREADS = 128;
@@ -667,7 +639,7 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     float X[PROP_IN];
 #pragma unroll
     for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
-    PropPair e3[3] = {};  // zero for skipped samples, whose lanes still join the merged reductions
+    PropPair e3[3];
     if (live) {
       const int64_t r = smp / Np;
       const int j = (int)(smp - r * Np);
@@ -737,29 +709,29 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     bool any = false;
 #pragma unroll
     for (int q = 0; q < 12; ++q) any |= (dX[q] != 0.0f);
-    const bool add = live && any;
-    if (__any_sync(0xffffffffu, add)) {  // every lane of the warp takes part in the merged reductions
+    if (live && any) {
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         const PropPair& e = e3[m];
         float* lb = glines + (int64_t)m * G * PROP_C;
         float* pb = gplanes + (int64_t)m * G * G * PROP_C;
-        float d[4];
+        float v[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) d[q] = add ? dX[m * 4 + q] : 0.0f;
-        warp_red4(lb, add ? e.tl.i0 : -1,
-                  make_float4(d[0] * e.P[0] * e.tl.w0, d[1] * e.P[1] * e.tl.w0, d[2] * e.P[2] * e.tl.w0,
-                              d[3] * e.P[3] * e.tl.w0));
-        warp_red4(lb, add ? e.tl.i1 : -1,
-                  make_float4(d[0] * e.P[0] * e.tl.w1, d[1] * e.P[1] * e.tl.w1, d[2] * e.P[2] * e.tl.w1,
-                              d[3] * e.P[3] * e.tl.w1));
+        for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w0;
+        atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i0 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.P[q] * e.tl.w1;
+        atomicAdd(reinterpret_cast<float4*>(lb + e.tl.i1 * PROP_C), make_float4(v[0], v[1], v[2], v[3]));
         const float w[4] = {e.tr.w0 * e.tc.w0, e.tr.w0 * e.tc.w1, e.tr.w1 * e.tc.w0, e.tr.w1 * e.tc.w1};
         const int rows[4] = {e.tr.i0, e.tr.i0, e.tr.i1, e.tr.i1};
         const int cols[4] = {e.tc.i0, e.tc.i1, e.tc.i0, e.tc.i1};
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-          warp_red4(pb, add ? rows[k] * G + cols[k] : -1,
-                    make_float4(d[0] * e.L[0] * w[k], d[1] * e.L[1] * w[k], d[2] * e.L[2] * w[k], d[3] * e.L[3] * w[k]));
+        for (int k = 0; k < 4; ++k) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) v[q] = dX[m * 4 + q] * e.L[q] * w[k];
+          atomicAdd(reinterpret_cast<float4*>(pb + ((int64_t)rows[k] * G + cols[k]) * PROP_C),
+                    make_float4(v[0], v[1], v[2], v[3]));
+        }
       }
     }
     first = false;
