@@ -236,12 +236,17 @@ def job_rays_per_s(rays_per_step, steps, world, ms_max):
 
 def time_train(state, data, steps, warmup, phases=True, start_step=0):
     """Warm-up, then `steps` timed steps on device-resident batches. Returns (ms total,
-    per-phase mean ms, kernel launches)."""
+    per-phase mean ms, kernel launches: the library's eager launches plus the kernels of
+    the replayed CUDA graphs). A phase pass runs the steps eagerly: phase events are
+    recorded by the library as it launches."""
     import ctypes
 
     from tensorf_gb300 import _lib
 
     lib = _lib.load()
+    graph_was = state.cuda_graph
+    if phases:
+        state.cuda_graph = False
     for i in range(warmup):
         r, c = data.batch(start_step + i)
         state.training_step(r, c, log=False)
@@ -254,6 +259,7 @@ def time_train(state, data, steps, warmup, phases=True, start_step=0):
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     l0 = lib.tvm_kernel_launches()
+    g0 = state.graph_kernel_launches
     start.record()
     for i in range(steps):
         if phases:
@@ -264,7 +270,8 @@ def time_train(state, data, steps, warmup, phases=True, start_step=0):
     _lib.call("tvm_set_phase_events", None, 0)
     end.record()
     torch.cuda.synchronize()
-    launches = int(lib.tvm_kernel_launches() - l0)
+    state.cuda_graph = graph_was
+    launches = int(lib.tvm_kernel_launches() - l0) + int(state.graph_kernel_launches - g0)
     phase_ms = {}
     if phases:
         phase_ms = {p: statistics.mean(evs[i][j].elapsed_time(evs[i][j + 1]) for i in range(steps))

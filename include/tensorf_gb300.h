@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define TVM_ABI_VERSION 2
+#define TVM_ABI_VERSION 3
 
 /* Symbols of this library are exported with default visibility. */
 #ifndef TVM_API
@@ -167,6 +167,14 @@ typedef struct {
   float proposal_loss_weight;    /* weight of the proposal bound loss (training) */
 } tvm_render_desc;
 
+/* The per-update Adam scalars in device memory, for training steps recorded once as a
+ * CUDA graph and replayed: the host writes the next update's values with
+ * tvm_adam_set_step on the replay stream before each replay. */
+typedef struct {
+  int32_t count;    /* step count after increment: 1 on the first update */
+  float lr_decay;   /* multiplier from the exponential decay (training.py:158-181) */
+} tvm_adam_step_scalars;
+
 /* Adam hyper-parameters (training.py:207-243; optax.scale_by_adam). */
 typedef struct {
   float lr_tensor;  /* 0.02 */
@@ -178,6 +186,9 @@ typedef struct {
   float* grad_sq;   /* optional device float, or NULL: overwritten with the sum of the squared
                        gradients the update consumed, the square of optax.global_norm(grads)
                        that training_step logs as grad_norm (training.py:190-196) */
+  const tvm_adam_step_scalars* device_step; /* optional device struct, or NULL: when set, the
+                       update reads count and lr_decay from it when it runs (the host fields
+                       are then not used), so a recorded step can be replayed */
 } tvm_adam_desc;
 
 /* ---- library ---------------------------------------------------------------------- */
@@ -380,6 +391,11 @@ TVM_API int tvm_loss_f64(const tvm_model_desc* model, const void* params, const 
  * non-NULL (TVM_BF16) the field segments are rounded into it. */
 TVM_API int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* mu, void* nu,
                   const tvm_adam_desc* adam, void* shadow, void* stream);
+/* Write count and lr_decay into a device tvm_adam_step_scalars, ordered on `stream`
+ * (one single-thread kernel: the values travel as launch arguments, so the host may
+ * reuse its variables at once). No counterpart in the reference, whose jitted step takes
+ * its optimizer state as traced arrays. */
+TVM_API int tvm_adam_set_step(tvm_adam_step_scalars* device_step, int32_t count, float lr_decay, void* stream);
 /* Round the field segments of params into the bf16 shadow (after init / load). */
 TVM_API int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow,
                        void* stream);

@@ -18,7 +18,13 @@ namespace tvm {
 struct AdamScalars {
   float b1, b2, omb1, omb2, rbc1, rbc2, eps, lr_t, lr_m, decay;
   float* grad_sq;  // accumulates the sum of g^2 when non-null
+  const tvm_adam_step_scalars* step;  // when non-null: count and decay are read from it
 };
+
+// optax.bias_correction: 1 / (1 - decay**count) in float32.
+__host__ __device__ __forceinline__ float bias_correction_rcp(float decay, int count) {
+  return 1.0f / (1.0f - powf(decay, (float)count));
+}
 
 // mu_hat = mu / (1 - b1^t) and nu_hat = nu / (1 - b2^t) as products with the
 // host-side reciprocals (at most one rounding apart from the quotients).
@@ -38,6 +44,12 @@ __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float*
                                                    float* __restrict__ m, float* __restrict__ v, int64_t n,
                                                    int64_t mlp_begin, __nv_bfloat16* __restrict__ shadow,
                                                    int64_t shadow_n, AdamScalars a) {
+  if (a.step != nullptr) {  // a replayed step: this update's scalars from device memory
+    const int count = a.step->count;
+    a.decay = a.step->lr_decay;
+    a.rbc1 = bias_correction_rcp(a.b1, count);
+    a.rbc2 = bias_correction_rcp(a.b2, count);
+  }
   const int64_t n4 = n / 4;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   float sq = 0.f;
@@ -93,14 +105,14 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
   a.b2 = d.b2;
   a.omb1 = (float)(1.0 - (double)d.b1);
   a.omb2 = (float)(1.0 - (double)d.b2);
-  // optax.bias_correction: 1 - decay**count in float32.
-  a.rbc1 = 1.0f / (1.0f - powf(d.b1, (float)d.count));
-  a.rbc2 = 1.0f / (1.0f - powf(d.b2, (float)d.count));
+  a.rbc1 = bias_correction_rcp(d.b1, d.count);
+  a.rbc2 = bias_correction_rcp(d.b2, d.count);
   a.eps = d.eps;
   a.lr_t = d.lr_tensor;
   a.lr_m = d.lr_mlp;
   a.decay = d.lr_decay;
   a.grad_sq = d.grad_sq;
+  a.step = d.device_step;
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n / 4 + 1, 256), (int64_t)blocks_per_sm * device_sms());
   adam_kernel<<<blocks, 256, 0, st>>>(params, grads, mu, nu, n, mlp_begin, shadow, shadow_n, a);
   return check_launch("adam");
@@ -115,6 +127,16 @@ int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t
   const bool sh = shadow != nullptr && lo < shadow_n;
   return launch_adam(params + lo, grads + lo, mu + lo, nu + lo, hi - lo, mlp_begin - lo, d, sh ? shadow + lo : nullptr,
                      sh ? shadow_n - lo : 0, st, blocks_per_sm);
+}
+
+__global__ void adam_set_step_kernel(tvm_adam_step_scalars* step, int32_t count, float lr_decay) {
+  step->count = count;
+  step->lr_decay = lr_decay;
+}
+
+int launch_adam_set_step(tvm_adam_step_scalars* step, int32_t count, float lr_decay, cudaStream_t st) {
+  adam_set_step_kernel<<<1, 1, 0, st>>>(step, count, lr_decay);
+  return check_launch("adam_set_step");
 }
 
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st) {

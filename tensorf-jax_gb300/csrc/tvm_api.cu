@@ -777,7 +777,8 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
   TVM_REQUIRE(params && grads && mu && nu && adam, TVM_ERR_INVALID, "NULL pointer");
   TVM_REQUIRE(aligned(params, 16) && aligned(grads, 16) && aligned(mu, 16) && aligned(nu, 16),
               TVM_ERR_ALIGN, "Adam buffers must be 16-byte aligned");
-  TVM_REQUIRE(adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  TVM_REQUIRE(adam->device_step || adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  TVM_REQUIRE(!adam->device_step || aligned(adam->device_step, 8), TVM_ERR_ALIGN, "device_step must be 8-byte aligned");
   tvm_param_layout L;
   make_layout(*model, L);
   cudaStream_t st = as_stream(stream);
@@ -790,6 +791,13 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
   return launch_adam(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
                      static_cast<float*>(nu), L.total, L.mlp_begin, *adam,
                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0, st);
+}
+
+int tvm_adam_set_step(tvm_adam_step_scalars* device_step, int32_t count, float lr_decay, void* stream) {
+  TVM_REQUIRE(device_step != nullptr, TVM_ERR_INVALID, "device_step is NULL");
+  TVM_REQUIRE(aligned(device_step, 8), TVM_ERR_ALIGN, "device_step must be 8-byte aligned");
+  TVM_REQUIRE(count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  return launch_adam_set_step(device_step, count, lr_decay, as_stream(stream));
 }
 
 int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow, void* stream) {
@@ -885,7 +893,8 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
   TVM_REQUIRE(rays->count == 0 || (colors && loss_out && workspace), TVM_ERR_INVALID, "NULL pointer");
   TVM_REQUIRE(adam_mu && adam_nu && adam, TVM_ERR_INVALID, "NULL pointer");
   TVM_REQUIRE(aligned(adam_mu, 16) && aligned(adam_nu, 16), TVM_ERR_ALIGN, "Adam buffers must be 16-byte aligned");
-  TVM_REQUIRE(adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  TVM_REQUIRE(adam->device_step || adam->count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
+  TVM_REQUIRE(!adam->device_step || aligned(adam->device_step, 8), TVM_ERR_ALIGN, "device_step must be 8-byte aligned");
   cudaStream_t st = as_stream(stream);
   tvm_param_layout L;
   make_layout(*model, L);

@@ -13,7 +13,7 @@ from ctypes import POINTER, c_char_p, c_double, c_float, c_int32, c_int64, c_siz
 PKG_DIR = pathlib.Path(__file__).resolve().parent
 LIB_PATH = PKG_DIR / "libtensorf_gb300.so"
 
-ABI_VERSION = 2  # TVM_ABI_VERSION of include/tensorf_gb300.h
+ABI_VERSION = 3  # TVM_ABI_VERSION of include/tensorf_gb300.h
 TVM_OK = 0
 ERROR_NAMES = {
     -1: "TVM_ERR_INVALID",
@@ -71,7 +71,7 @@ class RenderDesc(ctypes.Structure):
 class AdamDesc(ctypes.Structure):
     _fields_ = [("lr_tensor", c_float), ("lr_mlp", c_float), ("b1", c_float), ("b2", c_float),
                 ("eps", c_float), ("lr_decay", c_float), ("count", c_int32), ("_pad", c_int32),
-                ("grad_sq", c_void_p)]
+                ("grad_sq", c_void_p), ("device_step", c_void_p)]
 
 
 # name -> (restype, argtypes)
@@ -114,6 +114,7 @@ _SIGNATURES = {
                                     POINTER(RenderDesc), c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_adam_step": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, POINTER(AdamDesc),
                                 c_void_p, c_void_p]),
+    "tvm_adam_set_step": (c_int32, [c_void_p, c_int32, c_float, c_void_p]),
     "tvm_refresh_shadow": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p]),
     "tvm_l2_probe": (c_int32, [c_int32, c_void_p, c_size_t, c_int32, c_void_p]),
     "tvm_noise_fill": (c_int32, [c_void_p, c_int64, c_uint64, c_uint64, c_int32, c_void_p]),

@@ -240,14 +240,21 @@ class NoiseKey:
     def split(self) -> Tuple["NoiseKey", "NoiseKey"]:
         return NoiseKey(self.seed, self.stream * 2 + 1), NoiseKey(self.seed, self.stream * 2 + 2)
 
-    def uniform(self, n: int, device="cuda") -> torch.Tensor:
-        out = torch.empty(n, dtype=torch.float32, device=device)
-        _lib.call("tvm_noise_fill", ptr(out), n, self.seed & (2**64 - 1), self.stream & (2**64 - 1), 0, stream_handle())
-        return out
+    def uniform(self, n: int, device="cuda", out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """n uniforms in [0, 1); written into ``out`` (n float32 elements) when given."""
+        return self._fill(n, 0, device, out)
 
-    def gumbel(self, n: int, device="cuda") -> torch.Tensor:
-        out = torch.empty(n, dtype=torch.float32, device=device)
-        _lib.call("tvm_noise_fill", ptr(out), n, self.seed & (2**64 - 1), self.stream & (2**64 - 1), 1, stream_handle())
+    def gumbel(self, n: int, device="cuda", out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """n standard Gumbel draws; written into ``out`` when given."""
+        return self._fill(n, 1, device, out)
+
+    def _fill(self, n: int, kind: int, device, out: Optional[torch.Tensor]) -> torch.Tensor:
+        if out is None:
+            out = torch.empty(n, dtype=torch.float32, device=device)
+        if out.numel() != n or out.dtype != torch.float32 or not out.is_contiguous():
+            raise ValueError(f"noise buffer must be {n} contiguous float32 elements")
+        _lib.call("tvm_noise_fill", ptr(out), n, self.seed & (2**64 - 1), self.stream & (2**64 - 1), kind,
+                  stream_handle())
         return out
 
 
@@ -301,20 +308,24 @@ def init_proposal(grid: int, units: int, gen: torch.Generator) -> Dict[str, torc
 
 
 def draw_noise(key: NoiseKey, rays: int, config: RenderConfig, scene_contraction: bool,
-               proposal: Optional[ProposalConfig] = None) -> RenderNoise:
+               proposal: Optional[ProposalConfig] = None, out: Optional[RenderNoise] = None) -> RenderNoise:
     """Draw the noise render_rays needs from a key: the sample key drives the jitter
     ((N,) shared for bounded scenes, (R, N) for contracted ones, render.py:158-160,
     375-379) and the rgb key the Gumbel noise shared by every ray (render.py:461-469).
     Proposal-guided sampling draws per-ray jitter for both proposal bins and main
-    intervals."""
+    intervals. With ``out`` (the result of an earlier call with the same sizes), the draws
+    overwrite its buffers, whose addresses then stay fixed."""
     sample_key, rgb_key = key.split()
     n = config.density_samples_per_ray
-    gumbel = rgb_key.gumbel(n) if config.mode is RenderMode.RGB else None
+    o = out if out is not None else RenderNoise(None, None, None)
+    flat = lambda t: t.view(-1) if t is not None else None  # noqa: E731
+    gumbel = rgb_key.gumbel(n, out=flat(o.gumbel)) if config.mode is RenderMode.RGB else None
     if proposal is not None:
         k1, k2 = sample_key.split()
-        return RenderNoise(jitter=k1.uniform(rays * n).view(rays, n), gumbel=gumbel,
-                           proposal_jitter=k2.uniform(rays * proposal.samples).view(rays, proposal.samples))
-    jitter = sample_key.uniform(rays * n if scene_contraction else n)
+        return RenderNoise(jitter=k1.uniform(rays * n, out=flat(o.jitter)).view(rays, n), gumbel=gumbel,
+                           proposal_jitter=k2.uniform(rays * proposal.samples,
+                                                      out=flat(o.proposal_jitter)).view(rays, proposal.samples))
+    jitter = sample_key.uniform(rays * n if scene_contraction else n, out=flat(o.jitter))
     if scene_contraction:
         jitter = jitter.view(rays, n)
     return RenderNoise(jitter=jitter, gumbel=gumbel)

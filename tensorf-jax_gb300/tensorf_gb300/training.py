@@ -103,11 +103,36 @@ def sample_counts(grid_dim: int, cfg: TrainConfig) -> Tuple[int, int]:
     return n, k
 
 
+@dataclasses.dataclass
+class _StepGraph:
+    """A training step recorded as a CUDA graph, with the fixed-address buffers it reads:
+    rays, colours and camera indices copied in before each replay, noise drawn into them,
+    the contracted sampler's schedule, and the Adam scalars of the next update."""
+    key: tuple
+    origins: torch.Tensor
+    directions: torch.Tensor
+    colors: torch.Tensor
+    camera_indices: Optional[torch.Tensor]
+    noise: render.RenderNoise
+    schedule: Optional[torch.Tensor]
+    adam_step: torch.Tensor  # tvm_adam_step_scalars: int32 count, float32 lr_decay
+    graph: Optional[torch.cuda.CUDAGraph] = None
+    launches: int = 0        # kernel launches recorded into the graph
+
+
 class TrainState:
     """training.py:19-33 with the training step; mutated in place (the reference
-    donates its state, training.py:101)."""
+    donates its state, training.py:101).
 
-    def __init__(self, config: TrainConfig, learnable_params: render.LearnableParams, seed: int = 94709):
+    The reference jit-compiles its step (training.py:101). The GPU counterpart here is a
+    CUDA graph: with ``cuda_graph`` set, the first step for a batch size runs eagerly on
+    fixed-address input, noise and Adam-scalar buffers and is then recorded once; later
+    steps copy the batch in, draw the step's noise into those buffers, write the update's
+    count and learning-rate decay on the device and replay the graph. Steps given explicit
+    ``noise`` run eagerly."""
+
+    def __init__(self, config: TrainConfig, learnable_params: render.LearnableParams, seed: int = 94709,
+                 cuda_graph: bool = True):
         self.config = config
         self.learnable_params = learnable_params
         self.appearance_mlp = learnable_params.spec.mlp()
@@ -124,6 +149,9 @@ class TrainState:
         self.loss = self._stats[0:1]
         self._ws = None
         self._ws_key = None
+        self.cuda_graph = cuda_graph
+        self._graph: Optional[_StepGraph] = None
+        self.graph_kernel_launches = 0  # kernels run by graph replays (the library counts eager launches)
 
     @staticmethod
     def initialize(config: TrainConfig, spec: render.ModelSpec, seed: int = 94709) -> "TrainState":
@@ -169,6 +197,7 @@ class TrainState:
         self.appearance_mlp = new_spec.mlp()
         self._ws = None
         self._ws_key = None
+        self._graph = None
         return self
 
     def state_dict(self) -> dict:
@@ -221,6 +250,8 @@ class TrainState:
     def training_step(self, rays: cameras.Rays3D, colors: torch.Tensor,
                       noise: Optional[render.RenderNoise] = None, log: bool = True):
         """One step: returns (self, log_data). ``noise`` replaces the key-drawn noise."""
+        if noise is None and self.cuda_graph:
+            return self._graph_step(rays, colors, log)
         cfg = self.render_config()
         r = rays.origins.reshape(-1, 3).shape[0]
         lp = self.learnable_params
@@ -249,5 +280,83 @@ class TrainState:
             log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
                         "train/lr_tensor": adam.lr_decay * self.config.optimizer.lr_init_tensor,
                         "train/lr_mlp": adam.lr_decay * self.config.optimizer.lr_init_mlp,
+                        "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
+        return self, log_data
+
+    def _ensure_workspace(self, md, desc, r: int, cfg) -> None:
+        key = (r, cfg)
+        if self._ws_key != key:
+            nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
+            self._ws = workspace(nbytes, self.learnable_params.params.device)
+            self._ws_key = key
+
+    def _graph_call(self, g: _StepGraph, cfg, r: int) -> None:
+        """tvm_train_step on the graph's fixed buffers, Adam scalars read on the device."""
+        lp = self.learnable_params
+        prop = self.config.proposal
+        desc = render.make_render_desc(cfg, self.aabb, g.noise, r, lp.scene_contraction, g.schedule,
+                                       self.config.density_shift, proposal=prop)
+        md = lp.model_desc()
+        self._ensure_workspace(md, desc, r, cfg)
+        adam = self.adam_desc(1)
+        adam.device_step = g.adam_step.data_ptr()
+        rs = render.rays_struct(cameras.Rays3D(g.origins, g.directions, g.camera_indices))
+        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self.grads),
+                  ptr(self.mu), ptr(self.nu), ctypes.byref(adam), ctypes.byref(rs), ptr(g.colors),
+                  ctypes.byref(desc), ptr(self.loss), ptr(self._ws), self._ws.numel(), stream_handle())
+
+    def _graph_step(self, rays: cameras.Rays3D, colors: torch.Tensor, log: bool):
+        cfg = self.render_config()
+        lp = self.learnable_params
+        prop = self.config.proposal
+        o = rays.origins.reshape(-1, 3)
+        d = rays.directions.reshape(-1, 3)
+        ci = rays.camera_indices
+        r = o.shape[0]
+        key = (r, cfg, self.config, ci is not None, lp.params.data_ptr(), lp.shadow.data_ptr() if lp.shadow is not None
+               else 0, self.grads.data_ptr(), self.mu.data_ptr(), self.nu.data_ptr(), self.loss.data_ptr())
+        g = self._graph
+        fresh = g is None or g.key != key
+        if fresh:
+            dev = lp.params.device
+            sched = render._schedule_for(cfg, lp.scene_contraction, self.schedule(), prop)
+            g = _StepGraph(key=key, origins=torch.empty((r, 3), dtype=torch.float32, device=dev),
+                           directions=torch.empty((r, 3), dtype=torch.float32, device=dev),
+                           colors=torch.empty((r, 3), dtype=torch.float32, device=dev),
+                           camera_indices=torch.empty(r, dtype=torch.int32, device=dev) if ci is not None else None,
+                           noise=render.draw_noise(render.NoiseKey(0), r, cfg, lp.scene_contraction, prop),
+                           schedule=sched, adam_step=torch.zeros(2, dtype=torch.int32, device=dev))
+            self._graph = None
+        render_key, self.prng_key = self.prng_key.split()
+        for dst, src in ((g.origins, o), (g.directions, d), (g.colors, colors.reshape(-1, 3))):
+            if dst.data_ptr() != src.data_ptr():
+                dst.copy_(src)
+        if ci is not None and g.camera_indices.data_ptr() != ci.data_ptr():
+            g.camera_indices.copy_(ci.reshape(-1))
+        render.draw_noise(render_key, r, cfg, lp.scene_contraction, prop, out=g.noise)
+        decay = lr_decay_coeff(self.step, self.config)
+        _lib.call("tvm_adam_set_step", g.adam_step.data_ptr(), self.step + 1, decay, stream_handle())
+        if fresh:
+            # This step runs eagerly on the graph's buffers (the library's one-time setup
+            # happens here, outside any capture); the next ones replay its recording.
+            self._graph_call(g, cfg, r)
+            lib = _lib.load()
+            graph = torch.cuda.CUDAGraph()
+            before = lib.tvm_kernel_launches()
+            with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+                self._graph_call(g, cfg, r)
+            g.launches = int(lib.tvm_kernel_launches() - before)
+            g.graph = graph
+            self._graph = g
+        else:
+            g.graph.replay()
+            self.graph_kernel_launches += g.launches
+        self.step += 1
+        log_data = {}
+        if log:
+            mse, grad_sq = self._stats.tolist()
+            log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
+                        "train/lr_tensor": decay * self.config.optimizer.lr_init_tensor,
+                        "train/lr_mlp": decay * self.config.optimizer.lr_init_mlp,
                         "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
         return self, log_data

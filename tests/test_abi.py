@@ -24,7 +24,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for name in declared_symbols():
         assert hasattr(lib, name), name
-    assert lib.tvm_abi_version() == _lib.ABI_VERSION == 2
+    assert lib.tvm_abi_version() == _lib.ABI_VERSION == 3
 
 
 def _model(**kw):

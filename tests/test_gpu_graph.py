@@ -1,0 +1,129 @@
+"""TrainState with its step recorded as a CUDA graph (the counterpart of the reference's
+jit-compiled step, training.py:101) against the same steps run eagerly.
+
+Both states start from the same parameters and key, so they draw the same noise; the
+graph path reads the Adam scalars from device memory (tvm_adam_set_step) and its batches
+are copied into fixed buffers. After several steps parameters and both moments agree to
+the order of the atomic gradient reductions (FP32: all but a handful of elements to 1e-5;
+BF16, where last-bit differences flip bf16 roundings: no further from the eager run in norm
+than a second eager run is), the logged learning
+rates are equal, the replays ran (and counted) their kernels, and a grid resize records a
+new graph.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _close(x, y, tol=1e-5):
+    """Equal but for a handful of elements whose gradient sums to about zero, which may
+    take the other Adam direction under another reduction order."""
+    x, y = x.double().cpu(), y.double().cpu()
+    off = (x - y).abs() > tol * float(x.abs().max())
+    return int(off.sum()) <= max(8, x.numel() // 100000), int(off.sum())
+
+
+def _dist(x, y):
+    x, y = x.double().cpu(), y.double().cpu()
+    return float((x - y).norm() / x.norm())
+
+
+def _states(cfg, spec, graphs=(False, True)):
+    from tensorf_gb300 import render, training
+    return [training.TrainState(cfg, render.LearnableParams.initialize(spec, seed=4, scene_contraction=cfg.scene_contraction),
+                                seed=7, cuda_graph=g) for g in graphs]
+
+
+def _batches(R, n, seed, contract=False, cams=0):
+    from tensorf_gb300 import cameras, scene
+    out = []
+    for i in range(n):
+        if contract:
+            o, d = scene.unbounded_rays(R, seed + i)
+            c = np.random.default_rng(seed + i).uniform(size=(R, 3))
+        else:
+            o, d, c = scene.sphere_rays(R, seed + i)
+        ci = (torch.arange(R, dtype=torch.int32) % cams).cuda() if cams else None
+        out.append((cameras.Rays3D(torch.tensor(o, dtype=torch.float32).cuda(),
+                                   torch.tensor(d, dtype=torch.float32).cuda(), ci),
+                    torch.tensor(c, dtype=torch.float32).cuda()))
+    return out
+
+
+@pytest.mark.parametrize("case", ["bounded", "proposal_bf16", "contracted_cameras"])
+def test_graph_steps_match_eager_steps(case):
+    from tensorf_gb300 import render, training
+    kw = dict(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
+              appearance_samples_per_ray=8, density_shift=-1.0, n_iters=20, upsamp_iters=(3,))
+    spec = render.ModelSpec(grid_dim=24)
+    contract, cams = False, 0
+    if case == "proposal_bf16":
+        kw.update(density_samples_per_ray=32, proposal=render.ProposalConfig(samples=32))
+        spec = render.ModelSpec(grid_dim=24, precision="bf16", proposal_grid=16)
+    if case == "contracted_cameras":
+        kw.update(initial_aabb_min=(-2.0,) * 3, initial_aabb_max=(2.0,) * 3, scene_contraction=True)
+        spec = render.ModelSpec(grid_dim=24, num_cameras=3)
+        contract, cams = True, 3
+    cfg = training.TrainConfig(**kw)
+    bf16 = spec.precision == "bf16"
+    # BF16: a last-bit difference in a master weight (another reduction order) can flip the
+    # rounding of its bf16 copy, which every later gather reads, so any two runs drift apart
+    # element by element; a second eager run measures how far, and the graph run may not
+    # drift further from the first.
+    states = _states(cfg, spec, (False, True, False) if bf16 else (False, True))
+    eager, graph = states[0], states[1]
+    batches = _batches(256, 6, 11, contract, cams)
+    for rays, colors in batches:
+        logs = [st.training_step(rays, colors)[1] for st in states]
+        la, lb = logs[0], logs[1]
+        assert la["train/lr_tensor"] == lb["train/lr_tensor"] and la["train/lr_mlp"] == lb["train/lr_mlp"]
+        assert lb["train/mse"] == pytest.approx(la["train/mse"], rel=1e-3 if bf16 else 1e-4)
+    torch.cuda.synchronize()
+    assert eager.step == graph.step == 6
+    assert graph._graph is not None and graph.graph_kernel_launches >= 5 * graph._graph.launches > 0
+    for name in ("params", "mu", "nu"):
+        get = (lambda st: st.learnable_params.params) if name == "params" else (lambda st: getattr(st, name))
+        if bf16:
+            d_graph, d_eager = _dist(get(eager), get(graph)), _dist(get(eager), get(states[2]))
+            assert d_graph <= 3.0 * d_eager + 1e-6, (name, d_graph, d_eager)
+        else:
+            ok, n_off = _close(get(eager), get(graph))
+            assert ok, (name, n_off)
+    assert float(graph.grads.abs().max()) == 0.0
+
+
+def test_graph_recorded_again_after_resize():
+    from tensorf_gb300 import render, training
+    cfg = training.TrainConfig(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
+                               appearance_samples_per_ray=8, density_shift=-1.0, n_iters=20, upsamp_iters=(2,))
+    eager, graph = _states(cfg, render.ModelSpec(grid_dim=16))
+    batches = _batches(128, 5, 3)
+    for i, (rays, colors) in enumerate(batches):
+        if i == 2:
+            for st in (eager, graph):
+                st.resize_grid(24)
+        eager.training_step(rays, colors, log=False)
+        graph.training_step(rays, colors, log=False)
+    torch.cuda.synchronize()
+    assert graph.learnable_params.spec.grid_dim == 24 and graph._graph.key[4] == graph.learnable_params.params.data_ptr()
+    ok, n_off = _close(eager.learnable_params.params, graph.learnable_params.params)
+    assert ok, n_off
+
+
+def test_explicit_noise_runs_eagerly():
+    from tensorf_gb300 import render, training
+    cfg = training.TrainConfig(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=32,
+                               appearance_samples_per_ray=8, density_shift=-1.0)
+    st = training.TrainState.initialize(cfg, render.ModelSpec(grid_dim=16))
+    (rays, colors), = _batches(64, 1, 5)
+    rng = np.random.default_rng(0)
+    noise = render.RenderNoise(torch.tensor(rng.uniform(size=32), dtype=torch.float32).cuda(),
+                               torch.tensor(-np.log(-np.log(rng.uniform(1e-7, 1, size=32))),
+                                            dtype=torch.float32).cuda())
+    st.training_step(rays, colors, noise=noise)
+    assert st._graph is None and st.step == 1
+    assert dataclasses.is_dataclass(st.config)
