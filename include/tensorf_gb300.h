@@ -167,13 +167,14 @@ typedef struct {
   float proposal_loss_weight;    /* weight of the proposal bound loss (training) */
 } tvm_render_desc;
 
-/* The per-update Adam scalars in device memory, for training steps recorded once as a
- * CUDA graph and replayed: the host writes the next update's values with
- * tvm_adam_set_step on the replay stream before each replay. */
+/* The per-step scalars in device memory, for training steps recorded once as a CUDA
+ * graph and replayed: the host writes the next step's values with tvm_set_step_scalars
+ * on the replay stream before each replay, and the recorded kernels read them. */
 typedef struct {
-  int32_t count;    /* step count after increment: 1 on the first update */
-  float lr_decay;   /* multiplier from the exponential decay (training.py:158-181) */
-} tvm_adam_step_scalars;
+  int32_t count;         /* Adam step count after increment: 1 on the first update */
+  float lr_decay;        /* multiplier from the exponential decay (training.py:158-181) */
+  uint64_t noise_stream; /* stream id of the step's noise key (see tvm_noise_fill_keyed) */
+} tvm_step_scalars;
 
 /* Adam hyper-parameters (training.py:207-243; optax.scale_by_adam). */
 typedef struct {
@@ -186,7 +187,7 @@ typedef struct {
   float* grad_sq;   /* optional device float, or NULL: overwritten with the sum of the squared
                        gradients the update consumed, the square of optax.global_norm(grads)
                        that training_step logs as grad_norm (training.py:190-196) */
-  const tvm_adam_step_scalars* device_step; /* optional device struct, or NULL: when set, the
+  const tvm_step_scalars* device_step; /* optional device struct, or NULL: when set, the
                        update reads count and lr_decay from it when it runs (the host fields
                        are then not used), so a recorded step can be replayed */
 } tvm_adam_desc;
@@ -391,11 +392,12 @@ TVM_API int tvm_loss_f64(const tvm_model_desc* model, const void* params, const 
  * non-NULL (TVM_BF16) the field segments are rounded into it. */
 TVM_API int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* mu, void* nu,
                   const tvm_adam_desc* adam, void* shadow, void* stream);
-/* Write count and lr_decay into a device tvm_adam_step_scalars, ordered on `stream`
- * (one single-thread kernel: the values travel as launch arguments, so the host may
- * reuse its variables at once). No counterpart in the reference, whose jitted step takes
- * its optimizer state as traced arrays. */
-TVM_API int tvm_adam_set_step(tvm_adam_step_scalars* device_step, int32_t count, float lr_decay, void* stream);
+/* Write a step's scalars into a device tvm_step_scalars, ordered on `stream` (one
+ * single-thread kernel: the values travel as launch arguments, so the host may reuse its
+ * variables at once). No counterpart in the reference, whose jitted step takes its
+ * optimizer state and key as traced arrays. */
+TVM_API int tvm_set_step_scalars(tvm_step_scalars* device_step, int32_t count, float lr_decay,
+                                 uint64_t noise_stream, void* stream);
 /* Round the field segments of params into the bf16 shadow (after init / load). */
 TVM_API int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow,
                        void* stream);
@@ -414,6 +416,12 @@ TVM_API int tvm_l2_probe(int32_t kind, void* buf, size_t bytes, int32_t passes, 
  * (seed, stream_id, i). */
 TVM_API int tvm_noise_fill(float* dst, int64_t n, uint64_t seed, uint64_t stream_id, int32_t kind,
                    void* stream);
+/* tvm_noise_fill with the stream id read on the device when the kernel runs:
+ * stream_id = step->noise_stream * mul + add (mod 2^64). A key split k -> (2k+1, 2k+2)
+ * is a (mul, add) pair, so the draws of a recorded step follow the key the host writes
+ * into `step` before each replay. */
+TVM_API int tvm_noise_fill_keyed(float* dst, int64_t n, uint64_t seed, const tvm_step_scalars* step,
+                                 uint64_t mul, uint64_t add, int32_t kind, void* stream);
 /* Pinhole rays of one camera (cameras.py:100-143): K (3x3 row-major), R_wc (3x3),
  * t_wc (3): origins/directions (H*W, 3) float32, pixel (v, u) row-major. The
  * pixel subset `pixels` (n indices into H*W) may be NULL for the full frame. */

@@ -18,7 +18,7 @@ namespace tvm {
 struct AdamScalars {
   float b1, b2, omb1, omb2, rbc1, rbc2, eps, lr_t, lr_m, decay;
   float* grad_sq;  // accumulates the sum of g^2 when non-null
-  const tvm_adam_step_scalars* step;  // when non-null: count and decay are read from it
+  const tvm_step_scalars* step;  // when non-null: count and decay are read from it
 };
 
 // optax.bias_correction: 1 / (1 - decay**count) in float32.
@@ -129,14 +129,17 @@ int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t
                      sh ? shadow_n - lo : 0, st, blocks_per_sm);
 }
 
-__global__ void adam_set_step_kernel(tvm_adam_step_scalars* step, int32_t count, float lr_decay) {
+__global__ void set_step_scalars_kernel(tvm_step_scalars* step, int32_t count, float lr_decay,
+                                        uint64_t noise_stream) {
   step->count = count;
   step->lr_decay = lr_decay;
+  step->noise_stream = noise_stream;
 }
 
-int launch_adam_set_step(tvm_adam_step_scalars* step, int32_t count, float lr_decay, cudaStream_t st) {
-  adam_set_step_kernel<<<1, 1, 0, st>>>(step, count, lr_decay);
-  return check_launch("adam_set_step");
+int launch_set_step_scalars(tvm_step_scalars* step, int32_t count, float lr_decay, uint64_t noise_stream,
+                            cudaStream_t st) {
+  set_step_scalars_kernel<<<1, 1, 0, st>>>(step, count, lr_decay, noise_stream);
+  return check_launch("set_step_scalars");
 }
 
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st) {

@@ -793,11 +793,12 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0, st);
 }
 
-int tvm_adam_set_step(tvm_adam_step_scalars* device_step, int32_t count, float lr_decay, void* stream) {
+int tvm_set_step_scalars(tvm_step_scalars* device_step, int32_t count, float lr_decay, uint64_t noise_stream,
+                         void* stream) {
   TVM_REQUIRE(device_step != nullptr, TVM_ERR_INVALID, "device_step is NULL");
   TVM_REQUIRE(aligned(device_step, 8), TVM_ERR_ALIGN, "device_step must be 8-byte aligned");
   TVM_REQUIRE(count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
-  return launch_adam_set_step(device_step, count, lr_decay, as_stream(stream));
+  return launch_set_step_scalars(device_step, count, lr_decay, noise_stream, as_stream(stream));
 }
 
 int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow, void* stream) {

@@ -164,6 +164,7 @@ int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t
                       const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
                       int blocks_per_sm = 8);
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
-int launch_adam_set_step(tvm_adam_step_scalars* step, int32_t count, float lr_decay, cudaStream_t st);
+int launch_set_step_scalars(tvm_step_scalars* step, int32_t count, float lr_decay, uint64_t noise_stream,
+                            cudaStream_t st);
 
 }  // namespace tvm

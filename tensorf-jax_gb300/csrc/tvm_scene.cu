@@ -14,7 +14,10 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-__global__ void noise_kernel(float* __restrict__ dst, int64_t n, uint64_t seed, uint64_t sid, int kind) {
+// step (optional): the stream id is step->noise_stream * mul + add, read when it runs.
+__global__ void noise_kernel(float* __restrict__ dst, int64_t n, uint64_t seed, uint64_t sid, int kind,
+                             const tvm_step_scalars* __restrict__ step, uint64_t mul) {
+  if (step != nullptr) sid = step->noise_stream * mul + sid;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const uint64_t key = mix64(seed ^ mix64(sid + 0x9E3779B97F4A7C15ull));
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -136,7 +139,19 @@ int tvm_noise_fill(float* dst, int64_t n, uint64_t seed, uint64_t stream_id, int
   if (n == 0) return TVM_OK;
   TVM_REQUIRE(dst != nullptr, TVM_ERR_INVALID, "dst is NULL");
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
-  noise_kernel<<<blocks, 256, 0, as_stream(stream)>>>(dst, n, seed, stream_id, kind);
+  noise_kernel<<<blocks, 256, 0, as_stream(stream)>>>(dst, n, seed, stream_id, kind, nullptr, 0);
+  return check_launch("noise_fill");
+}
+
+int tvm_noise_fill_keyed(float* dst, int64_t n, uint64_t seed, const tvm_step_scalars* step, uint64_t mul,
+                         uint64_t add, int32_t kind, void* stream) {
+  TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
+  TVM_REQUIRE(kind == 0 || kind == 1, TVM_ERR_INVALID, "kind must be 0 (uniform) or 1 (gumbel)");
+  if (n == 0) return TVM_OK;
+  TVM_REQUIRE(dst != nullptr && step != nullptr, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(step, 8), TVM_ERR_ALIGN, "step must be 8-byte aligned");
+  const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
+  noise_kernel<<<blocks, 256, 0, as_stream(stream)>>>(dst, n, seed, add, kind, step, mul);
   return check_launch("noise_fill");
 }
 

@@ -114,7 +114,8 @@ _SIGNATURES = {
                                     POINTER(RenderDesc), c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_adam_step": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, POINTER(AdamDesc),
                                 c_void_p, c_void_p]),
-    "tvm_adam_set_step": (c_int32, [c_void_p, c_int32, c_float, c_void_p]),
+    "tvm_set_step_scalars": (c_int32, [c_void_p, c_int32, c_float, c_uint64, c_void_p]),
+    "tvm_noise_fill_keyed": (c_int32, [c_void_p, c_int64, c_uint64, c_void_p, c_uint64, c_uint64, c_int32, c_void_p]),
     "tvm_refresh_shadow": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p]),
     "tvm_l2_probe": (c_int32, [c_int32, c_void_p, c_size_t, c_int32, c_void_p]),
     "tvm_noise_fill": (c_int32, [c_void_p, c_int64, c_uint64, c_uint64, c_int32, c_void_p]),

@@ -331,6 +331,28 @@ def draw_noise(key: NoiseKey, rays: int, config: RenderConfig, scene_contraction
     return RenderNoise(jitter=jitter, gumbel=gumbel)
 
 
+def draw_noise_keyed(seed: int, step_scalars: torch.Tensor, rays: int, config: RenderConfig,
+                     proposal: Optional[ProposalConfig], out: RenderNoise) -> None:
+    """draw_noise(NoiseKey(seed, s), ...) into ``out``'s buffers, with the key's stream id
+    s read on the device from ``step_scalars`` (a tvm_step_scalars written by
+    tvm_set_step_scalars) when the kernels run. draw_noise's key splits are affine in s
+    (split: s -> 2s+1, 2s+2), so each draw is one (mul, add) pair; a recorded training
+    step therefore replays each step's own noise."""
+    sp = step_scalars.data_ptr()
+
+    def fill(buf: torch.Tensor, mul: int, add: int, kind: int) -> None:
+        _lib.call("tvm_noise_fill_keyed", ptr(buf), buf.numel(), seed & (2**64 - 1), sp, mul, add, kind,
+                  stream_handle())
+
+    if config.mode is RenderMode.RGB:
+        fill(out.gumbel, 2, 2, 1)           # rgb key 2s+2
+    if proposal is not None:
+        fill(out.jitter, 4, 3, 0)           # sample key 2s+1, split: 4s+3
+        fill(out.proposal_jitter, 4, 4, 0)  # and 4s+4
+    else:
+        fill(out.jitter, 2, 1, 0)           # sample key 2s+1
+
+
 # ---------------------------------------------------------------------------------
 # Descriptors.
 # ---------------------------------------------------------------------------------

@@ -106,8 +106,9 @@ def sample_counts(grid_dim: int, cfg: TrainConfig) -> Tuple[int, int]:
 @dataclasses.dataclass
 class _StepGraph:
     """A training step recorded as a CUDA graph, with the fixed-address buffers it reads:
-    rays, colours and camera indices copied in before each replay, noise drawn into them,
-    the contracted sampler's schedule, and the Adam scalars of the next update."""
+    rays, colours and camera indices copied in before each replay, the noise buffers the
+    recorded draws fill, the contracted sampler's schedule, and the step scalars (Adam
+    count and learning-rate decay, the noise key's stream id) of the next step."""
     key: tuple
     origins: torch.Tensor
     directions: torch.Tensor
@@ -115,9 +116,9 @@ class _StepGraph:
     camera_indices: Optional[torch.Tensor]
     noise: render.RenderNoise
     schedule: Optional[torch.Tensor]
-    adam_step: torch.Tensor  # tvm_adam_step_scalars: int32 count, float32 lr_decay
+    step_scalars: torch.Tensor  # tvm_step_scalars: int32 count, float32 lr_decay, uint64 noise stream
     graph: Optional[torch.cuda.CUDAGraph] = None
-    launches: int = 0        # kernel launches recorded into the graph
+    launches: int = 0           # kernel launches recorded into the graph
 
 
 class TrainState:
@@ -126,10 +127,10 @@ class TrainState:
 
     The reference jit-compiles its step (training.py:101). The GPU counterpart here is a
     CUDA graph: with ``cuda_graph`` set, the first step for a batch size runs eagerly on
-    fixed-address input, noise and Adam-scalar buffers and is then recorded once; later
-    steps copy the batch in, draw the step's noise into those buffers, write the update's
-    count and learning-rate decay on the device and replay the graph. Steps given explicit
-    ``noise`` run eagerly."""
+    fixed-address input, noise and step-scalar buffers and is then recorded once, noise
+    draws included; later steps copy the batch in, write the step's Adam count,
+    learning-rate decay and noise key into device memory and replay the graph. Steps
+    given explicit ``noise`` run eagerly."""
 
     def __init__(self, config: TrainConfig, learnable_params: render.LearnableParams, seed: int = 94709,
                  cuda_graph: bool = True):
@@ -298,8 +299,9 @@ class TrainState:
                                        self.config.density_shift, proposal=prop)
         md = lp.model_desc()
         self._ensure_workspace(md, desc, r, cfg)
+        render.draw_noise_keyed(self.prng_key.seed, g.step_scalars, r, cfg, prop, g.noise)
         adam = self.adam_desc(1)
-        adam.device_step = g.adam_step.data_ptr()
+        adam.device_step = g.step_scalars.data_ptr()
         rs = render.rays_struct(cameras.Rays3D(g.origins, g.directions, g.camera_indices))
         _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self.grads),
                   ptr(self.mu), ptr(self.nu), ctypes.byref(adam), ctypes.byref(rs), ptr(g.colors),
@@ -314,7 +316,8 @@ class TrainState:
         ci = rays.camera_indices
         r = o.shape[0]
         key = (r, cfg, self.config, ci is not None, lp.params.data_ptr(), lp.shadow.data_ptr() if lp.shadow is not None
-               else 0, self.grads.data_ptr(), self.mu.data_ptr(), self.nu.data_ptr(), self.loss.data_ptr())
+               else 0, self.grads.data_ptr(), self.mu.data_ptr(), self.nu.data_ptr(), self.loss.data_ptr(),
+               self.prng_key.seed)
         g = self._graph
         fresh = g is None or g.key != key
         if fresh:
@@ -325,7 +328,7 @@ class TrainState:
                            colors=torch.empty((r, 3), dtype=torch.float32, device=dev),
                            camera_indices=torch.empty(r, dtype=torch.int32, device=dev) if ci is not None else None,
                            noise=render.draw_noise(render.NoiseKey(0), r, cfg, lp.scene_contraction, prop),
-                           schedule=sched, adam_step=torch.zeros(2, dtype=torch.int32, device=dev))
+                           schedule=sched, step_scalars=torch.zeros(2, dtype=torch.int64, device=dev))
             self._graph = None
         render_key, self.prng_key = self.prng_key.split()
         for dst, src in ((g.origins, o), (g.directions, d), (g.colors, colors.reshape(-1, 3))):
@@ -333,12 +336,13 @@ class TrainState:
                 dst.copy_(src)
         if ci is not None and g.camera_indices.data_ptr() != ci.data_ptr():
             g.camera_indices.copy_(ci.reshape(-1))
-        render.draw_noise(render_key, r, cfg, lp.scene_contraction, prop, out=g.noise)
         decay = lr_decay_coeff(self.step, self.config)
-        _lib.call("tvm_adam_set_step", g.adam_step.data_ptr(), self.step + 1, decay, stream_handle())
+        _lib.call("tvm_set_step_scalars", g.step_scalars.data_ptr(), self.step + 1, decay,
+                  render_key.stream & (2**64 - 1), stream_handle())
         if fresh:
             # This step runs eagerly on the graph's buffers (the library's one-time setup
-            # happens here, outside any capture); the next ones replay its recording.
+            # happens here, outside any capture); the next ones replay its recording, the
+            # noise draws included.
             self._graph_call(g, cfg, r)
             lib = _lib.load()
             graph = torch.cuda.CUDAGraph()

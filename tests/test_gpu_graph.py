@@ -2,8 +2,8 @@
 jit-compiled step, training.py:101) against the same steps run eagerly.
 
 Both states start from the same parameters and key, so they draw the same noise; the
-graph path reads the Adam scalars from device memory (tvm_adam_set_step) and its batches
-are copied into fixed buffers. After several steps parameters and both moments agree to
+graph path reads the Adam scalars and the noise key from device memory
+(tvm_set_step_scalars) and its batches are copied into fixed buffers. After several steps parameters and both moments agree to
 the order of the atomic gradient reductions (FP32: all but a handful of elements to 1e-5;
 BF16, where last-bit differences flip bf16 roundings: no further from the eager run in norm
 than a second eager run is), the logged learning
@@ -127,3 +127,25 @@ def test_explicit_noise_runs_eagerly():
     st.training_step(rays, colors, noise=noise)
     assert st._graph is None and st.step == 1
     assert dataclasses.is_dataclass(st.config)
+
+
+@pytest.mark.parametrize("proposal", [False, True])
+def test_keyed_noise_equals_key_drawn_noise(proposal):
+    """tvm_noise_fill_keyed with the key's stream id in device memory draws bit for bit
+    what draw_noise draws from the key on the host, including stream ids past 2^63."""
+    from tensorf_gb300 import _lib, render
+    from tensorf_gb300._util import stream_handle
+    R = 100
+    cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, 24, 4)
+    prop = render.ProposalConfig(samples=16) if proposal else None
+    scal = torch.zeros(2, dtype=torch.int64, device="cuda")
+    for stream in (0, 5, 2**63 + 12345):
+        key = render.NoiseKey(77, stream)
+        want = render.draw_noise(key, R, cfg, False, prop)
+        got = render.draw_noise(render.NoiseKey(0), R, cfg, False, prop)
+        _lib.call("tvm_set_step_scalars", scal.data_ptr(), 1, 1.0, stream & (2**64 - 1), stream_handle())
+        render.draw_noise_keyed(77, scal, R, cfg, prop, got)
+        for a, b in ((want.jitter, got.jitter), (want.gumbel, got.gumbel), (want.proposal_jitter, got.proposal_jitter)):
+            assert (a is None) == (b is None)
+            if a is not None:
+                assert torch.equal(a, b)
