@@ -238,15 +238,17 @@ def time_train(state, data, steps, warmup, phases=True, start_step=0):
     """Warm-up, then `steps` timed steps on device-resident batches. Returns (ms total,
     per-phase mean ms, kernel launches: the library's eager launches plus the kernels of
     the replayed CUDA graphs). A phase pass runs the steps eagerly: phase events are
-    recorded by the library as it launches."""
+    recorded by the library as it launches, and it applies each step's whole Adam update
+    inside that step."""
     import ctypes
 
     from tensorf_gb300 import _lib
 
     lib = _lib.load()
-    graph_was = state.cuda_graph
-    if phases:
+    graph_was, defer_was = state.cuda_graph, state.defer_field_updates
+    if phases:  # every kernel of a step inside its own phases
         state.cuda_graph = False
+        state.defer_field_updates = False
     for i in range(warmup):
         r, c = data.batch(start_step + i)
         state.training_step(r, c, log=False)
@@ -270,7 +272,7 @@ def time_train(state, data, steps, warmup, phases=True, start_step=0):
     _lib.call("tvm_set_phase_events", None, 0)
     end.record()
     torch.cuda.synchronize()
-    state.cuda_graph = graph_was
+    state.cuda_graph, state.defer_field_updates = graph_was, defer_was
     launches = int(lib.tvm_kernel_launches() - l0) + int(state.graph_kernel_launches - g0)
     phase_ms = {}
     if phases:

@@ -174,6 +174,9 @@ typedef struct {
   int32_t count;         /* Adam step count after increment: 1 on the first update */
   float lr_decay;        /* multiplier from the exponential decay (training.py:158-181) */
   uint64_t noise_stream; /* stream id of the step's noise key (see tvm_noise_fill_keyed) */
+  int32_t pending_count; /* the field update the previous step left pending (tvm_adam_desc.
+                            defer_fields): its count, or 0 for none */
+  float pending_lr_decay;/* and its learning-rate decay */
 } tvm_step_scalars;
 
 /* Adam hyper-parameters (training.py:207-243; optax.scale_by_adam). */
@@ -183,13 +186,23 @@ typedef struct {
   float b1, b2, eps;/* 0.9, 0.99, 1e-8 */
   float lr_decay;   /* multiplier from the exponential decay (training.py:158-181) */
   int32_t count;    /* step count after increment: 1 on the first update */
-  int32_t _pad;
+  int32_t defer_fields; /* tvm_train_step only. 1: leave this step's update of the density and
+                       appearance fields (their parameters, moments and the gradients it
+                       would consume and zero) pending; the next tvm_train_step applies it
+                       first, beside its own start, or tvm_apply_pending_fields does.
+                       Nothing reads those segments in between, so the result is the same
+                       as updating at once. The fields' gradients are then not counted in
+                       grad_sq. */
   float* grad_sq;   /* optional device float, or NULL: overwritten with the sum of the squared
                        gradients the update consumed, the square of optax.global_norm(grads)
                        that training_step logs as grad_norm (training.py:190-196) */
   const tvm_step_scalars* device_step; /* optional device struct, or NULL: when set, the
-                       update reads count and lr_decay from it when it runs (the host fields
-                       are then not used), so a recorded step can be replayed */
+                       update reads count, lr_decay and the pending update's scalars from it
+                       when it runs (the host fields are then not used), so a recorded step
+                       can be replayed */
+  int32_t pending_count;   /* tvm_train_step with device_step NULL: the count of a field
+                              update the previous call left pending, or 0 for none */
+  float pending_lr_decay;  /* and its learning-rate decay */
 } tvm_adam_desc;
 
 /* ---- library ---------------------------------------------------------------------- */
@@ -348,7 +361,10 @@ TVM_API int tvm_render_fwd(const tvm_model_desc* model, const void* params, cons
 /* TrainState.training_step (training.py:101-205): render (RGB mode), MSE loss against
  * colors (R, 3), backward, Adam update of params/mu/nu (flat layout), refresh of the
  * bf16 shadow (TVM_BF16), grads zeroed for the next step. loss_out: device float,
- * written with the MSE. grads must be zero on entry (they are left zero). */
+ * written with the MSE. grads must be zero on entry (they are left zero), except for
+ * the field segments of a pending update (adam->pending_count or device_step), which
+ * this call applies first: on a side stream, with the forward's density and appearance
+ * kernels waiting for it. adam->defer_fields leaves this step's field update pending. */
 TVM_API size_t tvm_train_workspace_size(const tvm_model_desc* model, const tvm_render_desc* cfg,
                                 int64_t rays);
 TVM_API int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void* grads,
@@ -397,7 +413,13 @@ TVM_API int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads
  * variables at once). No counterpart in the reference, whose jitted step takes its
  * optimizer state and key as traced arrays. */
 TVM_API int tvm_set_step_scalars(tvm_step_scalars* device_step, int32_t count, float lr_decay,
-                                 uint64_t noise_stream, void* stream);
+                                 uint64_t noise_stream, int32_t pending_count, float pending_lr_decay,
+                                 void* stream);
+/* Apply a field update that tvm_train_step left pending (defer_fields): Adam over the
+ * density and appearance field segments with adam->pending_count and
+ * adam->pending_lr_decay, their gradients zeroed, their bf16 shadow refreshed. */
+TVM_API int tvm_apply_pending_fields(const tvm_model_desc* model, void* params, void* shadow, void* grads,
+                                     void* mu, void* nu, const tvm_adam_desc* adam, void* stream);
 /* Round the field segments of params into the bf16 shadow (after init / load). */
 TVM_API int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow,
                        void* stream);

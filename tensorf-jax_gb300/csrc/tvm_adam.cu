@@ -19,6 +19,7 @@ struct AdamScalars {
   float b1, b2, omb1, omb2, rbc1, rbc2, eps, lr_t, lr_m, decay;
   float* grad_sq;  // accumulates the sum of g^2 when non-null
   const tvm_step_scalars* step;  // when non-null: count and decay are read from it
+  int pending;                   // read the pending update's scalars from `step` instead
 };
 
 // optax.bias_correction: 1 / (1 - decay**count) in float32.
@@ -45,8 +46,9 @@ __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float*
                                                    int64_t mlp_begin, __nv_bfloat16* __restrict__ shadow,
                                                    int64_t shadow_n, AdamScalars a) {
   if (a.step != nullptr) {  // a replayed step: this update's scalars from device memory
-    const int count = a.step->count;
-    a.decay = a.step->lr_decay;
+    const int count = a.pending ? a.step->pending_count : a.step->count;
+    if (count <= 0) return;  // no pending update (the host applied it already)
+    a.decay = a.pending ? a.step->pending_lr_decay : a.step->lr_decay;
     a.rbc1 = bias_correction_rcp(a.b1, count);
     a.rbc2 = bias_correction_rcp(a.b2, count);
   }
@@ -85,8 +87,17 @@ __global__ void __launch_bounds__(256) adam_kernel(float* __restrict__ p, float*
     if (shadow != nullptr && e < shadow_n) shadow[e] = __float2bfloat16_rn(p[e]);
   }
   if (a.grad_sq != nullptr) {  // every thread of the block reaches this point
+    // One reduction per block into the single word: per-warp reductions to one address
+    // serialise in L2.
+    __shared__ float warp_sq[8];
     sq = warp_sum(sq);
-    if ((threadIdx.x & 31) == 0 && sq != 0.f) atomicAdd(a.grad_sq, sq);
+    if ((threadIdx.x & 31) == 0) warp_sq[threadIdx.x >> 5] = sq;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += warp_sq[w];
+      if (t != 0.f) atomicAdd(a.grad_sq, t);
+    }
   }
 }
 
@@ -98,7 +109,8 @@ __global__ void shadow_kernel(const float* __restrict__ src, __nv_bfloat16* __re
 }
 
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
-                const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st, int blocks_per_sm) {
+                const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st, int blocks_per_sm,
+                bool pending) {
   if (n == 0) return TVM_OK;
   AdamScalars a;
   a.b1 = d.b1;
@@ -113,6 +125,7 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
   a.decay = d.lr_decay;
   a.grad_sq = d.grad_sq;
   a.step = d.device_step;
+  a.pending = pending ? 1 : 0;
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n / 4 + 1, 256), (int64_t)blocks_per_sm * device_sms());
   adam_kernel<<<blocks, 256, 0, st>>>(params, grads, mu, nu, n, mlp_begin, shadow, shadow_n, a);
   return check_launch("adam");
@@ -120,25 +133,19 @@ int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, in
 
 int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
                       const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
-                      int blocks_per_sm) {
+                      int blocks_per_sm, bool pending) {
   if (hi <= lo) return TVM_OK;
   // lo is a segment start (a multiple of 64 elements), so the offset buffers keep their
   // 16-byte alignment and the kernel's float4 lanes stay whole.
   const bool sh = shadow != nullptr && lo < shadow_n;
   return launch_adam(params + lo, grads + lo, mu + lo, nu + lo, hi - lo, mlp_begin - lo, d, sh ? shadow + lo : nullptr,
-                     sh ? shadow_n - lo : 0, st, blocks_per_sm);
+                     sh ? shadow_n - lo : 0, st, blocks_per_sm, pending);
 }
 
-__global__ void set_step_scalars_kernel(tvm_step_scalars* step, int32_t count, float lr_decay,
-                                        uint64_t noise_stream) {
-  step->count = count;
-  step->lr_decay = lr_decay;
-  step->noise_stream = noise_stream;
-}
+__global__ void set_step_scalars_kernel(tvm_step_scalars* step, tvm_step_scalars v) { *step = v; }
 
-int launch_set_step_scalars(tvm_step_scalars* step, int32_t count, float lr_decay, uint64_t noise_stream,
-                            cudaStream_t st) {
-  set_step_scalars_kernel<<<1, 1, 0, st>>>(step, count, lr_decay, noise_stream);
+int launch_set_step_scalars(tvm_step_scalars* step, const tvm_step_scalars& v, cudaStream_t st) {
+  set_step_scalars_kernel<<<1, 1, 0, st>>>(step, v);
   return check_launch("set_step_scalars");
 }
 

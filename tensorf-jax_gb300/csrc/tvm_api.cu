@@ -81,10 +81,14 @@ int ensure_smem_limit(const void* fn, int bytes, const char* what) {
 //    depend only on the forward, run there beside the main field's backward;
 //  - `branch` (highest priority): the appearance branch of the backward (FeatureMlp
 //    backward, appearance scatter, their update), the longer of the two chains that
-//    follow the loss, runs there while the caller's stream runs the density branch.
+//    follow the loss, runs there while the caller's stream runs the density branch; at
+//    the start of a training step, the field update the previous step left pending runs
+//    there too, beside the proposal forward, and the density and appearance gathers wait
+//    for its two halves.
 struct SideStream {
   cudaStream_t stream = nullptr, branch = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
+  cudaEvent_t fork3 = nullptr, density_ready = nullptr, appearance_ready = nullptr;
 };
 
 static int side_stream(SideStream*& out) {
@@ -97,7 +101,7 @@ static int side_stream(SideStream*& out) {
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, least);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.branch, cudaStreamNonBlocking, greatest);
-    for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2})
+    for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2, &s.fork3, &s.density_ready, &s.appearance_ready})
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "side stream: %s", cudaGetErrorString(e));
   }
@@ -379,7 +383,25 @@ struct AdamPlan {
   tvm_adam_desc desc;
   __nv_bfloat16* shadow;  // BF16 models: the field shadow, refreshed with the update
   int64_t shadow_n;
+  bool pending;           // apply the previous step's pending field update first
+  bool defer;             // leave this step's field update pending
 };
+
+// The density and appearance fields' segments of the flat layout: [0, fields_end).
+static int64_t fields_end(const tvm_model_desc& m, const tvm_param_layout& L) {
+  return m.proposal_grid > 0 ? L.proposal_lines : L.mlp_begin;
+}
+
+// The scalars of a pending field update: the caller's pending count and decay, or (a
+// replayed step) those the kernels read from device_step.
+static tvm_adam_desc pending_desc(const tvm_adam_desc& d) {
+  tvm_adam_desc p = d;
+  p.count = d.pending_count;
+  p.lr_decay = d.pending_lr_decay;
+  p.grad_sq = nullptr;  // the previous step's gradients: not this step's norm
+  p.defer_fields = 0;
+  return p;
+}
 
 // render_rays forward, and (if grads != null) the loss and backward of training_step,
 // and (if adam != null) the step's Adam update.
@@ -400,6 +422,33 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   const bool proposal = c.sampler == TVM_SAMPLER_PROPOSAL;
   const SamplerArgs sp = proposal ? proposal_sampler(c) : SamplerArgs{};
   const float* edges = (proposal && c.contract) ? c.schedule : nullptr;
+  // The field update the previous step left pending (tvm_adam_desc.defer_fields). Nothing
+  // before the density gathers reads the field segments, so it runs beside the start of
+  // this pass on the branch stream: density first, then appearance, each half signalled
+  // to the gathers that read it. With phase events set it runs here, before phase 0.
+  SideStream* pend_side = nullptr;
+  if (backward && adam && adam->pending) {
+    const tvm_adam_desc pd = pending_desc(adam->desc);
+    const int64_t a0 = L.appearance_lines, a1 = fields_end(m, L);
+    if (g_n_events == 0) {
+      TVM_TRY(side_stream(pend_side));
+      cudaError_t e = cudaEventRecord(pend_side->fork3, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(pend_side->branch, pend_side->fork3, 0);
+      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update fork: %s", cudaGetErrorString(e));
+      const cudaStream_t ps = pend_side->branch;
+      TVM_TRY(launch_adam_range(adam->params, grads, adam->mu, adam->nu, 0, a0, L.mlp_begin, pd, adam->shadow,
+                                adam->shadow_n, ps, 8, true));
+      e = cudaEventRecord(pend_side->density_ready, ps);
+      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update: %s", cudaGetErrorString(e));
+      TVM_TRY(launch_adam_range(adam->params, grads, adam->mu, adam->nu, a0, a1, L.mlp_begin, pd, adam->shadow,
+                                adam->shadow_n, ps, 8, true));
+      e = cudaEventRecord(pend_side->appearance_ready, ps);
+      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update: %s", cudaGetErrorString(e));
+    } else {
+      TVM_TRY(launch_adam_range(adam->params, grads, adam->mu, adam->nu, 0, a1, L.mlp_begin, pd, adam->shadow,
+                                adam->shadow_n, st, 8, true));
+    }
+  }
   phase_mark(0, st);
   if (proposal) {
     // Proposal network forward, then resampling into explicit main samples.
@@ -425,6 +474,10 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   const int k = c.appearance_samples;
 
   phase_mark(1, st);
+  if (pend_side) {  // the density gathers read the pending update's result
+    cudaError_t e = cudaStreamWaitEvent(st, pend_side->density_ready, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update join: %s", cudaGetErrorString(e));
+  }
   TVM_TRY(launch_density_fwd(fd, c.density_shift, rays.origins, rays.directions, R, s, b.sigma, st));
   phase_mark(2, st);
   if (c.mode != TVM_MODE_RGB) {
@@ -495,6 +548,10 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
     TVM_TRY(branch_done(side->stream, side->join));
   }
   phase_mark(3, st);
+  if (pend_side) {  // the appearance gathers read the pending update's result
+    cudaError_t e = cudaStreamWaitEvent(st, pend_side->appearance_ready, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update join: %s", cudaGetErrorString(e));
+  }
   TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
@@ -527,9 +584,10 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, ab));
+  const bool defer = adam && adam->defer;  // the field segments' update is left pending
   if (overlap) {
     if (adam) {
-      TVM_TRY(adam_seg(L.appearance_lines, has_prop ? L.proposal_lines : L.mlp_begin, ab));
+      if (!defer) TVM_TRY(adam_seg(L.appearance_lines, fields_end(m, L), ab));
       TVM_TRY(adam_seg(L.mlp_begin, has_prop ? L.proposal_w1 : L.total, ab));
     }
     TVM_TRY(branch_done(ab, side->join2));
@@ -544,10 +602,11 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   if (proposal && !overlap) TVM_TRY(proposal_backward(st));
   phase_mark(11, st);
   if (adam) {
-    if (overlap)  // the density field
-      TVM_TRY(adam_seg(L.density_lines, L.appearance_lines, st));
-    else
-      TVM_TRY(adam_seg(0, L.total, st));
+    if (overlap) {  // the density field
+      if (!defer) TVM_TRY(adam_seg(L.density_lines, L.appearance_lines, st));
+    } else {
+      TVM_TRY(adam_seg(defer ? fields_end(m, L) : 0, L.total, st));
+    }
   }
   if (overlap) {  // the caller's stream resumes once both side streams are done
     TVM_TRY(join(side->join2));
@@ -794,11 +853,38 @@ int tvm_adam_step(const tvm_model_desc* model, void* params, void* grads, void* 
 }
 
 int tvm_set_step_scalars(tvm_step_scalars* device_step, int32_t count, float lr_decay, uint64_t noise_stream,
-                         void* stream) {
+                         int32_t pending_count, float pending_lr_decay, void* stream) {
   TVM_REQUIRE(device_step != nullptr, TVM_ERR_INVALID, "device_step is NULL");
   TVM_REQUIRE(aligned(device_step, 8), TVM_ERR_ALIGN, "device_step must be 8-byte aligned");
   TVM_REQUIRE(count >= 1, TVM_ERR_INVALID, "Adam count must be >= 1");
-  return launch_set_step_scalars(device_step, count, lr_decay, noise_stream, as_stream(stream));
+  TVM_REQUIRE(pending_count >= 0, TVM_ERR_INVALID, "pending count must be >= 0");
+  tvm_step_scalars v;
+  memset(&v, 0, sizeof(v));
+  v.count = count;
+  v.lr_decay = lr_decay;
+  v.noise_stream = noise_stream;
+  v.pending_count = pending_count;
+  v.pending_lr_decay = pending_lr_decay;
+  return launch_set_step_scalars(device_step, v, as_stream(stream));
+}
+
+int tvm_apply_pending_fields(const tvm_model_desc* model, void* params, void* shadow, void* grads, void* mu, void* nu,
+                             const tvm_adam_desc* adam, void* stream) {
+  TVM_TRY(validate_model(model));
+  TVM_REQUIRE(params && grads && mu && nu && adam, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(params, 16) && aligned(grads, 16) && aligned(mu, 16) && aligned(nu, 16),
+              TVM_ERR_ALIGN, "Adam buffers must be 16-byte aligned");
+  TVM_REQUIRE(adam->pending_count >= 1, TVM_ERR_INVALID, "no pending update (pending_count must be >= 1)");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  const bool bf16 = shadow && model->dtype == TVM_BF16;
+  TVM_REQUIRE(!bf16 || aligned(shadow, 8), TVM_ERR_ALIGN, "shadow must be 8-byte aligned");
+  tvm_adam_desc d = pending_desc(*adam);
+  d.device_step = nullptr;
+  return launch_adam_range(static_cast<float*>(params), static_cast<float*>(grads), static_cast<float*>(mu),
+                           static_cast<float*>(nu), 0, fields_end(*model, L), L.mlp_begin, d,
+                           bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0,
+                           as_stream(stream));
 }
 
 int tvm_refresh_shadow(const tvm_model_desc* model, const void* params, void* shadow, void* stream) {
@@ -899,8 +985,22 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
   cudaStream_t st = as_stream(stream);
   tvm_param_layout L;
   make_layout(*model, L);
+  TVM_REQUIRE(adam->pending_count >= 0, TVM_ERR_INVALID, "pending count must be >= 0");
+  const bool bf16 = shadow && model->dtype == TVM_BF16;
+  const AdamPlan plan{static_cast<float*>(params), static_cast<float*>(adam_mu), static_cast<float*>(adam_nu), *adam,
+                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0,
+                      adam->device_step != nullptr || adam->pending_count > 0, adam->defer_fields != 0};
   if (rays->count == 0) {  // no rays: a plain Adam step on zero gradients
-    TVM_TRY(tvm_adam_step(model, params, grads, adam_mu, adam_nu, adam, shadow, stream));
+    if (plan.pending)
+      TVM_TRY(launch_adam_range(plan.params, static_cast<float*>(grads), plan.mu, plan.nu, 0, fields_end(*model, L),
+                                L.mlp_begin, pending_desc(*adam), plan.shadow, plan.shadow_n, st, 8, true));
+    if (adam->grad_sq) {
+      cudaError_t e = cudaMemsetAsync(adam->grad_sq, 0, sizeof(float), st);
+      TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
+    }
+    TVM_TRY(launch_adam_range(plan.params, static_cast<float*>(grads), plan.mu, plan.nu,
+                              plan.defer ? fields_end(*model, L) : 0, L.total, L.mlp_begin, *adam, plan.shadow,
+                              plan.shadow_n, st));
     phase_mark(12, st);
     return TVM_OK;
   }
@@ -909,9 +1009,6 @@ int tvm_train_step(const tvm_model_desc* model, void* params, void* shadow, void
     cudaError_t e = cudaMemsetAsync(z, 0, sizeof(float), st);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "memset: %s", cudaGetErrorString(e));
   }
-  const bool bf16 = shadow && model->dtype == TVM_BF16;
-  const AdamPlan plan{static_cast<float*>(params), static_cast<float*>(adam_mu), static_cast<float*>(adam_nu), *adam,
-                      bf16 ? static_cast<__nv_bfloat16*>(shadow) : nullptr, bf16 ? L.shadow_total : 0};
   TVM_TRY(run_pass(*model, static_cast<const float*>(params), shadow, static_cast<float*>(grads), *rays, colors, *cfg,
                    loss_out, nullptr, workspace, workspace_bytes, st, &plan));
   phase_mark(12, st);

@@ -155,16 +155,17 @@ int launch_loss_f64(const tvm_param_layout& L, const tvm_model_desc& m, const fl
 // ---- Adam (tvm_adam.cu) ----
 // blocks_per_sm caps the grid-stride grid: a full 8 when Adam has the GPU to itself,
 // fewer when it runs beside other kernels on a side stream and must leave them room.
+// pending: with a device_step, read the pending update's scalars (and do nothing when
+// its count is 0).
 int launch_adam(float* params, float* grads, float* mu, float* nu, int64_t n, int64_t mlp_begin,
                 const tvm_adam_desc& a, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
-                int blocks_per_sm = 8);
+                int blocks_per_sm = 8, bool pending = false);
 // Adam over the elements [lo, hi) of the flat buffers only (lo a segment start); the
 // learning-rate group and the shadow follow the element's place in the whole layout.
 int launch_adam_range(float* params, float* grads, float* mu, float* nu, int64_t lo, int64_t hi, int64_t mlp_begin,
                       const tvm_adam_desc& d, __nv_bfloat16* shadow, int64_t shadow_n, cudaStream_t st,
-                      int blocks_per_sm = 8);
+                      int blocks_per_sm = 8, bool pending = false);
 int launch_shadow(const float* src, __nv_bfloat16* dst, int64_t n, cudaStream_t st);
-int launch_set_step_scalars(tvm_step_scalars* step, int32_t count, float lr_decay, uint64_t noise_stream,
-                            cudaStream_t st);
+int launch_set_step_scalars(tvm_step_scalars* step, const tvm_step_scalars& v, cudaStream_t st);
 
 }  // namespace tvm

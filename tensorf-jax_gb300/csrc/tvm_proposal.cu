@@ -439,11 +439,16 @@ __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* _
                                  const int32_t* __restrict__ bins, int64_t R, int Np, int Nm, float scale,
                                  float* __restrict__ loss, float* __restrict__ gprop) {
   extern __shared__ float smem_f[];
+  __shared__ float block_loss[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float* C = smem_f + warp * 2 * (Np + 2);
   float* diff = C + (Np + 2);
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
-  if (r >= R) return;
+  if (r >= R) {  // a whole warp past the last ray: it adds nothing to the block's loss
+    if (lane == 0) block_loss[warp] = 0.f;
+    __syncthreads();
+    return;
+  }
   float carry = 0.f;
   if (lane == 0) C[0] = 0.f;
   for (int base = 0; base < Np; base += 32) {
@@ -470,8 +475,16 @@ __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* _
       atomicAdd(&diff[hi + 1], -gi);
     }
   }
+  // One reduction per block into the single loss word: per-warp reductions to one
+  // address serialise in L2.
   my_loss = warp_sum(my_loss);
-  if (lane == 0 && loss) atomicAdd(loss, my_loss * scale);
+  if (lane == 0) block_loss[warp] = my_loss * scale;
+  __syncthreads();
+  if (threadIdx.x == 0 && loss) {
+    float t = 0.f;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += block_loss[q];
+    atomicAdd(loss, t);
+  }
   __syncwarp();
   carry = 0.f;
   for (int base = 0; base < Np; base += 32) {
@@ -831,7 +844,7 @@ int launch_resample(const float* wprop, const float* origins, const float* dirs,
 int launch_prop_loss(const float* wmain, const float* wprop, const int32_t* bins, int64_t R, int Np, int Nm,
                      float scale, float* loss, float* gprop, cudaStream_t st) {
   if (R == 0) return TVM_OK;
-  const int warps = 4;
+  const int warps = 8;
   const size_t smem = (size_t)warps * 2 * (Np + 2) * sizeof(float);
   prop_loss_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(wmain, wprop, bins, R, Np, Nm, scale, loss,
                                                                            gprop);

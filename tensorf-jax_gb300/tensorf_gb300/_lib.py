@@ -70,8 +70,9 @@ class RenderDesc(ctypes.Structure):
 
 class AdamDesc(ctypes.Structure):
     _fields_ = [("lr_tensor", c_float), ("lr_mlp", c_float), ("b1", c_float), ("b2", c_float),
-                ("eps", c_float), ("lr_decay", c_float), ("count", c_int32), ("_pad", c_int32),
-                ("grad_sq", c_void_p), ("device_step", c_void_p)]
+                ("eps", c_float), ("lr_decay", c_float), ("count", c_int32), ("defer_fields", c_int32),
+                ("grad_sq", c_void_p), ("device_step", c_void_p), ("pending_count", c_int32),
+                ("pending_lr_decay", c_float)]
 
 
 # name -> (restype, argtypes)
@@ -114,7 +115,9 @@ _SIGNATURES = {
                                     POINTER(RenderDesc), c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_adam_step": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, POINTER(AdamDesc),
                                 c_void_p, c_void_p]),
-    "tvm_set_step_scalars": (c_int32, [c_void_p, c_int32, c_float, c_uint64, c_void_p]),
+    "tvm_set_step_scalars": (c_int32, [c_void_p, c_int32, c_float, c_uint64, c_int32, c_float, c_void_p]),
+    "tvm_apply_pending_fields": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                           POINTER(AdamDesc), c_void_p]),
     "tvm_noise_fill_keyed": (c_int32, [c_void_p, c_int64, c_uint64, c_void_p, c_uint64, c_uint64, c_int32, c_void_p]),
     "tvm_refresh_shadow": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p]),
     "tvm_l2_probe": (c_int32, [c_int32, c_void_p, c_size_t, c_int32, c_void_p]),

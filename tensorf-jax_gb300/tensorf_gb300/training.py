@@ -130,17 +130,26 @@ class TrainState:
     fixed-address input, noise and step-scalar buffers and is then recorded once, noise
     draws included; later steps copy the batch in, write the step's Adam count,
     learning-rate decay and noise key into device memory and replay the graph. Steps
-    given explicit ``noise`` run eagerly."""
+    given explicit ``noise`` run eagerly.
+
+    With ``defer_field_updates`` (and a step that does not log), the step leaves the
+    Adam update of the two VM fields pending; the next step applies it on a side stream
+    beside its own start, before its gathers read the fields, so Adam's 0.5 GB stream
+    overlaps the forward instead of ending the step. Reading ``learnable_params``,
+    ``grads``, ``mu`` or ``nu`` applies a pending update first, so every value seen
+    outside the step is the one the reference's sequential step would hold."""
 
     def __init__(self, config: TrainConfig, learnable_params: render.LearnableParams, seed: int = 94709,
-                 cuda_graph: bool = True):
+                 cuda_graph: bool = True, defer_field_updates: bool = True):
         self.config = config
-        self.learnable_params = learnable_params
+        self._pending: Optional[Tuple[int, float]] = None  # (count, lr decay) of a pending field update
+        self._lp = learnable_params
         self.appearance_mlp = learnable_params.spec.mlp()
         p = learnable_params.params
-        self.grads = torch.zeros_like(p)
-        self.mu = torch.zeros_like(p)
-        self.nu = torch.zeros_like(p)
+        self._grads = torch.zeros_like(p)
+        self._mu = torch.zeros_like(p)
+        self._nu = torch.zeros_like(p)
+        self.defer_field_updates = defer_field_updates
         self.aabb = torch.tensor([config.initial_aabb_min, config.initial_aabb_max], dtype=torch.float32)
         self.prng_key = render.NoiseKey(seed)
         self.step = 0
@@ -151,8 +160,79 @@ class TrainState:
         self._ws = None
         self._ws_key = None
         self.cuda_graph = cuda_graph
-        self._graph: Optional[_StepGraph] = None
+        self._graphs: dict = {}  # one recorded step per deferral mode
+        self._last_graph_mode: Optional[bool] = None
         self.graph_kernel_launches = 0  # kernels run by graph replays (the library counts eager launches)
+
+    # Parameters, gradients and moments as seen from outside the step: a pending field
+    # update is applied first.
+    @property
+    def learnable_params(self) -> render.LearnableParams:
+        self.apply_pending()
+        return self._lp
+
+    @learnable_params.setter
+    def learnable_params(self, value: render.LearnableParams) -> None:
+        self.apply_pending()
+        self._lp = value
+        self._graphs = {}
+
+    @property
+    def grads(self) -> torch.Tensor:
+        self.apply_pending()
+        return self._grads
+
+    @grads.setter
+    def grads(self, value: torch.Tensor) -> None:
+        self.apply_pending()
+        self._grads = value
+        self._graphs = {}
+
+    @property
+    def mu(self) -> torch.Tensor:
+        self.apply_pending()
+        return self._mu
+
+    @mu.setter
+    def mu(self, value: torch.Tensor) -> None:
+        self.apply_pending()
+        self._mu = value
+        self._graphs = {}
+
+    @property
+    def nu(self) -> torch.Tensor:
+        self.apply_pending()
+        return self._nu
+
+    @nu.setter
+    def nu(self, value: torch.Tensor) -> None:
+        self.apply_pending()
+        self._nu = value
+        self._graphs = {}
+
+    @property
+    def _graph(self) -> Optional[_StepGraph]:
+        """The most recently used recorded step."""
+        return self._graphs.get(self._last_graph_mode) if self._graphs else None
+
+    def apply_pending(self) -> None:
+        """Apply the field update the last step left pending (tvm_apply_pending_fields)."""
+        if self._pending is None:
+            return
+        count, decay = self._pending
+        self._pending = None
+        lp = self._lp
+        adam = self.adam_desc(count)
+        adam.pending_count, adam.pending_lr_decay = count, decay
+        _lib.call("tvm_apply_pending_fields", ctypes.byref(lp.model_desc()), ptr(lp.params), ptr(lp.shadow),
+                  ptr(self._grads), ptr(self._mu), ptr(self._nu), ctypes.byref(adam), stream_handle())
+
+    def _adam_for_step(self, defer: bool) -> _lib.AdamDesc:
+        adam = self.adam_desc(self.step + 1)
+        adam.defer_fields = int(defer)
+        if self._pending is not None:
+            adam.pending_count, adam.pending_lr_decay = self._pending
+        return adam
 
     @staticmethod
     def initialize(config: TrainConfig, spec: render.ModelSpec, seed: int = 94709) -> "TrainState":
@@ -198,7 +278,7 @@ class TrainState:
         self.appearance_mlp = new_spec.mlp()
         self._ws = None
         self._ws_key = None
-        self._graph = None
+        self._graphs = {}
         return self
 
     def state_dict(self) -> dict:
@@ -226,14 +306,14 @@ class TrainState:
         return ts
 
     def render_config(self) -> render.RenderConfig:
-        n, k = sample_counts(self.learnable_params.spec.grid_dim, self.config)
+        n, k = sample_counts(self._lp.spec.grid_dim, self.config)
         return render.RenderConfig(near=self.config.render_near, far=self.config.render_far,
                                    mode=render.RenderMode.RGB, density_samples_per_ray=n,
                                    appearance_samples_per_ray=k)
 
     def schedule(self) -> Optional[onp.ndarray]:
         """The contracted sampler's fixed schedule when it is not the reference one."""
-        if not self.learnable_params.scene_contraction or self.config.proposal is not None:
+        if not self._lp.scene_contraction or self.config.proposal is not None:
             return None
         if self.config.contracted_spacing == "disparity":
             cfg = self.render_config()
@@ -245,17 +325,18 @@ class TrainState:
     def adam_desc(self, count: int) -> _lib.AdamDesc:
         o = self.config.optimizer
         return _lib.AdamDesc(lr_tensor=o.lr_init_tensor, lr_mlp=o.lr_init_mlp, b1=0.9, b2=0.99, eps=1e-8,
-                             lr_decay=lr_decay_coeff(self.step, self.config), count=count, _pad=0,
+                             lr_decay=lr_decay_coeff(self.step, self.config), count=count, defer_fields=0,
                              grad_sq=self._stats[1:].data_ptr())
 
     def training_step(self, rays: cameras.Rays3D, colors: torch.Tensor,
                       noise: Optional[render.RenderNoise] = None, log: bool = True):
         """One step: returns (self, log_data). ``noise`` replaces the key-drawn noise."""
+        defer = self.defer_field_updates and not log  # a logged step reports its whole update
         if noise is None and self.cuda_graph:
-            return self._graph_step(rays, colors, log)
+            return self._graph_step(rays, colors, log, defer)
         cfg = self.render_config()
         r = rays.origins.reshape(-1, 3).shape[0]
-        lp = self.learnable_params
+        lp = self._lp
         prop = self.config.proposal
         if noise is None:
             render_key, self.prng_key = self.prng_key.split()
@@ -264,61 +345,63 @@ class TrainState:
         desc = render.make_render_desc(cfg, self.aabb, noise, r, lp.scene_contraction, sched,
                                        self.config.density_shift, proposal=prop)
         md = lp.model_desc()
-        key = (r, cfg)
-        if self._ws_key != key:
-            nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
-            self._ws = workspace(nbytes, lp.params.device)
-            self._ws_key = key
-        adam = self.adam_desc(self.step + 1)
+        self._ensure_workspace(md, desc, r, cfg)
+        adam = self._adam_for_step(defer)
         rs = render.rays_struct(rays)
-        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self.grads),
-                  ptr(self.mu), ptr(self.nu), ctypes.byref(adam), ctypes.byref(rs), ptr(colors.contiguous()),
+        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self._grads),
+                  ptr(self._mu), ptr(self._nu), ctypes.byref(adam), ctypes.byref(rs), ptr(colors.contiguous()),
                   ctypes.byref(desc), ptr(self.loss), ptr(self._ws), self._ws.numel(), stream_handle())
+        self._pending = (adam.count, adam.lr_decay) if defer else None
         self.step += 1
-        log_data = {}
-        if log:  # training.py:143-196: mse, psnr, both learning rates, the gradient's global norm
-            mse, grad_sq = self._stats.tolist()
-            log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
-                        "train/lr_tensor": adam.lr_decay * self.config.optimizer.lr_init_tensor,
-                        "train/lr_mlp": adam.lr_decay * self.config.optimizer.lr_init_mlp,
-                        "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
-        return self, log_data
+        return self, self._log(log, adam.lr_decay)
+
+    def _log(self, log: bool, decay: float) -> dict:
+        if not log:
+            return {}
+        # training.py:143-196: mse, psnr, both learning rates, the gradient's global norm
+        mse, grad_sq = self._stats.tolist()
+        return {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
+                "train/lr_tensor": decay * self.config.optimizer.lr_init_tensor,
+                "train/lr_mlp": decay * self.config.optimizer.lr_init_mlp,
+                "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
 
     def _ensure_workspace(self, md, desc, r: int, cfg) -> None:
         key = (r, cfg)
         if self._ws_key != key:
             nbytes = _lib.load().tvm_train_workspace_size(ctypes.byref(md), ctypes.byref(desc), r)
-            self._ws = workspace(nbytes, self.learnable_params.params.device)
+            self._ws = workspace(nbytes, self._lp.params.device)
             self._ws_key = key
 
-    def _graph_call(self, g: _StepGraph, cfg, r: int) -> None:
-        """tvm_train_step on the graph's fixed buffers, Adam scalars read on the device."""
-        lp = self.learnable_params
+    def _graph_call(self, g: _StepGraph, cfg, r: int, defer: bool) -> None:
+        """tvm_train_step on the graph's fixed buffers; the Adam scalars, the pending
+        field update's and the noise key are read on the device."""
+        lp = self._lp
         prop = self.config.proposal
+        render.draw_noise_keyed(self.prng_key.seed, g.step_scalars, r, cfg, prop, g.noise)
         desc = render.make_render_desc(cfg, self.aabb, g.noise, r, lp.scene_contraction, g.schedule,
                                        self.config.density_shift, proposal=prop)
         md = lp.model_desc()
         self._ensure_workspace(md, desc, r, cfg)
-        render.draw_noise_keyed(self.prng_key.seed, g.step_scalars, r, cfg, prop, g.noise)
         adam = self.adam_desc(1)
         adam.device_step = g.step_scalars.data_ptr()
+        adam.defer_fields = int(defer)
         rs = render.rays_struct(cameras.Rays3D(g.origins, g.directions, g.camera_indices))
-        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self.grads),
-                  ptr(self.mu), ptr(self.nu), ctypes.byref(adam), ctypes.byref(rs), ptr(g.colors),
+        _lib.call("tvm_train_step", ctypes.byref(md), ptr(lp.params), ptr(lp.shadow), ptr(self._grads),
+                  ptr(self._mu), ptr(self._nu), ctypes.byref(adam), ctypes.byref(rs), ptr(g.colors),
                   ctypes.byref(desc), ptr(self.loss), ptr(self._ws), self._ws.numel(), stream_handle())
 
-    def _graph_step(self, rays: cameras.Rays3D, colors: torch.Tensor, log: bool):
+    def _graph_step(self, rays: cameras.Rays3D, colors: torch.Tensor, log: bool, defer: bool):
         cfg = self.render_config()
-        lp = self.learnable_params
+        lp = self._lp
         prop = self.config.proposal
         o = rays.origins.reshape(-1, 3)
         d = rays.directions.reshape(-1, 3)
         ci = rays.camera_indices
         r = o.shape[0]
         key = (r, cfg, self.config, ci is not None, lp.params.data_ptr(), lp.shadow.data_ptr() if lp.shadow is not None
-               else 0, self.grads.data_ptr(), self.mu.data_ptr(), self.nu.data_ptr(), self.loss.data_ptr(),
-               self.prng_key.seed)
-        g = self._graph
+               else 0, self._grads.data_ptr(), self._mu.data_ptr(), self._nu.data_ptr(), self.loss.data_ptr(),
+               self.prng_key.seed, defer)
+        g = self._graphs.get(defer)
         fresh = g is None or g.key != key
         if fresh:
             dev = lp.params.device
@@ -328,8 +411,8 @@ class TrainState:
                            colors=torch.empty((r, 3), dtype=torch.float32, device=dev),
                            camera_indices=torch.empty(r, dtype=torch.int32, device=dev) if ci is not None else None,
                            noise=render.draw_noise(render.NoiseKey(0), r, cfg, lp.scene_contraction, prop),
-                           schedule=sched, step_scalars=torch.zeros(2, dtype=torch.int64, device=dev))
-            self._graph = None
+                           schedule=sched, step_scalars=torch.zeros(3, dtype=torch.int64, device=dev))
+            self._graphs.pop(defer, None)
         render_key, self.prng_key = self.prng_key.split()
         for dst, src in ((g.origins, o), (g.directions, d), (g.colors, colors.reshape(-1, 3))):
             if dst.data_ptr() != src.data_ptr():
@@ -337,30 +420,26 @@ class TrainState:
         if ci is not None and g.camera_indices.data_ptr() != ci.data_ptr():
             g.camera_indices.copy_(ci.reshape(-1))
         decay = lr_decay_coeff(self.step, self.config)
+        pend_count, pend_decay = self._pending if self._pending is not None else (0, 0.0)
         _lib.call("tvm_set_step_scalars", g.step_scalars.data_ptr(), self.step + 1, decay,
-                  render_key.stream & (2**64 - 1), stream_handle())
+                  render_key.stream & (2**64 - 1), pend_count, pend_decay, stream_handle())
         if fresh:
             # This step runs eagerly on the graph's buffers (the library's one-time setup
             # happens here, outside any capture); the next ones replay its recording, the
             # noise draws included.
-            self._graph_call(g, cfg, r)
+            self._graph_call(g, cfg, r, defer)
             lib = _lib.load()
             graph = torch.cuda.CUDAGraph()
             before = lib.tvm_kernel_launches()
             with torch.cuda.graph(graph, capture_error_mode="thread_local"):
-                self._graph_call(g, cfg, r)
+                self._graph_call(g, cfg, r, defer)
             g.launches = int(lib.tvm_kernel_launches() - before)
             g.graph = graph
-            self._graph = g
+            self._graphs[defer] = g
         else:
             g.graph.replay()
             self.graph_kernel_launches += g.launches
+        self._last_graph_mode = defer
+        self._pending = (self.step + 1, decay) if defer else None
         self.step += 1
-        log_data = {}
-        if log:
-            mse, grad_sq = self._stats.tolist()
-            log_data = {"train/mse": mse, "train/psnr": utils.psnr_from_mse(mse),
-                        "train/lr_tensor": decay * self.config.optimizer.lr_init_tensor,
-                        "train/lr_mlp": decay * self.config.optimizer.lr_init_mlp,
-                        "train/grad_norm": math.sqrt(max(grad_sq, 0.0))}
-        return self, log_data
+        return self, self._log(log, decay)

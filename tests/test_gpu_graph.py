@@ -1,14 +1,15 @@
 """TrainState with its step recorded as a CUDA graph (the counterpart of the reference's
-jit-compiled step, training.py:101) against the same steps run eagerly.
+jit-compiled step, training.py:101), and with its field updates deferred to the next
+step, against the same steps run eagerly and updating at once.
 
 Both states start from the same parameters and key, so they draw the same noise; the
 graph path reads the Adam scalars and the noise key from device memory
-(tvm_set_step_scalars) and its batches are copied into fixed buffers. After several steps parameters and both moments agree to
-the order of the atomic gradient reductions (FP32: all but a handful of elements to 1e-5;
-BF16, where last-bit differences flip bf16 roundings: no further from the eager run in norm
-than a second eager run is), the logged learning
-rates are equal, the replays ran (and counted) their kernels, and a grid resize records a
-new graph.
+(tvm_set_step_scalars) and its batches are copied into fixed buffers. After several
+steps parameters and both moments agree to the order of the atomic gradient reductions
+(FP32: all but a handful of elements to 1e-5; BF16, where last-bit differences flip bf16
+roundings: no further from the eager run in norm than a second eager run is), the logged
+learning rates are equal, the replays ran (and counted) their kernels, and a grid resize
+records a new graph.
 """
 import dataclasses
 
@@ -138,14 +139,61 @@ def test_keyed_noise_equals_key_drawn_noise(proposal):
     R = 100
     cfg = render.RenderConfig(0.05, 200.0, render.RenderMode.RGB, 24, 4)
     prop = render.ProposalConfig(samples=16) if proposal else None
-    scal = torch.zeros(2, dtype=torch.int64, device="cuda")
+    scal = torch.zeros(3, dtype=torch.int64, device="cuda")  # tvm_step_scalars
     for stream in (0, 5, 2**63 + 12345):
         key = render.NoiseKey(77, stream)
         want = render.draw_noise(key, R, cfg, False, prop)
         got = render.draw_noise(render.NoiseKey(0), R, cfg, False, prop)
-        _lib.call("tvm_set_step_scalars", scal.data_ptr(), 1, 1.0, stream & (2**64 - 1), stream_handle())
+        _lib.call("tvm_set_step_scalars", scal.data_ptr(), 1, 1.0, stream & (2**64 - 1), 0, 0.0, stream_handle())
         render.draw_noise_keyed(77, scal, R, cfg, prop, got)
         for a, b in ((want.jitter, got.jitter), (want.gumbel, got.gumbel), (want.proposal_jitter, got.proposal_jitter)):
             assert (a is None) == (b is None)
             if a is not None:
                 assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("case", ["bounded", "proposal_bf16"])
+def test_deferred_field_updates_match_immediate(case, graph):
+    """Steps that leave the fields' Adam update pending (applied by the next step beside
+    its start, or when parameters are read) against steps that update at once: equal
+    parameters, moments and zero gradients whenever they are read, including mid-run."""
+    from tensorf_gb300 import render, training
+    kw = dict(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
+              appearance_samples_per_ray=8, density_shift=-1.0, n_iters=20, upsamp_iters=(3,))
+    spec = render.ModelSpec(grid_dim=24)
+    if case == "proposal_bf16":
+        kw.update(density_samples_per_ray=32, proposal=render.ProposalConfig(samples=32))
+        spec = render.ModelSpec(grid_dim=24, precision="bf16", proposal_grid=16)
+    cfg = training.TrainConfig(**kw)
+    bf16 = spec.precision == "bf16"
+
+    def make(defer, cuda_graph):
+        lp = render.LearnableParams.initialize(spec, seed=4)
+        return training.TrainState(cfg, lp, seed=7, cuda_graph=cuda_graph, defer_field_updates=defer)
+
+    states = [make(False, False), make(True, graph)] + ([make(False, False)] if bf16 else [])
+    batches = _batches(256, 6, 21)
+
+    def check():
+        ref, dfr = states[0], states[1]
+        for name in ("params", "mu", "nu"):
+            get = (lambda st: st.learnable_params.params) if name == "params" else (lambda st: getattr(st, name))
+            if bf16:
+                d_def, d_eager = _dist(get(ref), get(dfr)), _dist(get(ref), get(states[2]))
+                assert d_def <= 3.0 * d_eager + 1e-6, (name, d_def, d_eager)
+            else:
+                ok, n_off = _close(get(ref), get(dfr))
+                assert ok, (name, n_off)
+        assert float(dfr.grads.abs().max()) == 0.0
+
+    for i, (rays, colors) in enumerate(batches):
+        for st in states:
+            st.training_step(rays, colors, log=False)
+        assert states[1]._pending is not None
+        if i == 2:
+            check()  # reading applies the pending update; the next step then has none
+            assert states[1]._pending is None
+    torch.cuda.synchronize()
+    check()
+    assert states[1].step == 6
