@@ -70,11 +70,41 @@ __device__ void stage_weight(uint8_t* dst, const float* __restrict__ W, int ld, 
 
 // One 128-row tile of X0 (fp32, global) into a bf16 A tile (K-major canonical, SBO
 // sbo) at dst; rows at or past M are zero. Each thread issues all of its loads before
-// its first shared-memory store, so the tile costs one L2 round trip, not nine.
+// its first shared-memory store, so the tile costs one L2 round trip, not nine. The two
+// halves (x0_fetch: loads into registers, x0_store: conversion and stores) also let a
+// caller keep the next tile's loads in flight while it waits for an MMA.
+constexpr int X0_PER_THREAD = BM * (F / 8) / THREADS;
+static_assert(BM * (F / 8) % THREADS == 0, "whole chunks per thread");
+
+__device__ __forceinline__ void x0_fetch(float4 (&p)[X0_PER_THREAD], float4 (&q)[X0_PER_THREAD], const float* X0,
+                                         int64_t m0, int64_t M, int tid) {
+#pragma unroll
+  for (int i = 0; i < X0_PER_THREAD; ++i) {
+    const int c = tid + i * THREADS;
+    const int64_t row = m0 + c / (F / 8);
+    p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    q[i] = p[i];
+    if (row < M) {
+      const float4* src = reinterpret_cast<const float4*>(X0 + row * F + (c % (F / 8)) * 8);
+      p[i] = __ldg(src);
+      q[i] = __ldg(src + 1);
+    }
+  }
+}
+
+__device__ __forceinline__ void x0_store(const float4 (&p)[X0_PER_THREAD], const float4 (&q)[X0_PER_THREAD],
+                                         uint8_t* dst, int sbo, int tid) {
+#pragma unroll
+  for (int i = 0; i < X0_PER_THREAD; ++i) {
+    const int c = tid + i * THREADS;
+    *reinterpret_cast<uint4*>(dst + coff(c / (F / 8), c % (F / 8), sbo)) =
+        make_uint4(pack2(p[i].x, p[i].y), pack2(p[i].z, p[i].w), pack2(q[i].x, q[i].y), pack2(q[i].z, q[i].w));
+  }
+}
+
 __device__ __forceinline__ void load_x0_tile(uint8_t* dst, int sbo, const float* X0, int64_t m0, int64_t M,
                                              int tid) {
-  constexpr int PER_THREAD = BM * (F / 8) / THREADS;
-  static_assert(BM * (F / 8) % THREADS == 0, "whole chunks per thread");
+  constexpr int PER_THREAD = X0_PER_THREAD;
   float4 p[PER_THREAD], q[PER_THREAD];
 #pragma unroll
   for (int i = 0; i < PER_THREAD; ++i) {
@@ -175,11 +205,15 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   };
 
   const int64_t ntiles = (a.M + BM - 1) / BM;
+  // The X0 tile (128 rows x 18 chunks of 8 features) of the first tile is loaded here;
+  // each later one is fetched into registers while layer 2's MMA runs and stored into
+  // the A0 tile once that MMA has read H1 from it.
+  if ((int64_t)blockIdx.x < ntiles) load_x0_tile(smem + OFF_A0, SBO_F, a.X0, (int64_t)blockIdx.x * BM, a.M, tid);
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int64_t m0 = tile * BM;
-    load_x0_tile(smem + OFF_A0, SBO_F, a.X0, m0, a.M, tid);  // 128 rows x 18 chunks of 8 features
-    {  // the next tile's features travel to L2 while this tile computes
-      const int64_t nm0 = (tile + gridDim.x) * BM;
+    const int64_t next = tile + gridDim.x;
+    {  // the tile after the next one travels to L2 while this tile computes
+      const int64_t nm0 = (next + gridDim.x) * BM;
       if (nm0 < a.M) {
         const int64_t nbytes = (a.M - nm0 < BM ? a.M - nm0 : BM) * F * 4;
         for (int64_t off = (int64_t)tid * 128; off < nbytes; off += THREADS * 128)
@@ -270,7 +304,10 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
       }
     };
     hidden(D1, a.b1, OFF_A0);
+    float4 xp[X0_PER_THREAD], xq[X0_PER_THREAD];
+    if (next < ntiles) x0_fetch(xp, xq, a.X0, next * BM, a.M, tid);  // in flight during layer 2
     if (!layer(D2, OFF_A0, OFF_W2, U / 16, SBO_U, SBO_U, U)) { ok = 0; break; }
+    if (next < ntiles) x0_store(xp, xq, smem + OFF_A0, SBO_F, tid);  // layer 2 has read H1 from A0
     hidden(D2, a.b2, OFF_A1);
     if (!layer(D3, OFF_A1, OFF_W3, U / 16, SBO_U, SBO_U, OUTP)) { ok = 0; break; }
     if (half == 0) {
