@@ -88,9 +88,10 @@ __device__ __forceinline__ void prop_sample(const RayGeom& g, const SamplerArgs&
 // Features X[s] = [12 VM features (pair-major), x, y, z, |x|_inf], bin length, and
 // (with weights) the whole MLP in registers: h = relu(X W1 + b1), sigma = softplus(h W2
 // + b2 + shift). The weights sit in shared memory and every thread reads the same
-// element at the same time (broadcast); each thread carries two samples (blockDim
-// apart) through the MLP, so every weight it loads serves both. X and h are written only
-// when the backward needs them.
+// element at the same time (broadcast); each thread carries PROP_SPT samples (blockDim
+// apart) through the MLP, so every weight it loads serves all of them. X and h are
+// written only when the backward needs them.
+constexpr int PROP_SPT = 2;
 template <typename T>
 __device__ __forceinline__ void prop_sample_features(const T* __restrict__ lines, const T* __restrict__ planes, int G,
                                                      const float* __restrict__ origins, const float* __restrict__ dirs,
@@ -144,16 +145,18 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
     __syncthreads();
   }
   const int64_t n = R * s.N;
-  const int64_t smp0 = (int64_t)blockIdx.x * (2 * blockDim.x) + threadIdx.x;
-  const int64_t smps[2] = {smp0, smp0 + blockDim.x};
+  const int64_t smp0 = (int64_t)blockIdx.x * (PROP_SPT * blockDim.x) + threadIdx.x;
   if (smp0 >= n) return;
-  const bool two = smps[1] < n;
-  float out[2][PROP_IN];
+  int64_t smps[PROP_SPT];
+  bool has[PROP_SPT];
+  float out[PROP_SPT][PROP_IN];
 #pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (k == 1 && !two) {
+  for (int k = 0; k < PROP_SPT; ++k) {
+    smps[k] = smp0 + (int64_t)k * blockDim.x;
+    has[k] = smps[k] < n;
+    if (!has[k]) {
 #pragma unroll
-      for (int i = 0; i < PROP_IN; ++i) out[1][i] = 0.f;
+      for (int i = 0; i < PROP_IN; ++i) out[k][i] = 0.f;
       continue;
     }
     float len;
@@ -170,14 +173,18 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
   const float4* sw1 = reinterpret_cast<const float4*>(sw);  // row u: 16 weights
   const float* sb1 = sw + 16 * units;
   const float* sw2 = sw + 17 * units;
-  float z[2] = {__ldg(b2), __ldg(b2)};
+  float z[PROP_SPT];
+#pragma unroll
+  for (int k = 0; k < PROP_SPT; ++k) z[k] = __ldg(b2);
   for (int u = 0; u < units; ++u) {
-    float h[2] = {sb1[u], sb1[u]};
+    float h[PROP_SPT];
+#pragma unroll
+    for (int k = 0; k < PROP_SPT; ++k) h[k] = sb1[u];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const float4 w = sw1[u * 4 + q];
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < PROP_SPT; ++k) {
         h[k] = fmaf(out[k][4 * q], w.x, h[k]);
         h[k] = fmaf(out[k][4 * q + 1], w.y, h[k]);
         h[k] = fmaf(out[k][4 * q + 2], w.z, h[k]);
@@ -186,14 +193,15 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
     }
     const float w2u = sw2[u];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < PROP_SPT; ++k) {
       h[k] = fmaxf(h[k], 0.0f);
-      if (H && (k == 0 || two)) H[smps[k] * units + u] = h[k];
+      if (H && has[k]) H[smps[k] * units + u] = h[k];
       z[k] = fmaf(h[k], w2u, z[k]);
     }
   }
-  sigma[smps[0]] = softplus_f(z[0] + shift);
-  if (two) sigma[smps[1]] = softplus_f(z[1] + shift);
+#pragma unroll
+  for (int k = 0; k < PROP_SPT; ++k)
+    if (has[k]) sigma[smps[k]] = softplus_f(z[k] + shift);
 }
 
 // Fused proposal backward, one thread per sample, 128 samples per block: recompute the
@@ -502,7 +510,7 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
                          cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
-  const unsigned blocks = (unsigned)ceil_div(n, 256);  // 128 threads, two samples each
+  const unsigned blocks = (unsigned)ceil_div(n, 128 * PROP_SPT);  // 128 threads, PROP_SPT samples each
   const int units = mlp ? mlp->units : 0;
   const size_t smem = mlp ? (size_t)18 * units * sizeof(float) : 0;
   const float *w1 = mlp ? mlp->w1 : nullptr, *b1 = mlp ? mlp->b1 : nullptr, *w2 = mlp ? mlp->w2 : nullptr,
