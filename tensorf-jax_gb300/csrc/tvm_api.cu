@@ -556,7 +556,15 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
-  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, rays.camera_indices, k, R * k, b.rgb, ws, st));
+  // The fused BF16 MLP kernels fill every SM's shared memory and TMEM, so nothing runs
+  // beside them on an SM they hold. Where other streams have work at the same time (the
+  // proposal backward beside the forward; the density branch beside the backward) they
+  // take half the SMs, each CTA working through more tiles: same-box A/B, BF16 step
+  // 1.445 -> 1.399 ms and proposal step 0.366 -> 0.352 ms. Their time alone gets longer,
+  // so a pass on one stream keeps the whole GPU for them.
+  const int shared_ctas = device_sms() / 2;
+  TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, rays.camera_indices, k, R * k, b.rgb, ws, st,
+                      overlap && prop_forked ? shared_ctas : 0));
   phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
@@ -580,7 +588,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   }
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
   TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, rays.camera_indices, k, R * k, b.dZ3,
-                       b.dX0, ws2, ab));
+                       b.dX0, ws2, ab, overlap ? shared_ctas : 0));
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, ab));

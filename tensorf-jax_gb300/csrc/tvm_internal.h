@@ -94,15 +94,16 @@ size_t mlp_workspace_bytes(const MlpDims& d, int64_t M);      // forward + backw
 size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M);  // forward only (a prefix of the above)
 // rgb = FeatureMlp(X0, viewdir, camera). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...],
 // its camera cams[m / rows_per_dir] (cams is read only when d.cams > 0).
+// max_ctas: the fused BF16 kernels' grid cap (launch_mlp_fwd_fused), 0 for one CTA per SM.
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
-                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st);
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas = 0);
 // Needs the preceding mlp_forward on the same workspace: its kept row-major activations
 // (layered path), or its packed bf16 weights (fused path, which recomputes the forward
 // from X0 and the view directions).
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                  const int32_t* cams, int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws,
-                 cudaStream_t st);
+                 cudaStream_t st, int max_ctas = 0);
 int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
@@ -111,14 +112,16 @@ int prop_status(int32_t* out, cudaStream_t st);    // same for the tensor-core p
 bool mlp_fused_supported(const MlpDims& d);
 // wpack: mlp_fused_pack_bytes() of scratch (16-byte aligned) for the packed weights.
 size_t mlp_fused_pack_bytes();
+// max_ctas > 0 caps the persistent grid (fewer CTAs each take more tiles), leaving the
+// other SMs to kernels that run beside it on other streams; 0: one CTA per SM.
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st);
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas = 0);
 // Fused BF16 backward: recomputes the forward per tile, accumulates all weight and
 // bias gradients into g, writes dX0 (M, 144) when non-null. wpack: the images packed by
 // launch_mlp_fwd_fused.
 int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                          int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
-                         cudaStream_t st);
+                         cudaStream_t st, int max_ctas = 0);
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
 

@@ -816,7 +816,7 @@ bool mlp_fused_supported(const MlpDims& d) {
 size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }
 
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st) {
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas) {
   if (M == 0) return TVM_OK;
   TVM_TRY(ensure_smem_limit((const void*)fmlp::mlp_fwd_fused_kernel, fmlp::SMEM, "fused mlp"));
   const int sms = device_sms();
@@ -828,14 +828,14 @@ int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0,
   TVM_TRY(check_launch("pack_weights"));
   fmlp::Args a{M, wpack, X0, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(sms, 1));
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(max_ctas > 0 ? max_ctas : sms, 1));
   fmlp::mlp_fwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::SMEM, st>>>(a);
   return check_launch("mlp_fwd_fused");
 }
 
 int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                          int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
-                         cudaStream_t st) {
+                         cudaStream_t st, int max_ctas) {
   if (M == 0) return TVM_OK;
   TVM_TRY(ensure_smem_limit((const void*)fmlp::bwd::mlp_bwd_fused_kernel, fmlp::bwd::SMEM, "fused mlp backward"));
   const int sms = device_sms();
@@ -846,7 +846,7 @@ int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0
   fmlp::bwd::Args a{M, wpack, X0, dirs, rows_per_dir, w.b1, w.b2, dZ3, dX0,
                     g.w0, g.w1, g.b1, g.w2, g.b2, g.w3, g.b3};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(sms, 1));
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(max_ctas > 0 ? max_ctas : sms, 1));
   fmlp::bwd::mlp_bwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::bwd::SMEM, st>>>(a);
   return check_launch("mlp_bwd_fused");
 }
