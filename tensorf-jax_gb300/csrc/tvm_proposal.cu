@@ -814,7 +814,10 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
     TVM_TRY(ensure_smem_limit((const void*)ptc::prop_bwd_tc_kernel, ptc::SMEM, "proposal backward"));
     const int sms = device_sms();
     const int64_t tiles = ceil_div(n, ptc::THREADS);
-    const unsigned grid = (unsigned)std::min<int64_t>(tiles, 2 * std::max(sms, 1));  // 2 CTAs fit an SM
+    // One CTA per SM although two fit: the kernel runs beside the main field's backward on
+    // a side stream, and the room it leaves there is worth more than its own speed
+    // (same-box A/B of the proposal step: -2 us).
+    const unsigned grid = (unsigned)std::min<int64_t>(tiles, std::max(sms, 1));
     ptc::prop_bwd_tc_kernel<<<grid, ptc::THREADS, ptc::SMEM, st>>>(
         (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines, gplanes, origins, dirs, R, s, edges,
         jitter, dz, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2);
