@@ -211,14 +211,15 @@ TVM_API const char* tvm_last_error_message(void);
 /* Number of kernels this library has launched from the calling thread. */
 TVM_API uint64_t tvm_kernel_launches(void);
 /* Measurement hook: when `events` (n cudaEvent_t created by the caller) is set for the
- * calling thread, tvm_train_step / tvm_loss_and_grad / tvm_render_fwd record
- * events[i] on their stream at the boundary before phase i and events[n_phases] after
- * the last one (phases: 0 proposal network forward + resampling, 1 density fwd,
- * 2 composite+select, 3 appearance gather, 4 MLP fwd, 5 colour+loss, 6 MLP bwd,
- * 7 appearance scatter, 8 composite bwd, 9 density scatter, 10 the wait for the
- * proposal backward on its side stream, 11 Adam: in tvm_train_step, the density
- * field's update and the wait for the other segments' updates on their side stream).
- * Unused trailing phases record nothing. NULL disables. */
+ * calling thread, tvm_train_step / tvm_loss_and_grad / tvm_render_fwd run the whole pass
+ * on the caller's stream, in phase order (no side streams, full grids), and record
+ * events[i] there at the boundary before phase i and events[12] after the last one
+ * (phases: 0 proposal network forward + resampling, 1 density fwd, 2 composite+select,
+ * 3 appearance gather, 4 MLP fwd, 5 colour+loss, 6 MLP bwd, 7 appearance scatter,
+ * 8 composite bwd, 9 density scatter, 10 proposal bound loss + backward, 11 Adam: in
+ * tvm_train_step, one update over every segment whose update is not deferred). A field
+ * update left pending by the previous step runs before phase 0. Unused trailing phases
+ * record nothing. NULL disables. */
 TVM_API int tvm_set_phase_events(void* const* events, int32_t n);
 
 /* ---- parameter layout ---------------------------------------------------------- */
