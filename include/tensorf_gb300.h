@@ -349,6 +349,41 @@ TVM_API int tvm_gemm(int32_t math, int32_t a_trans, int32_t b_trans, int64_t M, 
  * tensor-core wait gave up (results of that call are invalid). */
 TVM_API int tvm_device_status(int32_t* out, void* stream);
 
+/* ---- (e) proposal network ------------------------------------------------------------ */
+/* The stages of TVM_SAMPLER_PROPOSAL that tvm_render_fwd and tvm_train_step run fused.
+ * The reference has no proposal network (it samples uniformly; render.py:126 suggests
+ * one); these seams stand beside its sampler seam (render.py:122-186), and a caller that
+ * binds them composes: fwd -> tvm_composite_fwd (p_terminates = the proposal weights) ->
+ * resample -> main field; in training the main weights -> loss -> tvm_composite_bwd ->
+ * bwd. cfg: sampler TVM_SAMPLER_PROPOSAL with proposal_samples (Np), proposal_jitter,
+ * proposal_shift, aabb, contract and (contract) the Np+1 edges in schedule. */
+/* Proposal forward: per ray, Np bins (uniform over the ray's aabb segment, or the
+ * caller's edges with contraction), one jittered point per bin, its 12 VM features
+ * plus [x, y, z, max|x|] through the 16 -> units -> 1 MLP, softplus(z + shift).
+ * sigmas, deltas (bin lengths): (R, Np). */
+TVM_API int tvm_proposal_fwd(const tvm_model_desc* model, const void* params, const void* shadow,
+                             const tvm_rays* rays, const tvm_render_desc* cfg, float* sigmas, float* deltas,
+                             void* stream);
+/* Resampling: proposal weights (R, Np) -> N = cfg->density_samples main intervals at the
+ * quantiles i/N of w + (0.01 sum w + 1e-4) / Np, one point each at cfg->jitter (R, N):
+ * ts, deltas (R, N) and bins (R, N+1) int32, the proposal bin of each interval edge. */
+TVM_API int tvm_proposal_resample(const tvm_rays* rays, const tvm_render_desc* cfg, const float* weights,
+                                  float* ts, float* deltas, int32_t* bins, void* stream);
+/* Bound loss: scale * sum_i max(0, w_i - bound_i)^2 / (w_i + 1e-7), bound_i the proposal
+ * mass over bins [bins_i, bins_i+1] (the fused step uses scale = loss_weight / R).
+ * main_weights (R, N) (no gradient), proposal_weights (R, Np), bins (R, N+1).
+ * loss: one device float, ACCUMULATED (may be NULL); grad_proposal_weights (R, Np)
+ * overwritten. */
+TVM_API int tvm_proposal_loss(const float* main_weights, const float* proposal_weights, const int32_t* bins,
+                              int64_t rays, int32_t proposal_samples, int32_t samples, float scale, float* loss,
+                              float* grad_proposal_weights, void* stream);
+/* Proposal backward: grad_sigmas (R, Np) of the sigmas tvm_proposal_fwd returned ->
+ * ACCUMULATES into the proposal segments of grads (field lines and planes, w1, b1, w2,
+ * b2). Recomputes the features from the same rays, cfg and proposal_jitter. */
+TVM_API int tvm_proposal_bwd(const tvm_model_desc* model, const void* params, const void* shadow, void* grads,
+                             const tvm_rays* rays, const tvm_render_desc* cfg, const float* sigmas,
+                             const float* grad_sigmas, void* stream);
+
 /* ---- fused render_rays / training_step ---------------------------------------------- */
 /* render_rays (render.py:105-279) for one chunk of rays. out: (R, 3) for RGB, (R,) for
  * distances. params: flat master buffer; shadow: bf16 copies (TVM_BF16 models) or

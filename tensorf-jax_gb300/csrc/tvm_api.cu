@@ -807,6 +807,95 @@ static int validate_params(const tvm_model_desc* m, const void* params, const vo
   return TVM_OK;
 }
 
+// ---- proposal seams: the stages of the fused pass's proposal-guided sampling, one
+// call each (bins -> sigma and lengths, weights -> main samples, bound loss, backward).
+static int validate_proposal(const tvm_model_desc* m, const tvm_rays* rays, const tvm_render_desc* c) {
+  TVM_TRY(validate_model(m));
+  TVM_TRY(validate_rays(rays));
+  TVM_REQUIRE(c != nullptr, TVM_ERR_INVALID, "render descriptor is NULL");
+  TVM_REQUIRE(m->proposal_grid > 0, TVM_ERR_INVALID, "the model has no proposal network");
+  TVM_REQUIRE(c->sampler == TVM_SAMPLER_PROPOSAL, TVM_ERR_INVALID, "the descriptor's sampler must be TVM_SAMPLER_PROPOSAL");
+  TVM_REQUIRE(c->proposal_samples >= 2 && c->proposal_samples <= 512, TVM_ERR_SHAPE,
+              "proposal_samples=%d outside [2, 512]", c->proposal_samples);
+  TVM_REQUIRE(rays->count == 0 || c->proposal_jitter != nullptr, TVM_ERR_INVALID, "proposal_jitter (R, Np) is NULL");
+  TVM_REQUIRE(!c->contract || c->schedule != nullptr, TVM_ERR_INVALID,
+              "unbounded proposal sampling needs the Np+1 bin edges in schedule");
+  for (int a = 0; a < 3; ++a)
+    TVM_REQUIRE(c->aabb[a] < c->aabb[3 + a], TVM_ERR_INVALID, "aabb min must be < max on every axis");
+  return TVM_OK;
+}
+
+int tvm_proposal_fwd(const tvm_model_desc* model, const void* params, const void* shadow, const tvm_rays* rays,
+                     const tvm_render_desc* cfg, float* sigmas, float* deltas, void* stream) {
+  TVM_TRY(validate_proposal(model, rays, cfg));
+  TVM_TRY(validate_params(model, params, shadow));
+  const int64_t R = rays->count;
+  TVM_REQUIRE(R == 0 || (sigmas && deltas), TVM_ERR_INVALID, "sigmas/deltas NULL");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  const float* p = static_cast<const float*>(params);
+  const PropMlp pm{model->proposal_units, p + L.proposal_w1, p + L.proposal_b1, p + L.proposal_w2,
+                   p + L.proposal_b2, cfg->proposal_shift, nullptr, sigmas};
+  return launch_prop_features(proposal_field(*model, L, p, shadow), rays->origins, rays->directions, R,
+                              proposal_sampler(*cfg), cfg->contract ? cfg->schedule : nullptr, cfg->proposal_jitter,
+                              nullptr, deltas, &pm, as_stream(stream));
+}
+
+int tvm_proposal_resample(const tvm_rays* rays, const tvm_render_desc* cfg, const float* weights, float* ts,
+                          float* deltas, int32_t* bins, void* stream) {
+  TVM_TRY(validate_rays(rays));
+  TVM_REQUIRE(cfg != nullptr, TVM_ERR_INVALID, "render descriptor is NULL");
+  TVM_REQUIRE(cfg->sampler == TVM_SAMPLER_PROPOSAL, TVM_ERR_INVALID, "the descriptor's sampler must be TVM_SAMPLER_PROPOSAL");
+  TVM_REQUIRE(cfg->proposal_samples >= 2 && cfg->proposal_samples <= 512, TVM_ERR_SHAPE,
+              "proposal_samples=%d outside [2, 512]", cfg->proposal_samples);
+  TVM_REQUIRE(cfg->density_samples >= 1 && cfg->density_samples <= 512, TVM_ERR_SHAPE,
+              "density_samples=%d outside [1, 512]", cfg->density_samples);
+  TVM_REQUIRE(!cfg->contract || cfg->schedule != nullptr, TVM_ERR_INVALID,
+              "unbounded proposal sampling needs the Np+1 bin edges in schedule");
+  const int64_t R = rays->count;
+  TVM_REQUIRE(R == 0 || (weights && cfg->jitter && ts && deltas && bins), TVM_ERR_INVALID,
+              "weights, jitter (R, N) and the outputs must be set");
+  for (int a = 0; a < 3; ++a)
+    TVM_REQUIRE(cfg->aabb[a] < cfg->aabb[3 + a], TVM_ERR_INVALID, "aabb min must be < max on every axis");
+  return launch_resample(weights, rays->origins, rays->directions, R, proposal_sampler(*cfg),
+                         cfg->contract ? cfg->schedule : nullptr, cfg->density_samples, cfg->jitter, ts, deltas, bins,
+                         as_stream(stream));
+}
+
+int tvm_proposal_loss(const float* main_weights, const float* proposal_weights, const int32_t* bins, int64_t rays,
+                      int32_t proposal_samples, int32_t samples, float scale, float* loss,
+                      float* grad_proposal_weights, void* stream) {
+  TVM_REQUIRE(rays >= 0 && rays <= (1LL << 31), TVM_ERR_SHAPE, "ray count out of range");
+  TVM_REQUIRE(proposal_samples >= 2 && proposal_samples <= 512 && samples >= 1 && samples <= 512, TVM_ERR_SHAPE,
+              "proposal_samples in [2, 512] and samples in [1, 512] required");
+  TVM_REQUIRE(rays == 0 || (main_weights && proposal_weights && bins && grad_proposal_weights), TVM_ERR_INVALID,
+              "NULL pointer");
+  return launch_prop_loss(main_weights, proposal_weights, bins, rays, proposal_samples, samples, scale, loss,
+                          grad_proposal_weights, as_stream(stream));
+}
+
+int tvm_proposal_bwd(const tvm_model_desc* model, const void* params, const void* shadow, void* grads,
+                     const tvm_rays* rays, const tvm_render_desc* cfg, const float* sigmas,
+                     const float* grad_sigmas, void* stream) {
+  TVM_TRY(validate_proposal(model, rays, cfg));
+  TVM_TRY(validate_params(model, params, shadow));
+  const int64_t R = rays->count;
+  TVM_REQUIRE(R == 0 || (sigmas && grad_sigmas), TVM_ERR_INVALID, "sigmas/grad_sigmas NULL");
+  TVM_REQUIRE(grads && aligned(grads, 16), TVM_ERR_ALIGN, "grads NULL or not 16-byte aligned");
+  tvm_param_layout L;
+  make_layout(*model, L);
+  const float* p = static_cast<const float*>(params);
+  float* g = static_cast<float*>(grads);
+  PropMlp pm{model->proposal_units, p + L.proposal_w1, p + L.proposal_b1, p + L.proposal_w2,
+             p + L.proposal_b2, cfg->proposal_shift, nullptr, nullptr};
+  pm.sigma_in = sigmas;
+  return launch_prop_bwd(proposal_field(*model, L, p, shadow), g + L.proposal_lines, g + L.proposal_planes,
+                         rays->origins, rays->directions, R, proposal_sampler(*cfg),
+                         cfg->contract ? cfg->schedule : nullptr, cfg->proposal_jitter, grad_sigmas, pm,
+                         g + L.proposal_w1, g + L.proposal_b1, g + L.proposal_w2, g + L.proposal_b2,
+                         as_stream(stream));
+}
+
 int tvm_render_fwd(const tvm_model_desc* model, const void* params, const void* shadow,
                    const tvm_rays* rays, const tvm_render_desc* cfg, float* out, void* workspace,
                    size_t workspace_bytes, void* stream) {

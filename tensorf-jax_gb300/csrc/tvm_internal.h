@@ -133,13 +133,14 @@ struct PropMlp {
   const float *w1, *b1, *w2, *b2;
   float shift;
   float* H;
-  float* sigma;
+  float* sigma;                    // forward: sigma out (may be NULL)
+  const float* sigma_in = nullptr;  // backward: if set, dz holds dL/dsigma of these sigmas
 };
 int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                          const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
                          cudaStream_t st);
-// Fused proposal backward from dz = dL/d(pre-softplus): field scatter and MLP weight
-// gradients (all accumulate).
+// Fused proposal backward from dz = dL/d(pre-softplus) (or dL/dsigma with
+// mlp.sigma_in): field scatter and MLP weight gradients (all accumulate).
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
                     const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st);

@@ -212,12 +212,21 @@ __global__ void __launch_bounds__(128) prop_features_kernel(
 // per weight per block.
 constexpr int PBWD_THREADS = 128;
 
+// dL/dz of sample i, z the proposal MLP's output before the shift and softplus: dz_in
+// holds it, or (sig_in set) dz_in holds dL/dsigma, scaled by dsigma/dz = sigmoid(z +
+// shift) = 1 - exp(-sigma) for sigma = softplus(z + shift).
+__device__ __forceinline__ float load_dz(const float* __restrict__ dz_in, const float* __restrict__ sig_in,
+                                         int64_t i) {
+  const float g = __ldg(dz_in + i);
+  return sig_in ? g * -expm1f(-__ldg(sig_in + i)) : g;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
     const T* __restrict__ lines, const T* __restrict__ planes, int G, float* __restrict__ glines,
     float* __restrict__ gplanes, const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R,
     SamplerArgs s, const float* __restrict__ edges, const float* __restrict__ jitter, const float* __restrict__ dz_in,
-    int units, const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
+    const float* __restrict__ sig_in, int units, const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
     float* __restrict__ gw1, float* __restrict__ gb1, float* __restrict__ gw2, float* __restrict__ gb2) {
   extern __shared__ __align__(16) float sm[];
   float* sw1 = sm;                          // transposed [U][16]
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
   const int Np = s.N;
   const int64_t smp = (int64_t)blockIdx.x * PBWD_THREADS + tid;
   const bool valid = smp < R * Np;
-  float dz = valid ? __ldg(dz_in + smp) : 0.f;
+  float dz = valid ? load_dz(dz_in, sig_in, smp) : 0.f;
   // A sample with dz = 0 adds nothing to any gradient (dh = 0, so dX, dW1, dW2 and db1
   // rows are all zero): its gathers and scatter are skipped.
   const bool live = valid && dz != 0.f;
@@ -442,37 +451,34 @@ __global__ void resample_kernel(const float* __restrict__ wprop, const float* __
   }
 }
 
-// Proposal bound loss and its gradient wrt w^ (one warp per ray).
+// Proposal bound loss and its gradient wrt w^ (one warp per ray). Each interval's bound
+// is summed directly over its bins: a difference of two prefix sums would lose the small
+// bounds of empty space to FP32 cancellation (the prefix reaches the ray's total mass).
+// The intervals tile the bins in order, so the direct sums read about Np + Nm values.
 __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* __restrict__ wprop,
                                  const int32_t* __restrict__ bins, int64_t R, int Np, int Nm, float scale,
                                  float* __restrict__ loss, float* __restrict__ gprop) {
   extern __shared__ float smem_f[];
   __shared__ float block_loss[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* C = smem_f + warp * 2 * (Np + 2);
-  float* diff = C + (Np + 2);
+  float* W = smem_f + warp * 2 * (Np + 2);
+  float* diff = W + (Np + 2);
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
   if (r >= R) {  // a whole warp past the last ray: it adds nothing to the block's loss
     if (lane == 0) block_loss[warp] = 0.f;
     __syncthreads();
     return;
   }
-  float carry = 0.f;
-  if (lane == 0) C[0] = 0.f;
-  for (int base = 0; base < Np; base += 32) {
-    const int j = base + lane;
-    const float q = (j < Np) ? __ldg(wprop + r * Np + j) : 0.f;
-    const float incl = warp_inclusive_scan(q, lane) + carry;
-    if (j < Np) C[j + 1] = incl;
-    carry = __shfl_sync(0xffffffffu, incl, 31);
-  }
+  for (int j = lane; j < Np; j += 32) W[j] = __ldg(wprop + r * Np + j);
   for (int j = lane; j < Np + 2; j += 32) diff[j] = 0.f;
   __syncwarp();
   float my_loss = 0.f;
   for (int i = lane; i < Nm; i += 32) {
-    const int lo = __ldg(bins + r * (Nm + 1) + i);
-    const int hi = __ldg(bins + r * (Nm + 1) + i + 1);
-    const float bound = C[hi + 1] - C[lo];
+    // Clamped into the ray's bins (the resampler's indices always are; a caller's may not).
+    const int lo = min(max(__ldg(bins + r * (Nm + 1) + i), 0), Np - 1);
+    const int hi = min(max(__ldg(bins + r * (Nm + 1) + i + 1), lo), Np - 1);
+    float bound = 0.f;
+    for (int j = lo; j <= hi; ++j) bound += W[j];
     const float w = __ldg(wmain + r * Nm + i);
     const float dd = fmaxf(w - bound, 0.f);
     const float inv = 1.0f / (w + 1e-7f);
@@ -494,7 +500,7 @@ __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* _
     atomicAdd(loss, t);
   }
   __syncwarp();
-  carry = 0.f;
+  float carry = 0.f;
   for (int base = 0; base < Np; base += 32) {
     const int j = base + lane;
     const float v = (j < Np) ? diff[j] : 0.f;
@@ -591,8 +597,8 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
     const __nv_bfloat16* __restrict__ lines, const __nv_bfloat16* __restrict__ planes, int G,
     float* __restrict__ glines, float* __restrict__ gplanes, const float* __restrict__ origins,
     const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
-    const float* __restrict__ jitter, const float* __restrict__ dz_in, const float* __restrict__ w1,
-    const float* __restrict__ b1, const float* __restrict__ w2, float* __restrict__ gw1, float* __restrict__ gb1,
+    const float* __restrict__ jitter, const float* __restrict__ dz_in, const float* __restrict__ sig_in,
+    const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2, float* __restrict__ gw1, float* __restrict__ gb1,
     float* __restrict__ gw2, float* __restrict__ gb2) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
@@ -652,7 +658,7 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int64_t smp = tile * THREADS + tid;
     const bool valid = smp < nsmp;
-    const float dz = valid ? __ldg(dz_in + smp) : 0.f;
+    const float dz = valid ? load_dz(dz_in, sig_in, smp) : 0.f;
     db2 += dz;
     // A sample with dz = 0 adds nothing to any gradient (its dH row is zero): it keeps a
     // zero row in the tile and skips its gathers and scatter.
@@ -820,7 +826,7 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
     const unsigned grid = (unsigned)std::min<int64_t>(tiles, std::max(sms, 1));
     ptc::prop_bwd_tc_kernel<<<grid, ptc::THREADS, ptc::SMEM, st>>>(
         (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines, gplanes, origins, dirs, R, s, edges,
-        jitter, dz, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2);
+        jitter, dz, mlp.sigma_in, mlp.w1, mlp.b1, mlp.w2, gw1, gb1, gw2, gb2);
     return check_launch("prop_bwd_tc");
   }
   const size_t smem = ((size_t)18 * U + PBWD_THREADS * 16 + 2 * PBWD_THREADS * (U + 4) + PBWD_THREADS) * sizeof(float);
@@ -829,14 +835,14 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
     auto fn = prop_bwd_kernel<__nv_bfloat16>;
     TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, glines,
-                                           gplanes, origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2,
+                                           gplanes, origins, dirs, R, s, edges, jitter, dz, mlp.sigma_in, U, mlp.w1, mlp.b1, mlp.w2,
                                            gw1, gb1, gw2, gb2);
   } else {
     auto fn = prop_bwd_kernel<float>;
     TVM_TRY(ensure_smem_limit((const void*)fn, (int)smem, "proposal backward"));
     fn<<<blocks, PBWD_THREADS, smem, st>>>((const float*)f.lines, (const float*)f.planes, f.G, glines, gplanes,
-                                           origins, dirs, R, s, edges, jitter, dz, U, mlp.w1, mlp.b1, mlp.w2, gw1, gb1,
-                                           gw2, gb2);
+                                           origins, dirs, R, s, edges, jitter, dz, mlp.sigma_in, U, mlp.w1, mlp.b1,
+                                           mlp.w2, gw1, gb1, gw2, gb2);
   }
   return check_launch("prop_bwd");
 }

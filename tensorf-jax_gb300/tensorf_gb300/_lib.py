@@ -97,7 +97,15 @@ _SIGNATURES = {
                               c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_mlp_fwd_static_scratch": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
                                             c_void_p]),
-    "tvm_loss_f64_workspace_size": (c_size_t, [POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
+    "tvm_proposal_fwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, POINTER(Rays), POINTER(RenderDesc),
+                                   c_void_p, c_void_p, c_void_p]),
+    "tvm_proposal_resample": (c_int32, [POINTER(Rays), POINTER(RenderDesc), c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p]),
+    "tvm_proposal_loss": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_int32, c_float, c_void_p,
+                                    c_void_p, c_void_p]),
+    "tvm_proposal_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, POINTER(Rays),
+                                   POINTER(RenderDesc), c_void_p, c_void_p, c_void_p]),
+    "tvm_loss_f64_workspace_size": (c_size_t,[POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
     "tvm_loss_f64": (c_int32, [POINTER(ModelDesc), c_void_p, POINTER(Rays), c_void_p, POINTER(RenderDesc), c_int64,
                                ctypes.c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_resize_field": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

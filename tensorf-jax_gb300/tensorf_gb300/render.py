@@ -609,3 +609,89 @@ def weighted_choice(p: torch.Tensor, gumbel: torch.Tensor, k: int) -> torch.Tens
     _lib.call("tvm_topk_select", ptr(p.contiguous()), ptr(gumbel.contiguous()), int(gumbel.dim() == 2), r, n, k,
               ptr(idx), stream_handle())
     return idx
+
+
+# Proposal network seams: the stages of proposal-guided sampling that render_rays and
+# training_step run fused, one call each. ``edges`` (Np + 1,) are the bin edges of
+# unbounded scenes (learnable_params.scene_contraction); bounded scenes split each ray's
+# aabb segment into Np uniform bins.
+def _proposal_desc(aabb, proposal: ProposalConfig, rays: int, contract: bool, edges, proposal_jitter=None,
+                   jitter=None, samples: int = 1):
+    d = _lib.RenderDesc()
+    d.sampler = _lib.TVM_SAMPLER_PROPOSAL
+    d.proposal_samples = proposal.samples
+    d.proposal_shift = proposal.shift
+    d.proposal_loss_weight = proposal.loss_weight
+    d.contract = int(contract)
+    d.density_samples = samples
+    d.appearance_samples = 1
+    d.mode = _MODE_CODE[RenderMode.DIST_MEAN]
+    for i, v in enumerate(_aabb6(aabb)):
+        d.aabb[i] = v
+    if contract and edges is None:
+        raise ValueError("unbounded proposal sampling needs the Np + 1 bin edges")
+    d.schedule = ptr(edges, torch.float32, "edges").value if contract else None
+    d.proposal_jitter = ptr(proposal_jitter, torch.float32, "proposal_jitter").value \
+        if proposal_jitter is not None else None
+    d.jitter = ptr(jitter, torch.float32, "jitter").value if jitter is not None else None
+    return d
+
+
+def proposal_forward(learnable_params: LearnableParams, aabb, rays_wrt_world: "cameras.Rays3D",
+                     proposal_jitter: torch.Tensor, proposal: ProposalConfig, edges: Optional[torch.Tensor] = None):
+    """tvm_proposal_fwd: proposal densities sigmas (R, Np) at one jittered point per bin
+    (proposal_jitter (R, Np)) and the bin lengths deltas (R, Np). The proposal weights
+    are compute_segment_probabilities(sigmas, deltas).p_terminates."""
+    r = rays_wrt_world.origins.reshape(-1, 3).shape[0]
+    desc = _proposal_desc(aabb, proposal, r, learnable_params.scene_contraction, edges, proposal_jitter)
+    md = learnable_params.model_desc()
+    sig = torch.empty((r, proposal.samples), dtype=torch.float32, device="cuda")
+    dl = torch.empty_like(sig)
+    _lib.call("tvm_proposal_fwd", ctypes.byref(md), ptr(learnable_params.params), ptr(learnable_params.shadow),
+              ctypes.byref(rays_struct(rays_wrt_world)), ctypes.byref(desc), ptr(sig), ptr(dl), stream_handle())
+    return sig, dl
+
+
+def proposal_backward(learnable_params: LearnableParams, grads: torch.Tensor, aabb, rays_wrt_world: "cameras.Rays3D",
+                      proposal_jitter: torch.Tensor, proposal: ProposalConfig, sigmas: torch.Tensor,
+                      grad_sigmas: torch.Tensor, edges: Optional[torch.Tensor] = None) -> None:
+    """tvm_proposal_bwd: the gradient of the proposal sigmas proposal_forward returned,
+    ACCUMULATED into the proposal segments of ``grads`` (flat layout)."""
+    r = rays_wrt_world.origins.reshape(-1, 3).shape[0]
+    desc = _proposal_desc(aabb, proposal, r, learnable_params.scene_contraction, edges, proposal_jitter)
+    md = learnable_params.model_desc()
+    _lib.call("tvm_proposal_bwd", ctypes.byref(md), ptr(learnable_params.params), ptr(learnable_params.shadow),
+              ptr(grads), ctypes.byref(rays_struct(rays_wrt_world)), ctypes.byref(desc),
+              ptr(sigmas, torch.float32, "sigmas"), ptr(grad_sigmas.contiguous(), torch.float32, "grad_sigmas"),
+              stream_handle())
+
+
+def proposal_resample(rays_wrt_world: "cameras.Rays3D", aabb, weights: torch.Tensor, jitter: torch.Tensor,
+                      samples: int, proposal: ProposalConfig, scene_contraction: bool = False,
+                      edges: Optional[torch.Tensor] = None):
+    """tvm_proposal_resample: proposal weights (R, Np) -> ``samples`` main intervals at
+    the quantiles of the padded histogram, one point each at jitter (R, N): ts, deltas
+    (R, N) and the proposal bin of each interval edge, bins (R, N + 1) int32."""
+    r = rays_wrt_world.origins.reshape(-1, 3).shape[0]
+    desc = _proposal_desc(aabb, proposal, r, scene_contraction, edges, jitter=jitter, samples=samples)
+    ts = torch.empty((r, samples), dtype=torch.float32, device="cuda")
+    dl = torch.empty_like(ts)
+    bins = torch.empty((r, samples + 1), dtype=torch.int32, device="cuda")
+    _lib.call("tvm_proposal_resample", ctypes.byref(rays_struct(rays_wrt_world)), ctypes.byref(desc),
+              ptr(weights.contiguous(), torch.float32, "weights"), ptr(ts), ptr(dl), ptr(bins), stream_handle())
+    return ts, dl, bins
+
+
+def proposal_loss(main_weights: torch.Tensor, proposal_weights: torch.Tensor, bins: torch.Tensor, scale: float):
+    """tvm_proposal_loss: scale * sum of max(0, w - bound)^2 / (w + 1e-7) over the main
+    intervals (bound: the proposal mass over each interval's bins) as a device scalar,
+    and its gradient with respect to proposal_weights (R, Np)."""
+    r, n = main_weights.shape
+    npb = proposal_weights.shape[1]
+    loss = torch.zeros(1, dtype=torch.float32, device=main_weights.device)
+    g = torch.empty_like(proposal_weights)
+    _lib.call("tvm_proposal_loss", ptr(main_weights.contiguous(), torch.float32, "main_weights"),
+              ptr(proposal_weights.contiguous(), torch.float32, "proposal_weights"),
+              ptr(bins.contiguous(), torch.int32, "bins"), r, npb, n, float(scale), ptr(loss), ptr(g),
+              stream_handle())
+    return loss, g

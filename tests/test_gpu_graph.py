@@ -7,7 +7,7 @@ graph path reads the Adam scalars and the noise key from device memory
 (tvm_set_step_scalars) and its batches are copied into fixed buffers. After several
 steps parameters and both moments agree to the order of the atomic gradient reductions
 (FP32: all but a handful of elements to 1e-5; BF16, where last-bit differences flip bf16
-roundings: no further from the eager run in norm than a second eager run is), the logged
+roundings: within 3x of a second eager run's distance plus 2e-3 in norm), the logged
 learning rates are equal, the replays ran (and counted) their kernels, and a grid resize
 records a new graph.
 """
@@ -33,6 +33,17 @@ def _dist(x, y):
     return float((x - y).norm() / x.norm())
 
 
+def _bf16_close(d, d_eager):
+    """BF16 runs drift apart chaotically: a last-bit difference flips a bf16 rounding
+    that every later gather reads. Two eager runs measured 4e-7 to 2e-5 apart (in norm)
+    after three steps and 1e-4 to 1e-3 after six, so one second run is a noisy
+    yardstick: the run under test may sit 3x further than it, plus 2e-3. A real ordering
+    fault (an update read before it lands, or applied twice) moves the parameters it
+    touches by a whole Adam step, about 1e-1 of their norm; the FP32 cases check the
+    same scheduling element by element."""
+    return d <= 3.0 * d_eager + 2e-3
+
+
 def _states(cfg, spec, graphs=(False, True)):
     from tensorf_gb300 import render, training
     return [training.TrainState(cfg, render.LearnableParams.initialize(spec, seed=4, scene_contraction=cfg.scene_contraction),
@@ -55,16 +66,16 @@ def _batches(R, n, seed, contract=False, cams=0):
     return out
 
 
-@pytest.mark.parametrize("case", ["bounded", "proposal_bf16", "contracted_cameras"])
+@pytest.mark.parametrize("case", ["bounded", "proposal_fp32", "proposal_bf16", "contracted_cameras"])
 def test_graph_steps_match_eager_steps(case):
     from tensorf_gb300 import render, training
     kw = dict(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
               appearance_samples_per_ray=8, density_shift=-1.0, n_iters=20, upsamp_iters=(3,))
     spec = render.ModelSpec(grid_dim=24)
     contract, cams = False, 0
-    if case == "proposal_bf16":
+    if case.startswith("proposal"):
         kw.update(density_samples_per_ray=32, proposal=render.ProposalConfig(samples=32))
-        spec = render.ModelSpec(grid_dim=24, precision="bf16", proposal_grid=16)
+        spec = render.ModelSpec(grid_dim=24, precision=case[-4:], proposal_grid=16)
     if case == "contracted_cameras":
         kw.update(initial_aabb_min=(-2.0,) * 3, initial_aabb_max=(2.0,) * 3, scene_contraction=True)
         spec = render.ModelSpec(grid_dim=24, num_cameras=3)
@@ -90,7 +101,7 @@ def test_graph_steps_match_eager_steps(case):
         get = (lambda st: st.learnable_params.params) if name == "params" else (lambda st: getattr(st, name))
         if bf16:
             d_graph, d_eager = _dist(get(eager), get(graph)), _dist(get(eager), get(states[2]))
-            assert d_graph <= 3.0 * d_eager + 1e-6, (name, d_graph, d_eager)
+            assert _bf16_close(d_graph, d_eager), (name, d_graph, d_eager)
         else:
             ok, n_off = _close(get(eager), get(graph))
             assert ok, (name, n_off)
@@ -153,7 +164,7 @@ def test_keyed_noise_equals_key_drawn_noise(proposal):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("case", ["bounded", "proposal_bf16"])
+@pytest.mark.parametrize("case", ["bounded", "proposal_fp32", "proposal_bf16"])
 def test_deferred_field_updates_match_immediate(case, graph):
     """Steps that leave the fields' Adam update pending (applied by the next step beside
     its start, or when parameters are read) against steps that update at once: equal
@@ -162,9 +173,9 @@ def test_deferred_field_updates_match_immediate(case, graph):
     kw = dict(initial_aabb_min=(-1.5,) * 3, initial_aabb_max=(1.5,) * 3, density_samples_per_ray=64,
               appearance_samples_per_ray=8, density_shift=-1.0, n_iters=20, upsamp_iters=(3,))
     spec = render.ModelSpec(grid_dim=24)
-    if case == "proposal_bf16":
+    if case.startswith("proposal"):
         kw.update(density_samples_per_ray=32, proposal=render.ProposalConfig(samples=32))
-        spec = render.ModelSpec(grid_dim=24, precision="bf16", proposal_grid=16)
+        spec = render.ModelSpec(grid_dim=24, precision=case[-4:], proposal_grid=16)
     cfg = training.TrainConfig(**kw)
     bf16 = spec.precision == "bf16"
 
@@ -181,7 +192,7 @@ def test_deferred_field_updates_match_immediate(case, graph):
             get = (lambda st: st.learnable_params.params) if name == "params" else (lambda st: getattr(st, name))
             if bf16:
                 d_def, d_eager = _dist(get(ref), get(dfr)), _dist(get(ref), get(states[2]))
-                assert d_def <= 3.0 * d_eager + 1e-6, (name, d_def, d_eager)
+                assert _bf16_close(d_def, d_eager), (name, d_def, d_eager)
             else:
                 ok, n_off = _close(get(ref), get(dfr))
                 assert ok, (name, n_off)
