@@ -284,7 +284,7 @@ TVM_API int tvm_topk_select(const float* p, const float* gumbel, int32_t gumbel_
 
 /* ---- (d) FeatureMlp (networks.py:45-121) --------------------------------------------- */
 /* features (n, 3*C_a), viewdirs (n, 3) -> rgb (n, 3). params: flat buffer in the
- * tvm_param_layout layout (master dtype float32; TVM_BF16 models use bf16 tensor
+ * tvm_param_layout layout, 16-byte aligned (master dtype float32; TVM_BF16 models use bf16 tensor
  * cores, TVM_F32 models float32 arithmetic). camera_indices (n,): camera of each row
  * for models with num_cameras > 0 (networks.py:103-111), else NULL. workspace:
  * tvm_mlp_workspace_size(). Models with camera embeddings run the layered GEMMs with a

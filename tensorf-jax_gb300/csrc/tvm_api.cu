@@ -303,10 +303,17 @@ struct PassBufs {
   float* sigma;
   int32_t* sel;
   float *w_sel, *p_last, *q_last, *wsum, *X0, *rgb, *dZ3, *gw, *gP, *gsum, *dX0;
+  uint8_t* X0t;  // the FeatureMlp input as tiles (BF16 models on the fused kernels), else X0
   // proposal-guided sampling
   float *sig_p, *delta_p, *w_p, *t_main, *d_main, *w_dense, *g_wp, *dz_p, *loss_p;
   int32_t* bins;
 };
+
+// BF16 models whose FeatureMlp runs on the fused kernels take its input as tiles
+// (launch_appearance_fwd_tiles): bf16 in the kernels' operand layout, one bulk copy each.
+static bool uses_input_tiles(const tvm_model_desc& m, const tvm_render_desc& c) {
+  return m.dtype == TVM_BF16 && c.mode == TVM_MODE_RGB && mlp_fused_supported(mlp_dims(m));
+}
 
 static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, int64_t R,
                            bool backward, Workspace& ws) {
@@ -321,7 +328,10 @@ static PassBufs carve_pass(const tvm_model_desc& m, const tvm_render_desc& c, in
   b.p_last = ws.take<float>(R);
   b.q_last = ws.take<float>(R);
   b.wsum = ws.take<float>(R);
-  b.X0 = ws.take<float>(M * F);
+  if (uses_input_tiles(m, c))
+    b.X0t = ws.take<uint8_t>(x0t_bytes(M));
+  else
+    b.X0 = ws.take<float>(M * F);
   b.rgb = ws.take<float>(M * 3);
   if (backward) {
     b.dZ3 = ws.take<float>(M * 3);
@@ -552,7 +562,10 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
     cudaError_t e = cudaStreamWaitEvent(st, pend_side->appearance_ready, 0);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "pending update join: %s", cudaGetErrorString(e));
   }
-  TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
+  if (b.X0t)
+    TVM_TRY(launch_appearance_fwd_tiles(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0t, st));
+  else
+    TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(4, st);
   const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
@@ -564,7 +577,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   // so a pass on one stream keeps the whole GPU for them.
   const int shared_ctas = device_sms() / 2;
   TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, rays.camera_indices, k, R * k, b.rgb, ws, st,
-                      overlap && prop_forked ? shared_ctas : 0));
+                      overlap && prop_forked ? shared_ctas : 0, b.X0t));
   phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,
@@ -588,7 +601,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   }
   Workspace ws2{static_cast<char*>(workspace), ws_bytes, mlp_off, false};
   TVM_TRY(mlp_backward(d, w, mlp_grads(L, grads), b.X0, rays.directions, rays.camera_indices, k, R * k, b.dZ3,
-                       b.dX0, ws2, ab, overlap ? shared_ctas : 0));
+                       b.dX0, ws2, ab, overlap ? shared_ctas : 0, b.X0t));
   phase_mark(7, st);
   TVM_TRY(launch_appearance_bwd(fa, grads + L.appearance_lines, grads + L.appearance_planes,
                                 rays.origins, rays.directions, R, s, b.sel, k, b.dX0, ab));
@@ -750,6 +763,7 @@ int tvm_mlp_fwd(const tvm_model_desc* model, const void* params, const float* fe
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
   TVM_REQUIRE(n == 0 || (params && features && viewdirs && rgb && workspace), TVM_ERR_INVALID,
               "NULL pointer");
+  TVM_REQUIRE(aligned(params, 16), TVM_ERR_ALIGN, "params must be 16-byte aligned");
   TVM_REQUIRE(n == 0 || model->num_cameras == 0 || camera_indices, TVM_ERR_INVALID,
               "a model with camera embeddings needs camera_indices");
   tvm_param_layout L;
@@ -766,6 +780,7 @@ int tvm_mlp_bwd(const tvm_model_desc* model, const void* params, const float* fe
   TVM_REQUIRE(n >= 0, TVM_ERR_SHAPE, "n < 0");
   TVM_REQUIRE(n == 0 || (params && features && viewdirs && grad_rgb && grads && workspace),
               TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(params, 16) && aligned(grads, 16), TVM_ERR_ALIGN, "params and grads must be 16-byte aligned");
   TVM_REQUIRE(n == 0 || model->num_cameras == 0 || camera_indices, TVM_ERR_INVALID,
               "a model with camera embeddings needs camera_indices");
   if (n == 0) return TVM_OK;

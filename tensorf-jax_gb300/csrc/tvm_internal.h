@@ -36,6 +36,18 @@ int launch_density_bwd(const FieldView& f, float* glines, float* gplanes, const 
 int launch_appearance_fwd(const FieldView& f, const float* origins, const float* dirs, int64_t R,
                           const SamplerArgs& s, const int32_t* sel_idx, int k, float* X0,
                           cudaStream_t st);
+// FeatureMlp input tiles of BF16 models: X0 stored as the fused MLP kernels' A-operand
+// images, one per 128 rows: 144 bf16 features per row in the tcgen05 K-major canonical
+// layout (core matrices of 8 rows x 16 bytes, K-chunks 128 bytes apart, 8-row groups
+// 2304 bytes apart). One bulk copy moves a tile into shared memory. Rows past the last
+// are zero.
+constexpr int X0T_ROWS = 128, X0T_FEAT = 144, X0T_SBO = (X0T_FEAT / 8) * 128;
+constexpr int64_t X0T_TILE_BYTES = (int64_t)X0T_ROWS * X0T_FEAT * 2;
+inline int64_t x0t_bytes(int64_t M) { return ((M + X0T_ROWS - 1) / X0T_ROWS) * X0T_TILE_BYTES; }
+// appearance_fwd writing tiles (bf16 fields with 48 channels per pair only).
+int launch_appearance_fwd_tiles(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                                const SamplerArgs& s, const int32_t* sel_idx, int k, uint8_t* X0t,
+                                cudaStream_t st);
 int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
                           const float* dirs, int64_t R, const SamplerArgs& s,
                           const int32_t* sel_idx, int k, const float* dX0, cudaStream_t st);
@@ -95,15 +107,17 @@ size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M);  // forward only (a
 // rgb = FeatureMlp(X0, viewdir, camera). Viewdir of row m is dirs[(m / rows_per_dir) * 3 ...],
 // its camera cams[m / rows_per_dir] (cams is read only when d.cams > 0).
 // max_ctas: the fused BF16 kernels' grid cap (launch_mlp_fwd_fused), 0 for one CTA per SM.
+// X0t: the input as tiles (launch_appearance_fwd_tiles) instead of X0; fused path only.
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
-                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas = 0);
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas = 0,
+                const uint8_t* X0t = nullptr);
 // Needs the preceding mlp_forward on the same workspace: its kept row-major activations
 // (layered path), or its packed bf16 weights (fused path, which recomputes the forward
 // from X0 and the view directions).
 // dZ3: gradient wrt the pre-sigmoid output (M,3). dX0 may be null.
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                  const int32_t* cams, int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws,
-                 cudaStream_t st, int max_ctas = 0);
+                 cudaStream_t st, int max_ctas = 0, const uint8_t* X0t = nullptr);
 int gemm_any(int math, bool at, bool bt, int64_t M, int N, int64_t K, const float* A, int64_t lda,
              const float* B, int64_t ldb, float* D, int64_t ldd, bool accumulate, cudaStream_t st);
 int device_status(int32_t* out, cudaStream_t st);  // copy + clear the tensor-core status word
@@ -114,14 +128,16 @@ bool mlp_fused_supported(const MlpDims& d);
 size_t mlp_fused_pack_bytes();
 // max_ctas > 0 caps the persistent grid (fewer CTAs each take more tiles), leaving the
 // other SMs to kernels that run beside it on other streams; 0: one CTA per SM.
+// X0t: input tiles instead of the row-major X0 (which is then not read).
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas = 0);
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas = 0,
+                         const uint8_t* X0t = nullptr);
 // Fused BF16 backward: recomputes the forward per tile, accumulates all weight and
 // bias gradients into g, writes dX0 (M, 144) when non-null. wpack: the images packed by
 // launch_mlp_fwd_fused.
 int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                          int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
-                         cudaStream_t st, int max_ctas = 0);
+                         cudaStream_t st, int max_ctas = 0, const uint8_t* X0t = nullptr);
 int launch_sigmoid_bwd(const float* rgb, const float* grad_rgb, int64_t M, float* dZ3,
                        cudaStream_t st);
 

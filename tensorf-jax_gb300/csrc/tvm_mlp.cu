@@ -648,7 +648,8 @@ size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M) {
 }
 
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
-                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas) {
+                int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas,
+                const uint8_t* X0t) {
   MlpBufs b = carve(d, M, ws, true);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
@@ -658,7 +659,11 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
   if (mlp_fused_supported(d)) {
     // BF16: all four layers in one tcgen05 kernel. Nothing is kept for the backward,
     // which recomputes the activations from X0 (only the packed weights are reused).
-    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st, max_ctas);
+    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st, max_ctas, X0t);
+  }
+  if (X0t) {
+    set_error("mlp: input tiles need the fused BF16 kernels");
+    return TVM_ERR_UNSUPPORTED;
   }
   if (pmlp_supported(d)) {
     const pg::PackJob jobs[3] = {{w.w0, d.squash, d.feat, d.squash, pg::kpad(d.feat), 32, 0, b.img[0]},
@@ -715,14 +720,18 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
 
 int mlp_backward(const MlpDims& d, const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                  const int32_t* cams, int rows_per_dir, int64_t M, const float* dZ3, float* dX0, Workspace& ws,
-                 cudaStream_t st, int max_ctas) {
+                 cudaStream_t st, int max_ctas, const uint8_t* X0t) {
   MlpBufs b = carve(d, M, ws, false);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
     return TVM_ERR_WORKSPACE;
   }
   if (mlp_fused_supported(d)) {
-    return launch_mlp_bwd_fused(w, g, X0, dirs, rows_per_dir, M, dZ3, dX0, b.wpack, st, max_ctas);
+    return launch_mlp_bwd_fused(w, g, X0, dirs, rows_per_dir, M, dZ3, dX0, b.wpack, st, max_ctas, X0t);
+  }
+  if (X0t) {
+    set_error("mlp: input tiles need the fused BF16 kernels");
+    return TVM_ERR_UNSUPPORTED;
   }
   const int l1 = ld_x1(d);
   const int64_t kc = -1;  // weight gradients: split-K over the rows, sized per GEMM

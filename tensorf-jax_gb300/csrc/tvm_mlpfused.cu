@@ -126,6 +126,41 @@ __device__ __forceinline__ void load_x0_tile(uint8_t* dst, int sbo, const float*
   }
 }
 
+// Fourier encoding of one row (networks.py:13-35, 68-76) into its K-chunks of the X1
+// tile. Columns: [h (27) | d (3) | PE(h): 4 per feature | PE(d): 4 per axis | `tail` at
+// column 150 | zeros to 160], PE(v) = [sin v, sin 2v, sin(v + pi/2), sin(2v + pi/2)]
+// computed as [s, 2sc, c, c^2 - s^2] from one sincos. v = [h0..h26, d0..d2]. Warp half
+// HALF writes chunks 10*HALF .. 10*HALF + 9, each with one 16-byte store: 2-byte stores
+// at the canonical positions of eight rows apart meet in the same banks.
+__device__ __forceinline__ float enc_value(int c, const float (&v)[SQ + 3], const float (&sn)[SQ + 3],
+                                           const float (&cs)[SQ + 3], float tail) {
+  if (c < SQ + 3) return v[c];
+  if (c < ENC) {
+    const int f = (c - SQ - 3) >> 2, q = (c - SQ - 3) & 3;
+    return q == 0 ? sn[f] : q == 1 ? 2.0f * sn[f] * cs[f] : q == 2 ? cs[f] : cs[f] * cs[f] - sn[f] * sn[f];
+  }
+  return c == ENC ? tail : 0.0f;
+}
+
+template <int HALF>
+__device__ __forceinline__ void encode_row(uint8_t* xrow, const float (&v)[SQ + 3], float tail) {
+  constexpr int K0 = HALF * (ENCP / 16);                          // first K-chunk of this half
+  constexpr int F0 = (K0 * 8 - SQ - 3) > 0 ? (K0 * 8 - SQ - 3) / 4 : 0;
+  constexpr int F1c = ((K0 + ENCP / 16) * 8 - SQ - 3 + 3) / 4;   // features whose PE these chunks hold
+  constexpr int F1 = F1c < SQ + 3 ? F1c : SQ + 3;
+  float sn[SQ + 3], cs[SQ + 3];
+#pragma unroll
+  for (int f = F0; f < F1; ++f) __sincosf(v[f], &sn[f], &cs[f]);
+#pragma unroll
+  for (int k = K0; k < K0 + ENCP / 16; ++k) {
+    float e[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) e[i] = enc_value(8 * k + i, v, sn, cs, tail);
+    *reinterpret_cast<uint4*>(xrow + k * 128) =
+        make_uint4(pack2(e[0], e[1]), pack2(e[2], e[3]), pack2(e[4], e[5]), pack2(e[6], e[7]));
+  }
+}
+
 __device__ __forceinline__ void issue(uint32_t tmem_d, uint32_t a, uint32_t b, int ksteps, uint32_t sbo_a,
                                       uint32_t sbo_b, uint32_t idesc) {
 #pragma unroll 1
@@ -148,16 +183,23 @@ __global__ void pack_weights_kernel(uint8_t* __restrict__ out, const float* __re
   stage_weight(out + OFF_W3, w3, 3, OUTP, U, 3, U, tid, n);
 }
 
+static_assert(X0T_ROWS == BM && X0T_FEAT == F && X0T_SBO == SBO_F, "input tiles are the A0 image");
+
 struct Args {
   int64_t M;
   const uint8_t* wpack;  // WPACK_BYTES of packed weights (16-byte aligned)
-  const float* X0;     // (M, 144)
+  const float* X0;     // (M, 144), or
+  const uint8_t* X0t;  // the same as input tiles (TILES kernels)
   const float* dirs;   // view direction of row m: dirs[(m / rows_per_dir) * 3 ...]
   int rows_per_dir;
   const float *w0, *w1, *b1, *w2, *b2, *w3, *b3;
   float* rgb;          // (M, 3)
 };
 
+// TILES: X0 arrives as input tiles, one bulk copy per tile into A0 (issued as soon as
+// layer 2 has read H1 from A0, waited for before layer 0). Otherwise from the row-major
+// fp32 X0 through registers.
+template <bool TILES>
 __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
@@ -166,16 +208,30 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   const int sub = warp & 3, half = warp >> 2;
 
   uint64_t* wbar = mbar + 2;
+  uint64_t* xbar = mbar + 3;  // input tile copies (TILES)
   if (warp == 0) tc::tmem_alloc(tslot, 512);
   if (tid == 0) {
     tc::mbar_init(mbar, 1);
     tc::mbar_init(wbar, 1);
+    tc::mbar_init(xbar, 1);
   }
   __syncthreads();
-  if (tid == 0) {  // one TMA bulk copy brings all weights in
+  const int64_t ntiles = (a.M + BM - 1) / BM;
+  if (tid == 0) {  // one TMA bulk copy brings all weights in (and the first input tile)
     tc::mbar_expect_tx(wbar, WPACK_BYTES);
     tc::bulk_g2s(smem + OFF_W0, a.wpack, WPACK_BYTES, wbar);
+    if (TILES && (int64_t)blockIdx.x < ntiles) {
+      tc::mbar_expect_tx(xbar, (uint32_t)X0T_TILE_BYTES);
+      tc::bulk_g2s(smem + OFF_A0, a.X0t + (int64_t)blockIdx.x * X0T_TILE_BYTES, (uint32_t)X0T_TILE_BYTES, xbar);
+    }
   }
+  // Row-major X0: the first tile (128 rows x 18 chunks of 8 features) is loaded while the
+  // weights travel; each later one is fetched into registers during layer 1's epilogue
+  // and layer 2's MMA and stored into the A0 tile once that MMA has read H1 from it.
+  if (!TILES && (int64_t)blockIdx.x < ntiles)
+    load_x0_tile(smem + OFF_A0, SBO_F, a.X0, (int64_t)blockIdx.x * BM, a.M, tid);
+  bool x_pending = TILES && (int64_t)blockIdx.x < ntiles;  // a tile copy not yet waited for
+  uint32_t xphase = 0;
   int ok = tc::mbar_wait(wbar, 0, WAIT_LIMIT) ? 1 : 0;
   ok = __syncthreads_and(ok);
   tc::fence_before_sync();
@@ -204,110 +260,97 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
     return all != 0;
   };
 
-  const int64_t ntiles = (a.M + BM - 1) / BM;
-  // The X0 tile (128 rows x 18 chunks of 8 features) of the first tile is loaded here;
-  // each later one is fetched into registers while layer 2's MMA runs and stored into
-  // the A0 tile once that MMA has read H1 from it.
-  if ((int64_t)blockIdx.x < ntiles) load_x0_tile(smem + OFF_A0, SBO_F, a.X0, (int64_t)blockIdx.x * BM, a.M, tid);
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int64_t m0 = tile * BM;
     const int64_t next = tile + gridDim.x;
     {  // the tile after the next one travels to L2 while this tile computes
-      const int64_t nm0 = (next + gridDim.x) * BM;
+      const int64_t nt = next + gridDim.x, nm0 = nt * BM;
       if (nm0 < a.M) {
-        const int64_t nbytes = (a.M - nm0 < BM ? a.M - nm0 : BM) * F * 4;
-        for (int64_t off = (int64_t)tid * 128; off < nbytes; off += THREADS * 128)
-          tc::prefetch_l2(reinterpret_cast<const char*>(a.X0 + nm0 * F) + off);
+        const char* src = TILES ? reinterpret_cast<const char*>(a.X0t + nt * X0T_TILE_BYTES)
+                                : reinterpret_cast<const char*>(a.X0 + nm0 * F);
+        const int64_t nbytes = TILES ? X0T_TILE_BYTES : (a.M - nm0 < BM ? a.M - nm0 : BM) * F * 4;
+        for (int64_t off = (int64_t)tid * 128; off < nbytes; off += THREADS * 128) tc::prefetch_l2(src + off);
+      }
+    }
+    if (TILES) {  // this tile's input, copied in during the previous tile
+      const int got = tc::mbar_wait(xbar, xphase, WAIT_LIMIT) ? 1 : 0;
+      if (!__syncthreads_and(got)) { ok = 0; break; }
+      xphase ^= 1u;
+      x_pending = false;
+    }
+    // The row's view direction, read now so that its latency passes under layer 0.
+    float dir[3] = {0.f, 0.f, 0.f};
+    {
+      const int64_t row = m0 + sub * 32 + lane;
+      if (row < a.M) {
+        const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
+        dir[0] = __ldg(dp);
+        dir[1] = __ldg(dp + 1);
+        dir[2] = __ldg(dp + 2);
       }
     }
     if (!layer(D0, OFF_A0, OFF_W0, F / 16, SBO_F, SBO_F, SQP)) { ok = 0; break; }
 
-    // Fourier encoding (networks.py:13-35, 68-76), row r = 32*sub + lane. X1 columns:
-    // [h (27) | d (3) | PE(h): 4 per feature | PE(d): 4 per axis | zero pad to 160], PE(v)
-    // = [sin v, sin 2v, sin(v + pi/2), sin(2v + pi/2)] computed as [s, 2sc, c, c^2 - s^2]
-    // from one sincos. Warp half 0 encodes features 0..13, half 1 features 14..26, the
-    // direction and the padding. Each value is one 2-byte store at its canonical position.
+    // Fourier encoding of row r = 32*sub + lane into X1 (encode_row): both warp halves
+    // read the row's 27 squashed features and its direction, and each writes ten K-chunks.
     {
       const int r = sub * 32 + lane;
-      const int64_t row = m0 + r;
+      float v[SQ + 3], v16[16];
+      tc::tmem_ld16(D0 + lane_off, v16);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = v16[j];
+      tc::tmem_ld16(D0 + lane_off + 16, v16);
+#pragma unroll
+      for (int j = 16; j < SQ; ++j) v[j] = v16[j - 16];
+      v[SQ] = dir[0];
+      v[SQ + 1] = dir[1];
+      v[SQ + 2] = dir[2];
       uint8_t* xrow = smem + OFF_A1 + (r >> 3) * SBO_E + (r & 7) * 16;
-      auto put = [&](int col, float v) {
-        *reinterpret_cast<__nv_bfloat16*>(xrow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
-      };
-      auto pe4 = [&](int col, float v) {
-        float sn, cs;
-        __sincosf(v, &sn, &cs);
-        put(col, sn);
-        put(col + 1, 2.0f * sn * cs);
-        put(col + 2, cs);
-        put(col + 3, cs * cs - sn * sn);
-      };
-      float v16[16];
-      if (half == 0) {
-        tc::tmem_ld16(D0 + lane_off, v16);
-#pragma unroll
-        for (int j = 0; j < 14; ++j) {
-          put(j, v16[j]);
-          pe4(SQ + 3 + 4 * j, v16[j]);
-        }
-      } else {
-        tc::tmem_ld16(D0 + lane_off, v16);  // columns 0..15: 14 and 15 are this half's
-        const float h14 = v16[14], h15 = v16[15];
-        tc::tmem_ld16(D0 + lane_off + 16, v16);
-        put(14, h14);
-        pe4(SQ + 3 + 4 * 14, h14);
-        put(15, h15);
-        pe4(SQ + 3 + 4 * 15, h15);
-#pragma unroll
-        for (int j = 16; j < SQ; ++j) {
-          put(j, v16[j - 16]);
-          pe4(SQ + 3 + 4 * j, v16[j - 16]);
-        }
-        float d[3] = {0.f, 0.f, 0.f};
-        if (row < a.M) {
-          const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
-          d[0] = __ldg(dp);
-          d[1] = __ldg(dp + 1);
-          d[2] = __ldg(dp + 2);
-        }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          put(SQ + q, d[q]);
-          pe4(SQ + 3 + 4 * SQ + 4 * q, d[q]);
-        }
-#pragma unroll
-        for (int c = ENC; c < ENCP; ++c)
-          *reinterpret_cast<__nv_bfloat16*>(xrow + (c >> 3) * 128 + (c & 7) * 2) = __float2bfloat16_rn(0.f);
-      }
+      if (half == 0)
+        encode_row<0>(xrow, v, 0.f);
+      else
+        encode_row<1>(xrow, v, 0.f);
     }
     if (!layer(D1, OFF_A1, OFF_W1, ENCP / 16, SBO_E, SBO_E, U)) { ok = 0; break; }
 
-    // Hidden layers: +bias, ReLU, bf16 into the next A tile.
+    // Hidden layers: +bias, ReLU, bf16 into the next A tile. Warp half h takes columns
+    // [64h, 64h + 64) of its rows: one TMEM load, float4 bias loads, 16-byte stores.
     auto hidden = [&](uint32_t Dsrc, const float* bias, int dst_off) {
       const int r = sub * 32 + lane;
-      for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
-        float vv[2][16];
-        tc::tmem_ld16x2(Dsrc + lane_off + cp * 16, Dsrc + lane_off + (cp + 1) * 16, vv[0], vv[1]);
+      float v[64];
+      tc::tmem_ld64(Dsrc + lane_off + half * 64, v);
+      const float4* b4 = reinterpret_cast<const float4*>(bias + half * 64);
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int ch = cp + u;
-          float* v = vv[u];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
-#pragma unroll
-          for (int q = 0; q < 2; ++q) {
-            *reinterpret_cast<uint4*>(smem + dst_off + coff(r, ch * 2 + q, SBO_U)) =
-                make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
-                           pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
-          }
-        }
+      for (int j = 0; j < 16; ++j) {
+        const float4 b = __ldg(b4 + j);
+        v[4 * j] = fmaxf(v[4 * j] + b.x, 0.f);
+        v[4 * j + 1] = fmaxf(v[4 * j + 1] + b.y, 0.f);
+        v[4 * j + 2] = fmaxf(v[4 * j + 2] + b.z, 0.f);
+        v[4 * j + 3] = fmaxf(v[4 * j + 3] + b.w, 0.f);
       }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<uint4*>(smem + dst_off + coff(r, half * 8 + q, SBO_U)) =
+            make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                       pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
     };
+    float4 xp[X0_PER_THREAD], xq[X0_PER_THREAD];  // row-major X0 only
+    if constexpr (!TILES) {
+      if (next < ntiles) x0_fetch(xp, xq, a.X0, next * BM, a.M, tid);  // in flight during hidden1, layer 2
+    }
     hidden(D1, a.b1, OFF_A0);
-    float4 xp[X0_PER_THREAD], xq[X0_PER_THREAD];
-    if (next < ntiles) x0_fetch(xp, xq, a.X0, next * BM, a.M, tid);  // in flight during layer 2
     if (!layer(D2, OFF_A0, OFF_W2, U / 16, SBO_U, SBO_U, U)) { ok = 0; break; }
-    if (next < ntiles) x0_store(xp, xq, smem + OFF_A0, SBO_F, tid);  // layer 2 has read H1 from A0
+    if (next < ntiles) {  // layer 2 has read H1 from A0: the next tile's input goes there
+      if constexpr (TILES) {
+        if (tid == 0) {
+          tc::mbar_expect_tx(xbar, (uint32_t)X0T_TILE_BYTES);
+          tc::bulk_g2s(smem + OFF_A0, a.X0t + next * X0T_TILE_BYTES, (uint32_t)X0T_TILE_BYTES, xbar);
+        }
+        x_pending = true;
+      } else {
+        x0_store(xp, xq, smem + OFF_A0, SBO_F, tid);
+      }
+    }
     hidden(D2, a.b2, OFF_A1);
     if (!layer(D3, OFF_A1, OFF_W3, U / 16, SBO_U, SBO_U, OUTP)) { ok = 0; break; }
     if (half == 0) {
@@ -326,8 +369,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_fwd_fused_kernel(Args a) {
   }
   if (!ok) {
     if (tid == 0) atomicOr(&g_fused_status, 1);
-    tc::mbar_wait(wbar, 0, WAIT_LIMIT);           // the weight copy, if it is still in flight
-    tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);  // drain the MMAs in flight before freeing TMEM
+    tc::mbar_wait(wbar, 0, WAIT_LIMIT);             // the weight copy, if it is still in flight
+    if (x_pending) tc::mbar_wait(xbar, xphase, WAIT_LIMIT);  // and an input tile copy
+    tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);    // drain the MMAs in flight before freeing TMEM
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -399,7 +443,8 @@ __device__ __forceinline__ void mma_run(uint32_t d, Op a, Op b, int ksteps, uint
 struct Args {
   int64_t M;
   const uint8_t* wpack;  // the forward's packed weight images (WPACK_BYTES)
-  const float* X0;       // (M, 144)
+  const float* X0;       // (M, 144), or
+  const uint8_t* X0t;    // the same as input tiles (TILES kernels)
   const float* dirs;
   int rows_per_dir;
   const float *b1, *b2;
@@ -444,10 +489,15 @@ __device__ __forceinline__ void encoding_bwd(uint32_t taddr, const float* hrow, 
   }
 }
 
+// TILES: each tile's input arrives by bulk copies into RA, for layer 0 (issued when the
+// previous tile's dW0 product has read RA) and again for dW0 (issued when dH1's products
+// have read RA). Otherwise from the row-major fp32 X0 through registers, at those points.
+template <bool TILES>
 __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + BAR);
   uint64_t* wbar = mbar + 1;
+  uint64_t* xbar = mbar + 3;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + BAR + 16);
   float* hstash = reinterpret_cast<float*>(smem + RF);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -458,6 +508,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
   if (tid == 0) {
     tc::mbar_init(mbar, 1);
     tc::mbar_init(wbar, 1);
+    tc::mbar_init(xbar, 1);
   }
   // Constant tile e3 (column 3 = 1): dH2^T e3 accumulates db2 into column 3 of dW3.
   for (int c = tid; c < BM * 2; c += THREADS) {
@@ -467,10 +518,29 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
     *reinterpret_cast<uint4*>(smem + RE3 + coff(row, kc, SBO_Z)) = v;
   }
   __syncthreads();
+  const int64_t ntiles = (a.M + BM - 1) / BM;
+  // Input tile copies into RA: issue_x0 (thread 0) and wait_x0 (everyone).
+  bool x_pending = false;
+  uint32_t xphase = 0;
+  auto issue_x0 = [&](int64_t t) {
+    if (tid == 0) {
+      tc::mbar_expect_tx(xbar, (uint32_t)X0T_TILE_BYTES);
+      tc::bulk_g2s(smem + RA, a.X0t + t * X0T_TILE_BYTES, (uint32_t)X0T_TILE_BYTES, xbar);
+    }
+    x_pending = true;
+  };
+  auto wait_x0 = [&]() -> bool {
+    const int got = tc::mbar_wait(xbar, xphase, WAIT_LIMIT) ? 1 : 0;
+    if (!__syncthreads_and(got)) return false;
+    xphase ^= 1u;
+    x_pending = false;
+    return true;
+  };
   if (tid == 0) {
     tc::mbar_expect_tx(wbar, WPACK_BYTES);
     tc::bulk_g2s(smem + OFF_W0, a.wpack, WPACK_BYTES, wbar);
   }
+  if (TILES && (int64_t)blockIdx.x < ntiles) issue_x0(blockIdx.x);
   int ok = tc::mbar_wait(wbar, 0, WAIT_LIMIT) ? 1 : 0;
   ok = __syncthreads_and(ok);
   tc::fence_before_sync();
@@ -503,55 +573,52 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
     load_x0_tile(smem + RA, SBO_A, a.X0, m0, a.M, tid);
   };
   // +bias, ReLU, bf16 into a natural tile.
+  // Warp half h takes columns [64h, 64h + 64) of its rows: one TMEM load, float4 bias
+  // loads, 16-byte stores.
   auto hidden = [&](const float* bias, int dst, int sbo) {
-    for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
-      float vv[2][16];
-      tc::tmem_ld16x2(tmem + T_CH + lane_off + cp * 16, tmem + T_CH + lane_off + (cp + 1) * 16, vv[0], vv[1]);
+    float v[64];
+    tc::tmem_ld64(tmem + T_CH + lane_off + half * 64, v);
+    const float4* b4 = reinterpret_cast<const float4*>(bias + half * 64);
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const int ch = cp + u;
-        float* v = vv[u];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = fmaxf(v[j] + __ldg(bias + ch * 16 + j), 0.f);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          *reinterpret_cast<uint4*>(smem + dst + coff(r, ch * 2 + q, sbo)) =
-              make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
-                         pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
-        }
-      }
+    for (int j = 0; j < 16; ++j) {
+      const float4 b = __ldg(b4 + j);
+      v[4 * j] = fmaxf(v[4 * j] + b.x, 0.f);
+      v[4 * j + 1] = fmaxf(v[4 * j + 1] + b.y, 0.f);
+      v[4 * j + 2] = fmaxf(v[4 * j + 2] + b.z, 0.f);
+      v[4 * j + 3] = fmaxf(v[4 * j + 3] + b.w, 0.f);
     }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      *reinterpret_cast<uint4*>(smem + dst + coff(r, half * 8 + q, sbo)) =
+          make_uint4(pack2(v[8 * q], v[8 * q + 1]), pack2(v[8 * q + 2], v[8 * q + 3]),
+                     pack2(v[8 * q + 4], v[8 * q + 5]), pack2(v[8 * q + 6], v[8 * q + 7]));
   };
   // dH = D * [H > 0], written over H in place (H's tile is no longer read by any MMA).
   auto relu_bwd = [&](int reg, int sbo) {
-    for (int cp = half * 4; cp < half * 4 + 4; cp += 2) {
-      float vv[2][16];
-      tc::tmem_ld16x2(tmem + T_CH + lane_off + cp * 16, tmem + T_CH + lane_off + (cp + 1) * 16, vv[0], vv[1]);
+    float v[64];
+    tc::tmem_ld64(tmem + T_CH + lane_off + half * 64, v);
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-      const int ch = cp + u;
-      float* v = vv[u];
+    for (int q = 0; q < 8; ++q) {
+      uint4* p = reinterpret_cast<uint4*>(smem + reg + coff(r, half * 8 + q, sbo));
+      uint4 hv = *p;
+      const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&hv);
+      uint32_t o[4];
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        uint4* p = reinterpret_cast<uint4*>(smem + reg + coff(r, ch * 2 + q, sbo));
-        uint4 hv = *p;
-        const __nv_bfloat162* hb = reinterpret_cast<const __nv_bfloat162*>(&hv);
-        uint32_t o[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float2 f = __bfloat1622float2(hb[e]);
-          o[e] = pack2(f.x > 0.f ? v[8 * q + 2 * e] : 0.f, f.y > 0.f ? v[8 * q + 2 * e + 1] : 0.f);
-        }
-        *p = make_uint4(o[0], o[1], o[2], o[3]);
+      for (int e = 0; e < 4; ++e) {
+        const float2 f = __bfloat1622float2(hb[e]);
+        o[e] = pack2(f.x > 0.f ? v[8 * q + 2 * e] : 0.f, f.y > 0.f ? v[8 * q + 2 * e + 1] : 0.f);
       }
-      }
+      *p = make_uint4(o[0], o[1], o[2], o[3]);
     }
   };
 
-  const int64_t ntiles = (a.M + BM - 1) / BM;
   for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const int64_t m0 = tile * BM;
-    load_x0(m0);
+    if (TILES) {
+      if (!wait_x0()) { ok = 0; break; }
+    } else {
+      load_x0(m0);
+    }
     if (tid < BM) {  // dZ tile: columns 0..2, zero to 16
       const int64_t row = m0 + tid;
       float z0 = 0.f, z1 = 0.f, z2 = 0.f;
@@ -570,8 +637,10 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
       const int64_t nm0 = (tile + gridDim.x) * BM;
       if (nm0 < a.M) {
         const int64_t nrows = a.M - nm0 < BM ? a.M - nm0 : BM;
-        for (int64_t off = (int64_t)tid * 128; off < nrows * F * 4; off += THREADS * 128)
-          tc::prefetch_l2(reinterpret_cast<const char*>(a.X0 + nm0 * F) + off);
+        const char* src = TILES ? reinterpret_cast<const char*>(a.X0t + (tile + gridDim.x) * X0T_TILE_BYTES)
+                                : reinterpret_cast<const char*>(a.X0 + nm0 * F);
+        const int64_t nbytes = TILES ? X0T_TILE_BYTES : nrows * F * 4;
+        for (int64_t off = (int64_t)tid * 128; off < nbytes; off += THREADS * 128) tc::prefetch_l2(src + off);
         if (tid * 128 < nrows * 12) tc::prefetch_l2(reinterpret_cast<const char*>(a.dZ3 + nm0 * 3) + tid * 128);
       }
     }
@@ -582,57 +651,29 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
     // also deliver db1), and h kept in fp32 for the encoding backward.
     {
       const int64_t row = m0 + r;
+      float v[SQ + 3], v16[16];
+      tc::tmem_ld16(tmem + T_CH + lane_off, v16);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[j] = v16[j];
+      tc::tmem_ld16(tmem + T_CH + lane_off + 16, v16);
+#pragma unroll
+      for (int j = 16; j < SQ; ++j) v[j] = v16[j - 16];
+      v[SQ] = v[SQ + 1] = v[SQ + 2] = 0.f;
+      if (row < a.M) {
+        const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
+        v[SQ] = __ldg(dp);
+        v[SQ + 1] = __ldg(dp + 1);
+        v[SQ + 2] = __ldg(dp + 2);
+      }
       uint8_t* xrow = smem + RB + (r >> 3) * SBO_B + (r & 7) * 16;
-      auto put = [&](int col, float v) {
-        *reinterpret_cast<__nv_bfloat16*>(xrow + (col >> 3) * 128 + (col & 7) * 2) = __float2bfloat16_rn(v);
-      };
-      auto pe4 = [&](int col, float v) {
-        float sn, cs;
-        __sincosf(v, &sn, &cs);
-        put(col, sn);
-        put(col + 1, 2.0f * sn * cs);
-        put(col + 2, cs);
-        put(col + 3, cs * cs - sn * sn);
-      };
-      float v16[16];
       if (half == 0) {
-        tc::tmem_ld16(tmem + T_CH + lane_off, v16);
+        encode_row<0>(xrow, v, 1.f);
 #pragma unroll
-        for (int j = 0; j < 14; ++j) {
-          put(j, v16[j]);
-          pe4(SQ + 3 + 4 * j, v16[j]);
-          hstash[r * SQ + j] = v16[j];
-        }
+        for (int j = 0; j < 14; ++j) hstash[r * SQ + j] = v[j];
       } else {
-        tc::tmem_ld16(tmem + T_CH + lane_off, v16);
-        const float h14 = v16[14], h15 = v16[15];
-        tc::tmem_ld16(tmem + T_CH + lane_off + 16, v16);
-        put(14, h14);
-        pe4(SQ + 3 + 4 * 14, h14);
-        hstash[r * SQ + 14] = h14;
-        put(15, h15);
-        pe4(SQ + 3 + 4 * 15, h15);
-        hstash[r * SQ + 15] = h15;
+        encode_row<1>(xrow, v, 1.f);
 #pragma unroll
-        for (int j = 16; j < SQ; ++j) {
-          put(j, v16[j - 16]);
-          pe4(SQ + 3 + 4 * j, v16[j - 16]);
-          hstash[r * SQ + j] = v16[j - 16];
-        }
-        float d[3] = {0.f, 0.f, 0.f};
-        if (row < a.M) {
-          const float* dp = a.dirs + (row / a.rows_per_dir) * 3;
-          d[0] = __ldg(dp);
-          d[1] = __ldg(dp + 1);
-          d[2] = __ldg(dp + 2);
-        }
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          put(SQ + q, d[q]);
-          pe4(SQ + 3 + 4 * SQ + 4 * q, d[q]);
-        }
-#pragma unroll
-        for (int c = ENC; c < ENCP; ++c) put(c, c == ENC ? 1.0f : 0.0f);
+        for (int j = 14; j < SQ; ++j) hstash[r * SQ + j] = v[j];
       }
     }
     // L1, L2 (the L1 product ignores column 150: W1's image is zero there).
@@ -667,6 +708,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
           mma_run(tmem + T_W1, mnmaj(sb + RA, SBO_A), mnmaj(sb + RB, SBO_B), BM / 16, idesc_t(BM, ENCP, true, true),
                   !first);
         })) { ok = 0; break; }
+    if (TILES) issue_x0(tile);  // RA is free: dW0 contracts X0 again
     {
       float dh[14];
       const float* hrow = hstash + r * SQ;
@@ -686,7 +728,11 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
         for (int c = SQ; c < SQP; ++c) put(c, 0.0f);
       }
     }
-    load_x0(m0);  // dW0 contracts X0 again; RA is free now
+    if (TILES) {
+      if (!wait_x0()) { ok = 0; break; }
+    } else {
+      load_x0(m0);  // dW0 contracts X0 again; RA is free now
+    }
     // (h) dX0 = dH0 W0^T; (i) dW0 += X0^T dH0 as two M = 128 products (features 0..127
     // and 16..143).
     if (!run([&] {
@@ -698,6 +744,8 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
           mma_run(tmem + T_W0B, mnmaj(sb + RA + 256, SBO_A), mnmaj(sb + RE, SBO_H0), BM / 16,
                   idesc_t(BM, SQP, true, true), !first);
         })) { ok = 0; break; }
+    // RA is free: the next tile's input travels while dX0 is stored.
+    if (TILES && tile + gridDim.x < ntiles) issue_x0(tile + gridDim.x);
     if (a.dX0) {
       // TMEM -> per-warp 32 x 17 staging (in RB) -> 16-byte row stores.
       float* buf = reinterpret_cast<float*>(smem + RB) + warp * (32 * 17);
@@ -779,6 +827,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_bwd_fused_kernel(Args a) {
   if (!ok) {
     if (tid == 0) atomicOr(&g_fused_status, 1);
     tc::mbar_wait(wbar, 0, WAIT_LIMIT);
+    if (x_pending) tc::mbar_wait(xbar, xphase, WAIT_LIMIT);  // an input tile copy in flight
     tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);
   }
   tc::fence_before_sync();
@@ -816,38 +865,52 @@ bool mlp_fused_supported(const MlpDims& d) {
 size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }
 
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas) {
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas, const uint8_t* X0t) {
   if (M == 0) return TVM_OK;
-  TVM_TRY(ensure_smem_limit((const void*)fmlp::mlp_fwd_fused_kernel, fmlp::SMEM, "fused mlp"));
+  const bool tiles = X0t != nullptr;
+  const void* kern = tiles ? (const void*)fmlp::mlp_fwd_fused_kernel<true> : (const void*)fmlp::mlp_fwd_fused_kernel<false>;
+  TVM_TRY(ensure_smem_limit(kern, fmlp::SMEM, "fused mlp"));
   const int sms = device_sms();
-  if (!aligned(wpack, 16) || !aligned(X0, 16)) {  // both are read with 16-byte loads
-    set_error("fused mlp: packed weights and features must be 16-byte aligned");
+  // Weights, features and biases are read with 16-byte loads or bulk copies.
+  if (!aligned(wpack, 16) || !aligned(tiles ? (const void*)X0t : (const void*)X0, 16) || !aligned(w.b1, 16) ||
+      !aligned(w.b2, 16)) {
+    set_error("fused mlp: packed weights, features and biases must be 16-byte aligned");
     return TVM_ERR_ALIGN;
   }
   fmlp::pack_weights_kernel<<<64, 256, 0, st>>>(wpack, w.w0, w.w1, w.w2, w.w3);
   TVM_TRY(check_launch("pack_weights"));
-  fmlp::Args a{M, wpack, X0, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb};
+  fmlp::Args a{M, wpack, X0, X0t, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(max_ctas > 0 ? max_ctas : sms, 1));
-  fmlp::mlp_fwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::SMEM, st>>>(a);
+  if (tiles)
+    fmlp::mlp_fwd_fused_kernel<true><<<grid, fmlp::THREADS, fmlp::SMEM, st>>>(a);
+  else
+    fmlp::mlp_fwd_fused_kernel<false><<<grid, fmlp::THREADS, fmlp::SMEM, st>>>(a);
   return check_launch("mlp_fwd_fused");
 }
 
 int launch_mlp_bwd_fused(const MlpWeights& w, const MlpGrads& g, const float* X0, const float* dirs,
                          int rows_per_dir, int64_t M, const float* dZ3, float* dX0, const uint8_t* wpack,
-                         cudaStream_t st, int max_ctas) {
+                         cudaStream_t st, int max_ctas, const uint8_t* X0t) {
   if (M == 0) return TVM_OK;
-  TVM_TRY(ensure_smem_limit((const void*)fmlp::bwd::mlp_bwd_fused_kernel, fmlp::bwd::SMEM, "fused mlp backward"));
+  const bool tiles = X0t != nullptr;
+  const void* kern =
+      tiles ? (const void*)fmlp::bwd::mlp_bwd_fused_kernel<true> : (const void*)fmlp::bwd::mlp_bwd_fused_kernel<false>;
+  TVM_TRY(ensure_smem_limit(kern, fmlp::bwd::SMEM, "fused mlp backward"));
   const int sms = device_sms();
-  if (!aligned(wpack, 16) || !aligned(X0, 16) || (dX0 && !aligned(dX0, 16))) {
-    set_error("fused mlp backward: packed weights, features and dX0 must be 16-byte aligned");
+  if (!aligned(wpack, 16) || !aligned(tiles ? (const void*)X0t : (const void*)X0, 16) || (dX0 && !aligned(dX0, 16)) ||
+      !aligned(w.b1, 16) || !aligned(w.b2, 16)) {
+    set_error("fused mlp backward: packed weights, features, biases and dX0 must be 16-byte aligned");
     return TVM_ERR_ALIGN;
   }
-  fmlp::bwd::Args a{M, wpack, X0, dirs, rows_per_dir, w.b1, w.b2, dZ3, dX0,
+  fmlp::bwd::Args a{M, wpack, X0, X0t, dirs, rows_per_dir, w.b1, w.b2, dZ3, dX0,
                     g.w0, g.w1, g.b1, g.w2, g.b2, g.w3, g.b3};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(max_ctas > 0 ? max_ctas : sms, 1));
-  fmlp::bwd::mlp_bwd_fused_kernel<<<grid, fmlp::THREADS, fmlp::bwd::SMEM, st>>>(a);
+  if (tiles)
+    fmlp::bwd::mlp_bwd_fused_kernel<true><<<grid, fmlp::THREADS, fmlp::bwd::SMEM, st>>>(a);
+  else
+    fmlp::bwd::mlp_bwd_fused_kernel<false><<<grid, fmlp::THREADS, fmlp::bwd::SMEM, st>>>(a);
   return check_launch("mlp_bwd_fused");
 }
 

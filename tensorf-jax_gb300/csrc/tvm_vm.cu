@@ -449,6 +449,64 @@ __global__ void __launch_bounds__(256) appearance_fwd_kernel(const T* __restrict
   }
 }
 
+// The same features written as FeatureMlp input tiles (bf16, 48 channels per pair): lane
+// sub of a row's quad holds channels [12 sub, 12 sub + 12) of every pair, stored as three
+// 8-byte pieces at their canonical positions. The quads of the padded rows past the last
+// selected sample write zeros, so a tile is whole.
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&h);
+}
+
+__global__ void __launch_bounds__(256) appearance_fwd_tiles_kernel(const __nv_bfloat16* __restrict__ lines,
+                                                                  const __nv_bfloat16* __restrict__ planes, int G,
+                                                                  const float* __restrict__ origins,
+                                                                  const float* __restrict__ dirs, int64_t rows,
+                                                                  int64_t rows_padded, int k, SamplerArgs s,
+                                                                  const int32_t* __restrict__ sel_idx,
+                                                                  uint8_t* __restrict__ X0t) {
+  constexpr int C = 48, CPL = C / 4;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  if (row >= rows_padded) return;
+  float v[3][CPL];
+  if (row < rows) {
+    const int64_t r = row / k;
+    const int i = __ldg(sel_idx + row);
+    RayGeom g = load_ray(origins, dirs, r, s);
+    float t, delta, x[3], u[3];
+    sample_t(g, s, r, i, t, delta);
+    sample_point(g, s, t, x);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u[a] = grid_coord(x[a], G);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      int a, b, c;
+      mode_perm(m, a, b, c);
+      PairEval<__nv_bfloat16, CPL> e;
+      vm_pair_eval<__nv_bfloat16, CPL>(lines, planes, G, C, m, u[a], u[b], u[c], sub * CPL, e);
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) v[m][j] = e.L[j] * e.P[j];
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int j = 0; j < CPL; ++j) v[m][j] = 0.f;
+  }
+  const int rr = (int)(row & (X0T_ROWS - 1));
+  uint8_t* base = X0t + (row / X0T_ROWS) * X0T_TILE_BYTES + (rr >> 3) * X0T_SBO + (rr & 7) * 16;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+#pragma unroll
+    for (int p = 0; p < CPL / 4; ++p) {
+      const int kk = m * C + sub * CPL + 4 * p;  // a multiple of 4: half a K-chunk
+      __stcs(reinterpret_cast<uint2*>(base + (kk >> 3) * 128 + (kk & 7) * 2),
+             make_uint2(pack_bf16x2(v[m][4 * p], v[m][4 * p + 1]), pack_bf16x2(v[m][4 * p + 2], v[m][4 * p + 3])));
+    }
+  }
+}
+
 template <typename T, int C>
 __global__ void __launch_bounds__(256) appearance_bwd_kernel(const T* __restrict__ lines,
                                                             const T* __restrict__ planes, int G,
@@ -712,6 +770,26 @@ int launch_appearance_fwd(const FieldView& f, const float* origins, const float*
   TVM_DISPATCH_FIELD(f, (appearance_fwd_kernel<TT, CC><<<quad_blocks(rows), 256, 0, st>>>(
                              L_, P_, f.G, origins, dirs, rows, k, s, sel_idx, X0)));
   return check_launch("appearance_fwd");
+}
+
+int launch_appearance_fwd_tiles(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                                const SamplerArgs& s, const int32_t* sel_idx, int k, uint8_t* X0t,
+                                cudaStream_t st) {
+  if (f.dtype != TVM_BF16 || f.C * 3 != X0T_FEAT) {
+    set_error("appearance input tiles need a bf16 field of 48 channels per pair");
+    return TVM_ERR_UNSUPPORTED;
+  }
+  if (!aligned(X0t, 16)) {
+    set_error("appearance input tiles must be 16-byte aligned");
+    return TVM_ERR_ALIGN;
+  }
+  const int64_t rows = R * k;
+  if (rows == 0) return TVM_OK;
+  const int64_t rows_padded = ceil_div(rows, (int64_t)X0T_ROWS) * X0T_ROWS;
+  appearance_fwd_tiles_kernel<<<quad_blocks(rows_padded), 256, 0, st>>>(
+      static_cast<const __nv_bfloat16*>(f.lines), static_cast<const __nv_bfloat16*>(f.planes), f.G, origins, dirs,
+      rows, rows_padded, k, s, sel_idx, X0t);
+  return check_launch("appearance_fwd_tiles");
 }
 
 int launch_appearance_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins,
