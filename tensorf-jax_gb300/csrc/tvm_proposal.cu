@@ -511,11 +511,17 @@ __global__ void prop_loss_kernel(const float* __restrict__ wmain, const float* _
 }
 
 // ---------------------------------------------------------------------------------
+static int launch_prop_fwd_tc(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                              const SamplerArgs& s, const float* edges, const float* jitter, float* delta,
+                              const PropMlp& mlp, cudaStream_t st);
+
 int launch_prop_features(const FieldView& f, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                          const float* edges, const float* jitter, float* X, float* delta, const PropMlp* mlp,
                          cudaStream_t st) {
   const int64_t n = R * s.N;
   if (n == 0) return TVM_OK;
+  if (f.dtype == TVM_BF16 && mlp && mlp->units == 64 && !X && !mlp->H && mlp->sigma)
+    return launch_prop_fwd_tc(f, origins, dirs, R, s, edges, jitter, delta, *mlp, st);  // BF16: tensor cores
   const unsigned blocks = (unsigned)ceil_div(n, 128 * PROP_SPT);  // 128 threads, PROP_SPT samples each
   const int units = mlp ? mlp->units : 0;
   const size_t smem = mlp ? (size_t)18 * units * sizeof(float) : 0;
@@ -793,7 +799,126 @@ __global__ void __launch_bounds__(THREADS) prop_bwd_tc_kernel(
   }
 }
 
+// Tensor-core proposal forward for BF16 models with 64 hidden units. Persistent CTAs of
+// 128 threads, one 128-sample tile at a time (thread = sample = TMEM lane): the 16
+// features go to a bf16 A tile, one MMA gives H = X W1 (TMEM, 64 fp32 columns), and the
+// epilogue forms z = b2 + sum_u relu(H_u + b1_u) w2_u and sigma = softplus(z + shift).
+// X and W1 are the bf16 operands of the tensor-core backward, so the forward's hidden
+// units are the ones the backward recomputes. A few KB of shared memory and 64 TMEM
+// columns per CTA let four CTAs share an SM: some gather while others wait for their
+// product.
+constexpr int FWD_BAR = OFF_X + 128 * 16 * 2;  // W1 image and X tile, then the barrier
+constexpr int FWD_SMEM = FWD_BAR + 64;
+constexpr uint32_t FWD_NCOLS = 64;
+constexpr int FWD_CTAS_PER_SM = 4;
+
+__global__ void __launch_bounds__(THREADS) prop_fwd_tc_kernel(
+    const __nv_bfloat16* __restrict__ lines, const __nv_bfloat16* __restrict__ planes, int G,
+    const float* __restrict__ origins, const float* __restrict__ dirs, int64_t R, SamplerArgs s,
+    const float* __restrict__ edges, const float* __restrict__ jitter, float* __restrict__ delta,
+    const float* __restrict__ w1, const float* __restrict__ b1, const float* __restrict__ w2,
+    const float* __restrict__ b2, float shift, float* __restrict__ sigma) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + FWD_BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + FWD_BAR + 8);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  if (warp == 0) tc::tmem_alloc(tslot, FWD_NCOLS);
+  if (tid == 0) tc::mbar_init(mbar, 1);
+  for (int c = tid; c < U * 2; c += THREADS) {  // W1 image (B operand [unit][input])
+    const int u = c >> 1, kc = c & 1;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = __ldg(w1 + (kc * 8 + e) * U + u);
+    *reinterpret_cast<uint4*>(smem + OFF_W1 + coff(u, kc, SBO_16)) =
+        make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t sb = tc::smem_u32(smem);
+  const float4* b14 = reinterpret_cast<const float4*>(b1);
+  const float4* w24 = reinterpret_cast<const float4*>(w2);
+  const float bias2 = __ldg(b2);
+  uint32_t phase = 0;
+  int ok = 1;
+  const int64_t nsmp = R * s.N;
+  const int64_t ntiles = (nsmp + THREADS - 1) / THREADS;
+  for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int64_t smp = tile * THREADS + tid;
+    const bool valid = smp < nsmp;
+    float X[PROP_IN];
+#pragma unroll
+    for (int i = 0; i < PROP_IN; ++i) X[i] = 0.f;
+    if (valid) {
+      float len;
+      prop_sample_features<__nv_bfloat16>(lines, planes, G, origins, dirs, s, edges, jitter, smp, X, len);
+      delta[smp] = len;
+    }
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc) {
+      *reinterpret_cast<uint4*>(smem + OFF_X + coff(tid, kc, SBO_16)) =
+          make_uint4(pack2(X[8 * kc], X[8 * kc + 1]), pack2(X[8 * kc + 2], X[8 * kc + 3]),
+                     pack2(X[8 * kc + 4], X[8 * kc + 5]), pack2(X[8 * kc + 6], X[8 * kc + 7]));
+    }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_run(tmem, kmaj(sb + OFF_X, SBO_16), kmaj(sb + OFF_W1, SBO_16), 1, idesc_t(128, U, false, false), false);
+      tc::mma_commit(mbar);
+    }
+    const int done = tc::mbar_wait(mbar, phase, WAIT_LIMIT) ? 1 : 0;
+    phase ^= 1u;
+    if (!__syncthreads_and(done)) {
+      ok = 0;
+      break;
+    }
+    tc::fence_after_sync();
+    float h[U];
+    tc::tmem_ld64(tmem + lane_off, h);
+    float z = bias2;
+#pragma unroll
+    for (int q = 0; q < U / 4; ++q) {
+      const float4 b = __ldg(b14 + q), w = __ldg(w24 + q);
+      z = fmaf(fmaxf(h[4 * q] + b.x, 0.f), w.x, z);
+      z = fmaf(fmaxf(h[4 * q + 1] + b.y, 0.f), w.y, z);
+      z = fmaf(fmaxf(h[4 * q + 2] + b.z, 0.f), w.z, z);
+      z = fmaf(fmaxf(h[4 * q + 3] + b.w, 0.f), w.w, z);
+    }
+    if (valid) sigma[smp] = softplus_f(z + shift);
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(&g_prop_status, 1);
+    tc::mbar_wait(mbar, phase ^ 1u, WAIT_LIMIT);  // the product in flight, before TMEM is freed
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, FWD_NCOLS);
+  }
+}
+
 }  // namespace ptc
+
+static int launch_prop_fwd_tc(const FieldView& f, const float* origins, const float* dirs, int64_t R,
+                              const SamplerArgs& s, const float* edges, const float* jitter, float* delta,
+                              const PropMlp& mlp, cudaStream_t st) {
+  if (!aligned(mlp.b1, 16) || !aligned(mlp.w2, 16)) {
+    set_error("proposal forward: b1 and w2 must be 16-byte aligned");
+    return TVM_ERR_ALIGN;
+  }
+  const int64_t tiles = ceil_div(R * s.N, (int64_t)ptc::THREADS);
+  const unsigned grid =
+      (unsigned)std::min<int64_t>(tiles, (int64_t)ptc::FWD_CTAS_PER_SM * std::max(device_sms(), 1));
+  ptc::prop_fwd_tc_kernel<<<grid, ptc::THREADS, ptc::FWD_SMEM, st>>>(
+      (const __nv_bfloat16*)f.lines, (const __nv_bfloat16*)f.planes, f.G, origins, dirs, R, s, edges, jitter, delta,
+      mlp.w1, mlp.b1, mlp.w2, mlp.b2, mlp.shift, mlp.sigma);
+  return check_launch("prop_fwd_tc");
+}
 
 int prop_status(int32_t* out, cudaStream_t st) {
   int32_t v = 0;

@@ -9,6 +9,8 @@ kernels actually use, rounded to bf16 at the points where those kernels round.
 * FeatureMlp: the fused tcgen05 kernels round the layer inputs and weights, dZ3 and the
   back-propagated dH2 / dH1 / dH0 to bf16, and accumulate in FP32
   (test_gpu_bf16._mirror_mlp / _mirror_mlp_backward).
+* Proposal forward (prop_fwd_tc_kernel): bf16 features X and weights W1 feed the
+  product; b1, the ReLU, w2, b2 and the softplus stay FP32.
 * Proposal backward (prop_bwd_tc_kernel): bf16 features X, weights W1, hidden units h,
   their gradient dh and the loss gradient dz feed the products; b1, w2 and the scatter
   stay FP32.
@@ -194,10 +196,32 @@ def test_bf16_render_and_gradients_match_rounding_mirror(monkeypatch):
     assert all(errs[n] < plain[n] for n in mlp_side), (errs, plain)
 
 
+def _proposal_features(prop, o, d, aabb, Np, pj):
+    """Bin edges, lengths, and the 16 proposal MLP inputs (FP64) of every bin."""
+    e = O.proposal_edges(o, d, aabb, Np)
+    length = e[:, 1:] - e[:, :-1]
+    t = e[:, :-1] + pj * length
+    x = O.normalize_points((o[:, None, :] + d[:, None, :] * t[:, :, None]).permute(2, 0, 1), aabb)
+    feats = O.vm_interpolate(prop["vector"].detach(), prop["matrix"].detach(), x).permute(1, 2, 0)
+    xp = x.permute(1, 2, 0)
+    return e, length, torch.cat([feats, xp, xp.abs().amax(-1, keepdim=True)], -1)
+
+
+def _proposal_forward_bf16(prop, o, d, aabb, Np, pj, shift_p):
+    """prop_fwd_tc_kernel's forward: bin edges and proposal weights from the bf16
+    product of X and W1, the rest in FP64."""
+    with torch.no_grad():
+        e, length, X = _proposal_features(prop, o, d, aabb, Np, pj)
+        w1, b1, w2, b2 = (prop[n].detach() for n in ("w1", "b1", "w2", "b2"))
+        z = (torch.relu(_bf(X) @ _bf(w1) + b1) @ w2)[..., 0] + b2[0]
+        _, wp = O.compute_segment_probabilities(O.softplus(z + shift_p), length)
+    return e, wp
+
+
 def _proposal_mirror_grads(prop, o, d, aabb, Np, pj, shift_p, w_main, bins, loss_w):
-    """Gradients of the proposal bound loss with prop_bwd_tc_kernel's rounding. prop:
+    """Gradients of the proposal bound loss with the tensor-core kernels' rounding. prop:
     FP64 proposal parameters with bf16-rounded fields. The forward (and so dz) uses the
-    unrounded MLP weights, as prop_features_kernel does in FP32."""
+    bf16 product of X and W1, as prop_fwd_tc_kernel does."""
     e = O.proposal_edges(o, d, aabb, Np)
     length = e[:, 1:] - e[:, :-1]
     t = e[:, :-1] + pj * length
@@ -209,14 +233,13 @@ def _proposal_mirror_grads(prop, o, d, aabb, Np, pj, shift_p, w_main, bins, loss
     xp = x.permute(1, 2, 0)
     X = torch.cat([feats.detach(), xp, xp.abs().amax(-1, keepdim=True)], -1)
     w1, b1, w2, b2 = (prop[n].detach() for n in ("w1", "b1", "w2", "b2"))
-    zf = torch.relu(X @ w1 + b1) @ w2
-    z = (zf[..., 0] + b2[0]).requires_grad_(True)
-    _, wp = O.compute_segment_probabilities(O.softplus(z + shift_p), length)
-    lprop = O.proposal_loss(w_main, wp, bins, loss_w)
-    (dz,) = torch.autograd.grad(lprop, z)
     Xb, W1b = _bf(X), _bf(w1)
     pre = Xb @ W1b + b1
     h = torch.relu(pre)
+    z = ((h @ w2)[..., 0] + b2[0]).requires_grad_(True)
+    _, wp = O.compute_segment_probabilities(O.softplus(z + shift_p), length)
+    lprop = O.proposal_loss(w_main, wp, bins, loss_w)
+    (dz,) = torch.autograd.grad(lprop, z)
     dh = dz[..., None] * w2[:, 0] * (h > 0)
     Hb, dHb, dzb = _bf(h), _bf(dh), _bf(dz)
     dX = dHb @ W1b.T
@@ -226,11 +249,7 @@ def _proposal_mirror_grads(prop, o, d, aabb, Np, pj, shift_p, w_main, bins, loss
              "b1": dHb.reshape(-1, 64).sum(0),
              "w2": (Hb * dzb[..., None]).reshape(-1, 64).sum(0)[:, None],
              "b2": dz.sum().reshape(1)}
-    with torch.no_grad():
-        zpre = X @ w1 + b1
-    kink = torch.zeros(o.shape[0], dtype=torch.bool)
-    for zz in (pre, zpre):
-        kink |= (zz.abs() < KINK_REL * float(zz.pow(2).mean().sqrt())).any(-1).any(-1)
+    kink = (pre.abs() < KINK_REL * float(pre.pow(2).mean().sqrt())).any(-1).any(-1)
     return grads, ~kink
 
 
@@ -252,8 +271,8 @@ def test_bf16_proposal_backward_matches_rounding_mirror(monkeypatch):
     def mirror(o_, d_, jit_, pj_):
         r64 = _oracle_bf16(ref)
         with torch.no_grad():
-            e, wp, _, _ = O.proposal_forward(r64["proposal"], o_.double(), d_.double(), aabb.double(), Np,
-                                             pj_.double(), shift_p)
+            e, wp = _proposal_forward_bf16(r64["proposal"], o_.double(), d_.double(), aabb.double(), Np,
+                                           pj_.double(), shift_p)
             t, delta, bins = O.resample(e, wp, N, jit_.double())
             _, aux = O.render_explicit(r64, aabb.double(), o_.double(), d_.double(), t, delta, k, gum.double(),
                                        density_shift=shift, return_aux=True)
