@@ -89,6 +89,7 @@ struct SideStream {
   cudaStream_t stream = nullptr, branch = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
   cudaEvent_t fork3 = nullptr, density_ready = nullptr, appearance_ready = nullptr;
+  cudaEvent_t fork4 = nullptr, packed = nullptr;
 };
 
 static int side_stream(SideStream*& out) {
@@ -101,7 +102,8 @@ static int side_stream(SideStream*& out) {
     cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, least);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.branch, cudaStreamNonBlocking, greatest);
-    for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2, &s.fork3, &s.density_ready, &s.appearance_ready})
+    for (cudaEvent_t* ev : {&s.fork, &s.join, &s.fork2, &s.join2, &s.fork3, &s.density_ready, &s.appearance_ready,
+                            &s.fork4, &s.packed})
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "side stream: %s", cudaGetErrorString(e));
   }
@@ -459,6 +461,21 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
                                 adam->shadow_n, st, 8, true));
     }
   }
+  // The fused BF16 MLP's weight images depend only on the MLP weights, final since the
+  // last update: off the pass's critical path, they are packed on the side stream beside
+  // its start, where mlp_forward would otherwise pack them just before the forward.
+  const MlpWeights w = mlp_weights(L, params);
+  SideStream* pack_side = nullptr;
+  if (g_n_events == 0 && b.X0t) {
+    TVM_TRY(side_stream(pack_side));
+    cudaError_t e = cudaEventRecord(pack_side->fork4, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(pack_side->stream, pack_side->fork4, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "weight packing fork: %s", cudaGetErrorString(e));
+    TVM_TRY(launch_mlp_pack_fused(w, mlp_fused_wpack(Workspace{static_cast<char*>(workspace), ws_bytes, ws.used, false}),
+                                  pack_side->stream));
+    e = cudaEventRecord(pack_side->packed, pack_side->stream);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "weight packing: %s", cudaGetErrorString(e));
+  }
   phase_mark(0, st);
   if (proposal) {
     // Proposal network forward, then resampling into explicit main samples.
@@ -567,8 +584,11 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   else
     TVM_TRY(launch_appearance_fwd(fa, rays.origins, rays.directions, R, s, b.sel, k, b.X0, st));
   phase_mark(4, st);
-  const MlpWeights w = mlp_weights(L, params);
   const size_t mlp_off = ws.used;
+  if (pack_side) {
+    cudaError_t e = cudaStreamWaitEvent(st, pack_side->packed, 0);
+    TVM_REQUIRE(e == cudaSuccess, TVM_ERR_LAUNCH, "weight packing join: %s", cudaGetErrorString(e));
+  }
   // The fused BF16 MLP kernels fill every SM's shared memory and TMEM, so nothing runs
   // beside them on an SM they hold. Where other streams have work at the same time (the
   // proposal backward beside the forward; the density branch beside the backward) they
@@ -577,7 +597,7 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   // so a pass on one stream keeps the whole GPU for them.
   const int shared_ctas = device_sms() / 2;
   TVM_TRY(mlp_forward(d, w, b.X0, rays.directions, rays.camera_indices, k, R * k, b.rgb, ws, st,
-                      overlap && prop_forked ? shared_ctas : 0, b.X0t));
+                      overlap && prop_forked ? shared_ctas : 0, b.X0t, pack_side != nullptr));
   phase_mark(5, st);
   if (!backward) {
     TVM_TRY(launch_color_loss(b.rgb, b.w_sel, b.p_last, b.q_last, b.wsum, R, k, nullptr, out, nullptr, nullptr,

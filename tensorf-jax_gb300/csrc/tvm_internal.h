@@ -108,9 +108,13 @@ size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M);  // forward only (a
 // its camera cams[m / rows_per_dir] (cams is read only when d.cams > 0).
 // max_ctas: the fused BF16 kernels' grid cap (launch_mlp_fwd_fused), 0 for one CTA per SM.
 // X0t: the input as tiles (launch_appearance_fwd_tiles) instead of X0; fused path only.
+// prepacked: the fused kernels' weight images are already at mlp_fused_wpack(ws)
+// (launch_mlp_pack_fused), packed since the weights last changed.
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas = 0,
-                const uint8_t* X0t = nullptr);
+                const uint8_t* X0t = nullptr, bool prepacked = false);
+// Where mlp_forward on this workspace state keeps the fused kernels' weight images.
+uint8_t* mlp_fused_wpack(Workspace ws);
 // Needs the preceding mlp_forward on the same workspace: its kept row-major activations
 // (layered path), or its packed bf16 weights (fused path, which recomputes the forward
 // from X0 and the view directions).
@@ -131,7 +135,10 @@ size_t mlp_fused_pack_bytes();
 // X0t: input tiles instead of the row-major X0 (which is then not read).
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
                          int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas = 0,
-                         const uint8_t* X0t = nullptr);
+                         const uint8_t* X0t = nullptr, bool prepacked = false);
+// The fused kernels' bf16 weight images into wpack (what launch_mlp_fwd_fused does first
+// unless prepacked).
+int launch_mlp_pack_fused(const MlpWeights& w, uint8_t* wpack, cudaStream_t st);
 // Fused BF16 backward: recomputes the forward per tile, accumulates all weight and
 // bias gradients into g, writes dX0 (M, 144) when non-null. wpack: the images packed by
 // launch_mlp_fwd_fused.

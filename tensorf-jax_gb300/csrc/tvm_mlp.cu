@@ -647,9 +647,11 @@ size_t mlp_fwd_workspace_bytes(const MlpDims& d, int64_t M) {
   return ws.used + 256;
 }
 
+uint8_t* mlp_fused_wpack(Workspace ws) { return ws.take<uint8_t>((int64_t)mlp_fused_pack_bytes()); }
+
 int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, const int32_t* cams,
                 int rows_per_dir, int64_t M, float* rgb, Workspace& ws, cudaStream_t st, int max_ctas,
-                const uint8_t* X0t) {
+                const uint8_t* X0t, bool prepacked) {
   MlpBufs b = carve(d, M, ws, true);
   if (!ws.ok()) {
     set_error("mlp workspace too small");
@@ -659,7 +661,7 @@ int mlp_forward(const MlpDims& d, const MlpWeights& w, const float* X0, const fl
   if (mlp_fused_supported(d)) {
     // BF16: all four layers in one tcgen05 kernel. Nothing is kept for the backward,
     // which recomputes the activations from X0 (only the packed weights are reused).
-    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st, max_ctas, X0t);
+    return launch_mlp_fwd_fused(d, w, X0, dirs, rows_per_dir, M, rgb, b.wpack, st, max_ctas, X0t, prepacked);
   }
   if (X0t) {
     set_error("mlp: input tiles need the fused BF16 kernels");

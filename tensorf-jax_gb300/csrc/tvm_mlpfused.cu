@@ -864,8 +864,18 @@ bool mlp_fused_supported(const MlpDims& d) {
 
 size_t mlp_fused_pack_bytes() { return fmlp::WPACK_BYTES; }
 
+int launch_mlp_pack_fused(const MlpWeights& w, uint8_t* wpack, cudaStream_t st) {
+  if (!aligned(wpack, 16)) {
+    set_error("fused mlp: packed weights must be 16-byte aligned");
+    return TVM_ERR_ALIGN;
+  }
+  fmlp::pack_weights_kernel<<<64, 256, 0, st>>>(wpack, w.w0, w.w1, w.w2, w.w3);
+  return check_launch("pack_weights");
+}
+
 int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0, const float* dirs, int rows_per_dir,
-                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas, const uint8_t* X0t) {
+                         int64_t M, float* rgb, uint8_t* wpack, cudaStream_t st, int max_ctas, const uint8_t* X0t,
+                         bool prepacked) {
   if (M == 0) return TVM_OK;
   const bool tiles = X0t != nullptr;
   const void* kern = tiles ? (const void*)fmlp::mlp_fwd_fused_kernel<true> : (const void*)fmlp::mlp_fwd_fused_kernel<false>;
@@ -877,8 +887,7 @@ int launch_mlp_fwd_fused(const MlpDims& d, const MlpWeights& w, const float* X0,
     set_error("fused mlp: packed weights, features and biases must be 16-byte aligned");
     return TVM_ERR_ALIGN;
   }
-  fmlp::pack_weights_kernel<<<64, 256, 0, st>>>(wpack, w.w0, w.w1, w.w2, w.w3);
-  TVM_TRY(check_launch("pack_weights"));
+  if (!prepacked) TVM_TRY(launch_mlp_pack_fused(w, wpack, st));
   fmlp::Args a{M, wpack, X0, X0t, dirs, rows_per_dir, w.w0, w.w1, w.b1, w.w2, w.b2, w.w3, w.b3, rgb};
   const int64_t ntiles = ceil_div(M, fmlp::BM);
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(max_ctas > 0 ? max_ctas : sms, 1));
