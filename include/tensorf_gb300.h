@@ -480,6 +480,19 @@ TVM_API int tvm_noise_fill(float* dst, int64_t n, uint64_t seed, uint64_t stream
  * into `step` before each replay. */
 TVM_API int tvm_noise_fill_keyed(float* dst, int64_t n, uint64_t seed, const tvm_step_scalars* step,
                                  uint64_t mul, uint64_t add, int32_t kind, void* stream);
+/* Up to TVM_NOISE_BATCH_MAX tvm_noise_fill_keyed draws of one seed in one launch (a
+ * training step's jitter, proposal jitter and Gumbel noise): each job is filled exactly as
+ * tvm_noise_fill_keyed fills it. */
+#define TVM_NOISE_BATCH_MAX 4
+typedef struct {
+  float* dst;
+  int64_t n;
+  uint64_t mul, add;
+  int32_t kind; /* 0 uniform [0, 1), 1 Gumbel */
+  int32_t _pad;
+} tvm_noise_job;
+TVM_API int tvm_noise_fill_keyed_batch(const tvm_noise_job* jobs, int32_t njobs, uint64_t seed,
+                                       const tvm_step_scalars* step, void* stream);
 /* Pinhole rays of one camera (cameras.py:100-143): K (3x3 row-major), R_wc (3x3),
  * t_wc (3): origins/directions (H*W, 3) float32, pixel (v, u) row-major. The
  * pixel subset `pixels` (n indices into H*W) may be NULL for the full frame. */

@@ -14,13 +14,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-// step (optional): the stream id is step->noise_stream * mul + add, read when it runs.
-__global__ void noise_kernel(float* __restrict__ dst, int64_t n, uint64_t seed, uint64_t sid, int kind,
-                             const tvm_step_scalars* __restrict__ step, uint64_t mul) {
-  if (step != nullptr) sid = step->noise_stream * mul + sid;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+// Elements [i0, n) step `stride` of the draw (seed, stream id sid): uniform [0, 1) or
+// Gumbel from 24 random bits of each element's hash.
+__device__ __forceinline__ void noise_range(float* __restrict__ dst, int64_t n, uint64_t seed, uint64_t sid, int kind,
+                                            int64_t i0, int64_t stride) {
   const uint64_t key = mix64(seed ^ mix64(sid + 0x9E3779B97F4A7C15ull));
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  for (int64_t i = i0; i < n; i += stride) {
     const uint64_t h = mix64(key + (uint64_t)i * 0xD1B54A32D192ED03ull);
     const uint32_t bits = (uint32_t)(h >> 40);  // 24 random bits
     if (kind == 0) {
@@ -30,6 +29,24 @@ __global__ void noise_kernel(float* __restrict__ dst, int64_t n, uint64_t seed, 
       dst[i] = -logf(-logf(u));
     }
   }
+}
+
+// step (optional): the stream id is step->noise_stream * mul + add, read when it runs.
+__global__ void noise_kernel(float* __restrict__ dst, int64_t n, uint64_t seed, uint64_t sid, int kind,
+                             const tvm_step_scalars* __restrict__ step, uint64_t mul) {
+  if (step != nullptr) sid = step->noise_stream * mul + sid;
+  noise_range(dst, n, seed, sid, kind, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+              (int64_t)gridDim.x * blockDim.x);
+}
+
+// Several keyed draws, one per blockIdx.y.
+struct NoiseBatch {
+  tvm_noise_job job[TVM_NOISE_BATCH_MAX];
+};
+__global__ void noise_batch_kernel(NoiseBatch b, uint64_t seed, const tvm_step_scalars* __restrict__ step) {
+  const tvm_noise_job& j = b.job[blockIdx.y];
+  noise_range(j.dst, j.n, seed, step->noise_stream * j.mul + j.add, j.kind,
+              (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 struct Cam {
@@ -141,6 +158,28 @@ int tvm_noise_fill(float* dst, int64_t n, uint64_t seed, uint64_t stream_id, int
   const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 16);
   noise_kernel<<<blocks, 256, 0, as_stream(stream)>>>(dst, n, seed, stream_id, kind, nullptr, 0);
   return check_launch("noise_fill");
+}
+
+int tvm_noise_fill_keyed_batch(const tvm_noise_job* jobs, int32_t njobs, uint64_t seed, const tvm_step_scalars* step,
+                               void* stream) {
+  TVM_REQUIRE(njobs >= 0 && njobs <= TVM_NOISE_BATCH_MAX, TVM_ERR_SHAPE, "njobs=%d outside [0, %d]", njobs,
+              TVM_NOISE_BATCH_MAX);
+  if (njobs == 0) return TVM_OK;
+  TVM_REQUIRE(jobs != nullptr && step != nullptr, TVM_ERR_INVALID, "NULL pointer");
+  TVM_REQUIRE(aligned(step, 8), TVM_ERR_ALIGN, "step must be 8-byte aligned");
+  NoiseBatch b{};
+  int64_t most = 0;
+  for (int q = 0; q < njobs; ++q) {
+    TVM_REQUIRE(jobs[q].n >= 0, TVM_ERR_SHAPE, "job %d: n < 0", q);
+    TVM_REQUIRE(jobs[q].kind == 0 || jobs[q].kind == 1, TVM_ERR_INVALID, "job %d: kind must be 0 or 1", q);
+    TVM_REQUIRE(jobs[q].n == 0 || jobs[q].dst != nullptr, TVM_ERR_INVALID, "job %d: dst is NULL", q);
+    b.job[q] = jobs[q];
+    most = std::max(most, jobs[q].n);
+  }
+  if (most == 0) return TVM_OK;
+  const dim3 grid((unsigned)std::min<int64_t>(ceil_div(most, 256), 152 * 16), (unsigned)njobs);
+  noise_batch_kernel<<<grid, 256, 0, as_stream(stream)>>>(b, seed, step);
+  return check_launch("noise_fill_batch");
 }
 
 int tvm_noise_fill_keyed(float* dst, int64_t n, uint64_t seed, const tvm_step_scalars* step, uint64_t mul,

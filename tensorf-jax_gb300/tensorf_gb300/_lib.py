@@ -75,6 +75,13 @@ class AdamDesc(ctypes.Structure):
                 ("pending_lr_decay", c_float)]
 
 
+class NoiseJob(ctypes.Structure):
+    _fields_ = [("dst", c_void_p), ("n", c_int64), ("mul", c_uint64), ("add", c_uint64), ("kind", c_int32),
+                ("_pad", c_int32)]
+
+
+NOISE_BATCH_MAX = 4
+
 # name -> (restype, argtypes)
 _SIGNATURES = {
     "tvm_abi_version": (c_int32, []),
@@ -105,7 +112,7 @@ _SIGNATURES = {
                                     c_void_p, c_void_p]),
     "tvm_proposal_bwd": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, POINTER(Rays),
                                    POINTER(RenderDesc), c_void_p, c_void_p, c_void_p]),
-    "tvm_loss_f64_workspace_size": (c_size_t,[POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
+    "tvm_loss_f64_workspace_size": (c_size_t, [POINTER(ModelDesc), POINTER(RenderDesc), c_int64]),
     "tvm_loss_f64": (c_int32, [POINTER(ModelDesc), c_void_p, POINTER(Rays), c_void_p, POINTER(RenderDesc), c_int64,
                                ctypes.c_double, c_void_p, c_void_p, c_size_t, c_void_p]),
     "tvm_resize_field": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
@@ -127,6 +134,7 @@ _SIGNATURES = {
     "tvm_apply_pending_fields": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                            POINTER(AdamDesc), c_void_p]),
     "tvm_noise_fill_keyed": (c_int32, [c_void_p, c_int64, c_uint64, c_void_p, c_uint64, c_uint64, c_int32, c_void_p]),
+    "tvm_noise_fill_keyed_batch": (c_int32, [POINTER(NoiseJob), c_int32, c_uint64, c_void_p, c_void_p]),
     "tvm_refresh_shadow": (c_int32, [POINTER(ModelDesc), c_void_p, c_void_p, c_void_p]),
     "tvm_l2_probe": (c_int32, [c_int32, c_void_p, c_size_t, c_int32, c_void_p]),
     "tvm_noise_fill": (c_int32, [c_void_p, c_int64, c_uint64, c_uint64, c_int32, c_void_p]),

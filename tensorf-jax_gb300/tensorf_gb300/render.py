@@ -338,11 +338,10 @@ def draw_noise_keyed(seed: int, step_scalars: torch.Tensor, rays: int, config: R
     tvm_set_step_scalars) when the kernels run. draw_noise's key splits are affine in s
     (split: s -> 2s+1, 2s+2), so each draw is one (mul, add) pair; a recorded training
     step therefore replays each step's own noise."""
-    sp = step_scalars.data_ptr()
+    jobs = []
 
     def fill(buf: torch.Tensor, mul: int, add: int, kind: int) -> None:
-        _lib.call("tvm_noise_fill_keyed", ptr(buf), buf.numel(), seed & (2**64 - 1), sp, mul, add, kind,
-                  stream_handle())
+        jobs.append(_lib.NoiseJob(dst=ptr(buf).value, n=buf.numel(), mul=mul, add=add, kind=kind))
 
     if config.mode is RenderMode.RGB:
         fill(out.gumbel, 2, 2, 1)           # rgb key 2s+2
@@ -351,6 +350,9 @@ def draw_noise_keyed(seed: int, step_scalars: torch.Tensor, rays: int, config: R
         fill(out.proposal_jitter, 4, 4, 0)  # and 4s+4
     else:
         fill(out.jitter, 2, 1, 0)           # sample key 2s+1
+    arr = (_lib.NoiseJob * len(jobs))(*jobs)  # one launch for all of the step's draws
+    _lib.call("tvm_noise_fill_keyed_batch", arr, len(jobs), seed & (2**64 - 1), step_scalars.data_ptr(),
+              stream_handle())
 
 
 # ---------------------------------------------------------------------------------

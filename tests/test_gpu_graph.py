@@ -7,7 +7,7 @@ graph path reads the Adam scalars and the noise key from device memory
 (tvm_set_step_scalars) and its batches are copied into fixed buffers. After several
 steps parameters and both moments agree to the order of the atomic gradient reductions
 (FP32: all but a handful of elements to 1e-5; BF16, where last-bit differences flip bf16
-roundings: within 3x of a second eager run's distance plus 2e-3 in norm), the logged
+roundings: within 3x of a second eager run's distance plus 1e-2 in norm), the logged
 learning rates are equal, the replays ran (and counted) their kernels, and a grid resize
 records a new graph.
 """
@@ -35,13 +35,14 @@ def _dist(x, y):
 
 def _bf16_close(d, d_eager):
     """BF16 runs drift apart chaotically: a last-bit difference flips a bf16 rounding
-    that every later gather reads. Two eager runs measured 4e-7 to 2e-5 apart (in norm)
-    after three steps and 1e-4 to 1e-3 after six, so one second run is a noisy
-    yardstick: the run under test may sit 3x further than it, plus 2e-3. A real ordering
-    fault (an update read before it lands, or applied twice) moves the parameters it
-    touches by a whole Adam step, about 1e-1 of their norm; the FP32 cases check the
-    same scheduling element by element."""
-    return d <= 3.0 * d_eager + 2e-3
+    (of a field value, or of a proposal feature, which can move a resampled bin) that
+    every later step reads. Runs of the same steps measured 4e-7 to 2e-5 apart (in norm)
+    after three steps and 1e-4 to 3e-3 after six, so one second run is a noisy yardstick:
+    the run under test may sit 3x further than it, plus 1e-2. A real ordering fault in
+    the BF16-only work (a field update whose bf16 shadow is not refreshed before the
+    gathers read it) moves every field parameter by a whole Adam step, about 1e-1 of
+    their norm; the FP32 cases check the shared scheduling element by element."""
+    return d <= 3.0 * d_eager + 1e-2
 
 
 def _states(cfg, spec, graphs=(False, True)):
