@@ -17,8 +17,8 @@ from ._util import ptr, stream_handle
 
 @dataclasses.dataclass
 class Rays3D:
-    """cameras.py:10-20. origins / directions (*, 3) float32; camera indices are only
-    used by FiLM camera embeddings, which this path does not implement."""
+    """cameras.py:10-20. origins / directions (*, 3) float32; camera_indices (*,) int32,
+    read by models with FiLM camera embeddings (networks.py:103-111)."""
     origins: torch.Tensor
     directions: torch.Tensor
     camera_indices: Optional[torch.Tensor] = None
