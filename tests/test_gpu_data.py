@@ -34,7 +34,10 @@ def test_blender_training_rays_match_oracle(tmp_path):
 
 
 @pytest.mark.parametrize("model", ["OPENCV", "OPENCV_FISHEYE"])
-def test_nerfstudio_rays_without_distortion_are_pinhole_rays(tmp_path, model):
+def test_nerfstudio_rays_without_distortion_coefficients(tmp_path, model):
+    """With all coefficients zero the pinhole model gives the pinhole rays; the fisheye
+    model is then the equidistant projection (image radius = angle off the axis), so a
+    pixel at normalised radius r has the ray at angle r."""
     import json
     from tensorf_gb300 import data
     meta = _nerfstudio_dataset(tmp_path, model)
@@ -48,6 +51,14 @@ def test_nerfstudio_rays_without_distortion_are_pinhole_rays(tmp_path, model):
     for i, cam in enumerate(ds.get_cameras()):
         sl = slice(i * n, (i + 1) * n)
         o, d = O.camera_pixel_rays(cam.K, cam.R_world_camera, cam.t_world_camera, meta["w"], meta["h"])
+        if model == "OPENCV_FISHEYE":
+            v, u = np.mgrid[:meta["h"], :meta["w"]]
+            x = (u.ravel() - cam.K[0, 2]) / cam.K[0, 0]
+            y = (v.ravel() - cam.K[1, 2]) / cam.K[1, 1]
+            r = np.sqrt(x * x + y * y)
+            s = np.where(r > 0, np.tan(r) / np.maximum(r, 1e-30), 1.0)
+            c = np.stack([x * s, y * s, np.ones_like(x)], axis=-1)
+            d = (c / np.linalg.norm(c, axis=-1, keepdims=True)) @ cam.R_world_camera.T
         np.testing.assert_allclose(rr.rays_wrt_world.directions[sl].cpu().numpy(), d, atol=1e-6)
         np.testing.assert_allclose(rr.rays_wrt_world.origins[sl].cpu().numpy(), o, atol=1e-6)
         img = data.read_png(tmp_path / f"f{i}.png")
