@@ -199,3 +199,69 @@ def test_nerfstudio_preset_matches_reference_defaults():
     G = spec.grid_dim
     assert lay.appearance_lines - lay.density_lines >= 3 * 32 * G * (G + 1)
 
+
+
+def _proposal_render(**kw):
+    rd = _lib.RenderDesc(density_samples=48, appearance_samples=7, mode=_lib.TVM_MODE_RGB,
+                         sampler=_lib.TVM_SAMPLER_PROPOSAL, proposal_samples=64)
+    for i, v in enumerate((-1.5, -1.5, -1.5, 1.5, 1.5, 1.5)):
+        rd.aabb[i] = v
+    rd.proposal_jitter = 0x1000
+    rd.jitter = 0x2000
+    for k, v in kw.items():
+        setattr(rd, k, v)
+    return rd
+
+
+def test_proposal_seam_argument_checks():
+    """Each proposal seam rejects bad arguments with its code before any launch."""
+    lib = _lib.load()
+    rays = _lib.Rays(count=4, origins=0x1000, directions=0x2000)
+    p16 = ctypes.c_void_p(0x1000)
+    no_prop = _model()
+    with_prop = _model(proposal_grid=16, proposal_rank=4, proposal_units=64)
+    rd = _proposal_render()
+    # forward: a model without a proposal network, a wrong sampler, too many bins, no jitter
+    assert lib.tvm_proposal_fwd(ctypes.byref(no_prop), p16, None, ctypes.byref(rays), ctypes.byref(rd), p16, p16,
+                                None) == -1
+    bad = _proposal_render(sampler=_lib.TVM_SAMPLER_BBOX)
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), p16, None, ctypes.byref(rays), ctypes.byref(bad), p16, p16,
+                                None) == -1
+    bad = _proposal_render(proposal_samples=513)
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), p16, None, ctypes.byref(rays), ctypes.byref(bad), p16, p16,
+                                None) == -2
+    bad = _proposal_render(proposal_jitter=None)
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), p16, None, ctypes.byref(rays), ctypes.byref(bad), p16, p16,
+                                None) == -1
+    bad = _proposal_render(contract=1)  # unbounded bins need the caller's edges
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), p16, None, ctypes.byref(rays), ctypes.byref(bad), p16, p16,
+                                None) == -1
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), ctypes.c_void_p(0x1004), None, ctypes.byref(rays),
+                                ctypes.byref(rd), p16, p16, None) == -4
+    # resample: main samples past 512, missing outputs
+    bad = _proposal_render(density_samples=513)
+    assert lib.tvm_proposal_resample(ctypes.byref(rays), ctypes.byref(bad), p16, p16, p16, p16, None) == -2
+    assert lib.tvm_proposal_resample(ctypes.byref(rays), ctypes.byref(rd), p16, None, p16, p16, None) == -1
+    # loss: bin counts, NULL buffers; backward: unaligned gradients
+    assert lib.tvm_proposal_loss(p16, p16, p16, 4, 1, 48, ctypes.c_float(1.0), None, p16, None) == -2
+    assert lib.tvm_proposal_loss(p16, None, p16, 4, 64, 48, ctypes.c_float(1.0), None, p16, None) == -1
+    assert lib.tvm_proposal_bwd(ctypes.byref(with_prop), p16, None, ctypes.c_void_p(0x1008), ctypes.byref(rays),
+                                ctypes.byref(rd), p16, p16, None) == -4
+    # zero rays: nothing to do
+    none = _lib.Rays(count=0, origins=None, directions=None)
+    assert lib.tvm_proposal_fwd(ctypes.byref(with_prop), p16, None, ctypes.byref(none), ctypes.byref(rd), None, None,
+                                None) == 0
+    assert lib.tvm_proposal_loss(None, None, None, 0, 64, 48, ctypes.c_float(1.0), None, None, None) == 0
+
+
+def test_noise_batch_argument_checks():
+    lib = _lib.load()
+    jobs = (_lib.NoiseJob * 5)()
+    assert lib.tvm_noise_fill_keyed_batch(jobs, 5, 1, ctypes.c_void_p(0x1000), None) == -2
+    assert lib.tvm_noise_fill_keyed_batch(jobs, 0, 1, None, None) == 0
+    jobs[0].n, jobs[0].kind = 8, 2
+    assert lib.tvm_noise_fill_keyed_batch(jobs, 1, 1, ctypes.c_void_p(0x1000), None) == -1
+    jobs[0].kind, jobs[0].dst = 0, None
+    assert lib.tvm_noise_fill_keyed_batch(jobs, 1, 1, ctypes.c_void_p(0x1000), None) == -1
+    jobs[0].dst = 0x1000
+    assert lib.tvm_noise_fill_keyed_batch(jobs, 1, 1, ctypes.c_void_p(0x1004), None) == -4
