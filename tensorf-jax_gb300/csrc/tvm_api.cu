@@ -479,15 +479,15 @@ static int run_pass(const tvm_model_desc& m, const float* params, const void* sh
   phase_mark(0, st);
   if (proposal) {
     // Proposal network forward, then resampling into explicit main samples.
-    // Features and the 16-U-1 MLP in one kernel; X and h are kept only for the backward.
+    // Features and the 16-U-1 MLP in one kernel (the proposal backward recomputes them).
     const FieldView fp = proposal_field(m, L, params, shadow);
     const PropMlp pm{m.proposal_units, params + L.proposal_w1, params + L.proposal_b1, params + L.proposal_w2,
                      params + L.proposal_b2, c.proposal_shift, nullptr, b.sig_p};
     TVM_TRY(launch_prop_features(fp, rays.origins, rays.directions, R, sp, edges, c.proposal_jitter, nullptr,
                                  b.delta_p, &pm, st));
-    TVM_TRY(launch_segment_fwd(b.sig_p, b.delta_p, R, c.proposal_samples, nullptr, b.w_p, st));
-    TVM_TRY(launch_resample(b.w_p, rays.origins, rays.directions, R, sp, edges, c.density_samples, c.jitter,
-                            b.t_main, b.d_main, b.bins, st));
+    // The proposal weights (kept in w_p for the bound loss) and the resampling, one launch.
+    TVM_TRY(launch_resample(nullptr, rays.origins, rays.directions, R, sp, edges, c.density_samples, c.jitter,
+                            b.t_main, b.d_main, b.bins, st, b.sig_p, b.delta_p, b.w_p));
     s = SamplerArgs{};
     s.sampler = TVM_SAMPLER_EXPLICIT;
     s.N = c.density_samples;

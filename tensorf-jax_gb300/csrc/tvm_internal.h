@@ -167,9 +167,11 @@ int launch_prop_features(const FieldView& f, const float* origins, const float* 
 int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const float* origins, const float* dirs,
                     int64_t R, const SamplerArgs& s, const float* edges, const float* jitter, const float* dz,
                     const PropMlp& mlp, float* gw1, float* gb1, float* gw2, float* gb2, cudaStream_t st);
+// Resampling of the proposal weights wprop (R, Np), or (sig set) of the weights of the
+// bin densities sig and lengths len, which are then written to w_out.
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                     const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
-                    cudaStream_t st);
+                    cudaStream_t st, const float* sig = nullptr, const float* len = nullptr, float* w_out = nullptr);
 int launch_prop_loss(const float* wmain, const float* wprop, const int32_t* bins, int64_t R, int Np, int Nm,
                      float scale, float* loss, float* gprop, cudaStream_t st);
 

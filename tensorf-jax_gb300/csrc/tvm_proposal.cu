@@ -389,7 +389,12 @@ __global__ void __launch_bounds__(PBWD_THREADS) prop_bwd_kernel(
 // Resampling, one warp per ray: histogram q_j = w^_j + (0.01 * sum w^ + 1e-4) / Np over
 // the Np bins, main edges at the quantiles i/N (i = 0..N) by linear interpolation
 // inside the bin, one main sample per interval at edge_i + jitter * length.
-__global__ void resample_kernel(const float* __restrict__ wprop, const float* __restrict__ origins,
+// WEIGHTS: the proposal weights are computed here from the bin densities and lengths,
+// with segment_fwd_kernel's arithmetic, and written to wprop (one launch fewer on the
+// pass's critical path); otherwise wprop is read.
+template <bool WEIGHTS>
+__global__ void resample_kernel(float* __restrict__ wprop, const float* __restrict__ sig,
+                                const float* __restrict__ len, const float* __restrict__ origins,
                                 const float* __restrict__ dirs, int64_t R, SamplerArgs s, const float* __restrict__ edges,
                                 int Nm, const float* __restrict__ jitter, float* __restrict__ t_out,
                                 float* __restrict__ d_out, int32_t* __restrict__ bins) {
@@ -402,15 +407,39 @@ __global__ void resample_kernel(const float* __restrict__ wprop, const float* __
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
   if (r >= R) return;
   RayGeom g = load_ray(origins, dirs, r, s);
+  // cdf[j + 1] holds bin j's weight until the scan below replaces it.
   float tot = 0.f;
-  for (int j = lane; j < Np; j += 32) tot += __ldg(wprop + r * Np + j);
+  if (WEIGHTS) {
+    float carry_s = 0.f;
+    for (int base = 0; base < Np; base += 32) {
+      const int j = base + lane;
+      const bool valid = j < Np;
+      const float sv = valid ? -__ldg(sig + r * Np + j) * __ldg(len + r * Np + j) : 0.f;
+      const float incl = warp_inclusive_scan(sv, lane) + carry_s;
+      const float prev = __shfl_up_sync(0xffffffffu, incl, 1);
+      const float excl = (lane == 0) ? carry_s : prev;
+      if (valid) {
+        const float w = -expm1f(sv) * expf(excl);
+        wprop[r * Np + j] = w;
+        cdf[j + 1] = w;
+        tot += w;
+      }
+      carry_s = __shfl_sync(0xffffffffu, incl, 31);
+    }
+  } else {
+    for (int j = lane; j < Np; j += 32) {
+      cdf[j + 1] = __ldg(wprop + r * Np + j);
+      tot += cdf[j + 1];
+    }
+  }
   tot = warp_sum(tot);
   const float floor_w = (0.01f * tot + 1e-4f) / (float)Np;
   float carry = 0.f;
+  __syncwarp();
   if (lane == 0) cdf[0] = 0.f;
   for (int base = 0; base < Np; base += 32) {
     const int j = base + lane;
-    const float q = (j < Np) ? __ldg(wprop + r * Np + j) + floor_w : 0.f;
+    const float q = (j < Np) ? cdf[j + 1] + floor_w : 0.f;
     const float incl = warp_inclusive_scan(q, lane) + carry;
     if (j < Np) cdf[j + 1] = incl;
     carry = __shfl_sync(0xffffffffu, incl, 31);
@@ -974,12 +1003,17 @@ int launch_prop_bwd(const FieldView& f, float* glines, float* gplanes, const flo
 
 int launch_resample(const float* wprop, const float* origins, const float* dirs, int64_t R, const SamplerArgs& s,
                     const float* edges, int Nm, const float* jitter, float* t_out, float* d_out, int32_t* bins,
-                    cudaStream_t st) {
+                    cudaStream_t st, const float* sig, const float* len, float* w_out) {
   if (R == 0) return TVM_OK;
   const int warps = 4;
   const size_t smem = (size_t)warps * (2 * (s.N + 1) + (Nm + 1)) * sizeof(float);
-  resample_kernel<<<(unsigned)ceil_div(R, warps), warps * 32, smem, st>>>(wprop, origins, dirs, R, s, edges, Nm, jitter,
-                                                                          t_out, d_out, bins);
+  const unsigned grid = (unsigned)ceil_div(R, warps);
+  if (sig)
+    resample_kernel<true><<<grid, warps * 32, smem, st>>>(w_out, sig, len, origins, dirs, R, s, edges, Nm, jitter, t_out,
+                                                          d_out, bins);
+  else
+    resample_kernel<false><<<grid, warps * 32, smem, st>>>(const_cast<float*>(wprop), nullptr, nullptr, origins, dirs,
+                                                           R, s, edges, Nm, jitter, t_out, d_out, bins);
   return check_launch("resample");
 }
 
