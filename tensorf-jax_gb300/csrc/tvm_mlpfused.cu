@@ -4,13 +4,15 @@
 // Persistent CTAs (one per SM, 256 threads). The four weight matrices are staged once
 // per CTA into shared memory as bf16 B operands (K-major canonical layout, N padded to
 // a multiple of 16, K to a multiple of 16). Per 128-row tile:
-//   X0 (fp32, global) -> bf16 A tile -> MMA L0 (N=32, K=144) -> TMEM D0
+//   X0 -> bf16 A tile (one bulk copy of an input tile, or fp32 rows through registers)
+//      -> MMA L0 (N=32, K=144) -> TMEM D0
 //   tcgen05.ld D0 -> Fourier encoding in registers -> bf16 X1 tile (K=160)
 //   MMA L1 (N=128, K=160) -> D1 -> +b1, ReLU -> bf16 H1 tile (reuses the X0 tile)
 //   MMA L2 (N=128, K=128) -> D2 -> +b2, ReLU -> bf16 H2 tile (reuses the X1 tile)
 //   MMA L3 (N=16,  K=128) -> D3 -> +b3, sigmoid -> rgb (global)
-// Activations never leave the SM (the fused backward recomputes them). One elected thread issues the MMAs and commits to an
-// mbarrier; every wait is bounded and reports through the device status word.
+// Activations never leave the SM (the fused backward recomputes them). One elected thread
+// issues the MMAs and commits to an mbarrier; every wait is bounded and reports through
+// the device status word.
 #include "tvm_internal.h"
 #include "tvm_tc.cuh"
 
