@@ -186,7 +186,7 @@ def test_bf16_render_and_gradients_match_rounding_mirror(monkeypatch):
     g = lp.to_reference(grads)
     got = {f"{grp}.{nm}": g[grp][i] for grp in ("density", "appearance") for i, nm in enumerate(("vector", "matrix"))}
     got.update({f"{layer}.{nm}": g["mlp"][layer][nm] for layer in g["mlp"] for nm in g["mlp"][layer]})
-    errs = {"render": _nrel(img, out), "loss": abs(loss - float(L)) / float(L)}
+    errs = {"render": _nrel(img, out), "loss": abs(loss - float(L.detach())) / float(L.detach())}
     errs.update({name: _nrel(got[name], want[name]) for name in want})
     plain = {name: _nrel(got[name], want_plain[name]) for name in want}
     print("vs mirror", {k_: f"{v:.1e}" for k_, v in errs.items()})

@@ -115,7 +115,7 @@ def _check_parity(G, o, d, c, N, k, shift, seed, min_keep):
     L = O.mse(out, c.double())
     L.backward()
     assert _rel_err(img, out) < RTOL, _rel_err(img, out)
-    assert abs(loss - float(L)) <= RTOL * float(L), (loss, float(L))
+    assert abs(loss - float(L.detach())) <= RTOL * float(L.detach()), (loss, float(L.detach()))
     g = lp.to_reference(grads)
     pairs = {"density.vector": (g["density"][0], ref64["density"][0].grad),
              "density.matrix": (g["density"][1], ref64["density"][1].grad),

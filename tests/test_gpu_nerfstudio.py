@@ -112,7 +112,7 @@ def test_preset_render_and_gradients_match_oracle():
     L = O.mse(out, c.double())
     L.backward()
     assert _rel(img, out) < RTOL, _rel(img, out)
-    assert abs(loss - float(L)) <= RTOL * float(L), (loss, float(L))
+    assert abs(loss - float(L.detach())) <= RTOL * float(L.detach()), (loss, float(L.detach()))
     g = lp.to_reference(grads)
     errs = {f"{grp}.{i}": _rel(g[grp][i], ref64[grp][i].grad) for grp in ("density", "appearance") for i in (0, 1)}
     errs.update({f"{layer}.{nm}": _rel(g["mlp"][layer][nm], ref64["mlp"][layer][nm].grad)

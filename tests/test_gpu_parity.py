@@ -271,7 +271,7 @@ def test_loss_and_grad_matches_oracle_autograd(tg):
                         density_shift=shift)
     L = O.mse(out, c.double())
     L.backward()
-    assert abs(float(loss.item()) - float(L)) <= RTOL * float(L)
+    assert abs(float(loss.item()) - float(L.detach())) <= RTOL * float(L.detach())
     g = lp.to_reference(grads)
     pairs = [(g["density"][0], ref64["density"][0].grad), (g["density"][1], ref64["density"][1].grad),
              (g["appearance"][0], ref64["appearance"][0].grad), (g["appearance"][1], ref64["appearance"][1].grad)]

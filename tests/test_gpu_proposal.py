@@ -117,7 +117,7 @@ def test_proposal_gradients_match_oracle():
     lprop = O.proposal_loss(aux["p_terminates"], wp, bins, 3.0)
     assert lprop.item() > 0.0  # the untrained proposal does not bound the field yet
     (mse + lprop).backward()
-    assert abs(float(loss.item()) - float(mse)) <= RTOL * float(mse)
+    assert abs(float(loss.item()) - float(mse.detach())) <= RTOL * float(mse.detach())
     g = lp.to_reference(grads)
     pairs = [(g["density"][0], ref64["density"][0].grad), (g["density"][1], ref64["density"][1].grad),
              (g["appearance"][0], ref64["appearance"][0].grad), (g["appearance"][1], ref64["appearance"][1].grad)]

@@ -87,8 +87,8 @@ def test_proposal_loss_seam_matches_oracle():
     wp64 = wp_t.double().requires_grad_(True)
     want = O.proposal_loss(wm_t.double(), wp64, b_t.long(), weight)
     want.backward()
-    assert float(want) > 0.0
-    assert abs(float(loss.item()) - float(want)) <= RTOL * float(want)
+    assert float(want.detach()) > 0.0
+    assert abs(float(loss.item()) - float(want.detach())) <= RTOL * float(want.detach())
     assert _rel(g, wp64.grad) < RTOL
 
 
