@@ -7,9 +7,9 @@ as CUDA tensors, the rays built on the device by ``Camera.pixel_rays_wrt_world``
 or from the undistorted pixel directions (nerfstudio).
 
 The reference reads images with PIL and undistorts and resizes with OpenCV. Neither is
-a dependency here: PNG files are decoded by ``read_png`` (zlib and the five PNG row
-filters, PNG specification 1.2, section 6) and other formats need PIL when it is
-installed; undistortion restates the OpenCV pinhole (Brown-Conrady k1, k2, p1, p2) and
+a dependency here: images are read through PIL where it is installed, and without it PNG
+files are decoded by ``read_png`` (zlib and the five PNG row filters, PNG specification
+1.2, section 6); undistortion restates the OpenCV pinhole (Brown-Conrady k1, k2, p1, p2) and
 fisheye (Kannala-Brandt k1..k4) models and inverts them iteratively as
 ``cv2.undistortPoints`` and ``cv2.fisheye.undistortPoints`` do; the resize is bilinear
 with half-pixel centres, as ``cv2.resize`` with its default interpolation.
@@ -43,16 +43,18 @@ _PNG_CHANNELS = {0: 1, 2: 3, 4: 2, 6: 4}  # colour type -> samples per pixel
 
 
 def _unfilter_row(ftype: int, row: bytearray, prev: bytes, bpp: int) -> None:
-    """Undo one PNG row filter in place (PNG 1.2 section 6.3)."""
+    """Undo one PNG row filter in place (PNG 1.2 section 6.3). Sub and Up are running sums
+    and sums over the row (numpy); Average and Paeth depend on the byte just decoded, one
+    byte at a time."""
     n = len(row)
     if ftype == 0:
         return
-    if ftype == 1:  # Sub
-        for i in range(bpp, n):
-            row[i] = (row[i] + row[i - bpp]) & 0xFF
+    if ftype == 1:  # Sub: per channel, a running sum mod 256 along the row
+        a = onp.frombuffer(bytes(row), dtype=onp.uint8).reshape(-1, bpp).astype(onp.uint32)
+        row[:] = (onp.cumsum(a, axis=0) & 0xFF).astype(onp.uint8).tobytes()
     elif ftype == 2:  # Up
-        for i in range(n):
-            row[i] = (row[i] + prev[i]) & 0xFF
+        row[:] = ((onp.frombuffer(bytes(row), dtype=onp.uint8).astype(onp.uint16) +
+                   onp.frombuffer(prev, dtype=onp.uint8)) & 0xFF).astype(onp.uint8).tobytes()
     elif ftype == 3:  # Average
         for i in range(n):
             left = row[i - bpp] if i >= bpp else 0
@@ -109,15 +111,18 @@ def read_png(path: Union[str, pathlib.Path]) -> onp.ndarray:
 
 
 def read_image(path: Union[str, pathlib.Path]) -> onp.ndarray:
-    """An image file as uint8 (H, W, C): PNGs decoded here, other formats through PIL."""
+    """An image file as uint8 (H, W, C), through PIL where it is installed (as the
+    reference reads them, data.py:344-354); without PIL, PNG files are decoded here."""
     path = pathlib.Path(path)
-    if path.read_bytes()[:8] == _PNG_SIGNATURE:
-        return read_png(path)
     try:
         import PIL.Image
-    except ImportError as e:
-        raise RuntimeError(f"{path}: only PNG images can be read without PIL") from e
-    return onp.array(PIL.Image.open(path))
+    except ImportError:
+        PIL = None
+    if PIL is not None:
+        return onp.array(PIL.Image.open(path))
+    if path.read_bytes()[:8] == _PNG_SIGNATURE:
+        return read_png(path)
+    raise RuntimeError(f"{path}: only PNG images can be read without PIL")
 
 
 def resize_bilinear(image: onp.ndarray, width: int, height: int) -> onp.ndarray:
