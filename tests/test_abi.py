@@ -265,3 +265,16 @@ def test_noise_batch_argument_checks():
     assert lib.tvm_noise_fill_keyed_batch(jobs, 1, 1, ctypes.c_void_p(0x1000), None) == -1
     jobs[0].dst = 0x1000
     assert lib.tvm_noise_fill_keyed_batch(jobs, 1, 1, ctypes.c_void_p(0x1004), None) == -4
+
+
+def test_proposal_descriptor_from_python():
+    """render._proposal_desc: the seams' descriptor (host logic only)."""
+    from tensorf_gb300 import render
+    prop = render.ProposalConfig(samples=32, shift=0.25, loss_weight=2.0)
+    d = render._proposal_desc(((-1.0, -2.0, -3.0), (1.0, 2.0, 3.0)), prop, 10, False, None, samples=24)
+    assert d.sampler == _lib.TVM_SAMPLER_PROPOSAL and d.proposal_samples == 32 and d.density_samples == 24
+    assert abs(d.proposal_shift - 0.25) < 1e-7 and abs(d.proposal_loss_weight - 2.0) < 1e-7 and d.contract == 0
+    assert list(d.aabb) == [-1.0, -2.0, -3.0, 1.0, 2.0, 3.0]
+    assert not d.schedule and not d.proposal_jitter and not d.jitter
+    with pytest.raises(ValueError):  # unbounded bins need the caller's edges
+        render._proposal_desc(((-2.0,) * 3, (2.0,) * 3), prop, 10, True, None)
